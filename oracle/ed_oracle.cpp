@@ -1,0 +1,825 @@
+// ORACLE — test infrastructure, not product code.
+//
+// CPU restatement of the LSQuantumED hot path (fixed-Sz basis -> Heisenberg
+// J1-J2 Hamiltonian -> Krylov-Schur -> correlations / DSF coefficients).  Only
+// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
+// may load it, and only as the checker or the timed CPU baseline.  Nothing in
+// the lsquantumed_gb300 package calls it.
+//
+// Every function cites the reference file:line it restates.  Parity is pinned
+// by the reference's own golden tests (tests/unit_tests/**), extracted into
+// tests/golden/*.json by tests/golden/make_golden.py.
+//
+// Conventions that follow the reference exactly:
+//   * states are bit strings, bit i = site i is "up"; basis in ascending
+//     numeric order (Gosper enumeration, src/basis.cpp:192-215);
+//   * rank = combinadic index (src/hamiltonian.cpp:9-27) computed with exact
+//     integer binomials (the reference sums Boost double binomials and rounds;
+//     both are exact for every N <= 50);
+//   * matrix elements: off-diagonal J*0.5 per antiparallel bond, duplicates
+//     summed in nn-pass-then-nnn-pass order (include/hamiltonian.tmpl_func.hpp
+//     :229-344); diagonal Delta*0.25*E per bond type (ibid :129-225); disorder
+//     diagonal Delta1*0.25*E_nn + Delta2*0.25*E_nnn + 0.5*sum(+-h_i) (ibid
+//     :97-125, src/hamiltonian.cpp:31-49).
+#include <cstdint>
+#include <cstring>
+#include <cmath>
+#include <complex>
+#include <vector>
+#include <algorithm>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <omp.h>
+
+typedef std::complex<double> cplx;
+
+// --------------------------------------------------------------------------
+// Exact binomials C(n,k), n <= 64.
+// --------------------------------------------------------------------------
+static uint64_t g_binom[65][65];
+static bool g_binom_ready = false;
+static void binom_init() {
+  if (g_binom_ready) return;
+  for (int n = 0; n <= 64; ++n) {
+    g_binom[n][0] = 1;
+    for (int k = 1; k <= 64; ++k)
+      g_binom[n][k] = (n == 0) ? 0 : g_binom[n - 1][k - 1] + g_binom[n - 1][k];
+  }
+  g_binom_ready = true;
+}
+static inline uint64_t binom(int n, int k) {
+  if (k < 0 || n < 0 || k > n) return 0;
+  return g_binom[n][k];
+}
+
+extern "C" {
+
+// src/basis.cpp:38-46 — dim = C(N, nup) as a floating product rounded.
+int64_t orc_compute_size(int nspins, int nspins_up) {
+  double size = 1.0;
+  for (int64_t i = 1; i <= (nspins - nspins_up); ++i)
+    size *= ((double)(i + nspins_up) / (double)i);
+  return (int64_t)std::floor(size + 0.5);
+}
+
+// src/basis.cpp:9-36 — unrank: greedy from the top bit.
+uint64_t orc_search_elem(int64_t index, int nspins, int nspins_up) {
+  binom_init();
+  int64_t pi = nspins - 1;
+  int64_t rest = index;
+  uint64_t elem = 0;
+  int64_t sup = nspins_up;
+  while (sup > 0) {
+    uint64_t b = (pi < sup) ? 0 : binom((int)pi, (int)sup);
+    if ((int64_t)b <= rest) {
+      rest -= (int64_t)b;
+      elem |= (1ull << pi);
+      sup -= 1;
+    }
+    pi -= 1;
+  }
+  return elem;
+}
+
+// src/hamiltonian.cpp:9-27 — rank: sum over set bits p (k-th from the bottom,
+// k = 1..) of C(p, k), skipped when p < k.
+int64_t orc_search_index(uint64_t state, int nspins) {
+  binom_init();
+  int64_t spinup_index = 0;
+  uint64_t index = 0;
+  for (int bit = 0; bit < nspins; ++bit) {
+    if ((state >> bit) & 1ull) {
+      ++spinup_index;
+      if (!(bit < spinup_index)) index += binom(bit, (int)spinup_index);
+    }
+  }
+  return (int64_t)index;
+}
+
+// src/basis.cpp:66-80 — validation and the block row split.  Returns 0 on
+// success, 1 on |mag| > N/2, 2 on size < mpi_size.
+int orc_basis_layout(int nspins, int total_mag, int mpi_size, int mpi_rank,
+                     int64_t* size, int64_t* local_size, int64_t* global_start) {
+  if (total_mag > nspins / 2 || total_mag < -nspins / 2) return 1;
+  int nup = total_mag + nspins / 2;
+  int64_t sz = orc_compute_size(nspins, nup);
+  if (sz < mpi_size) return 2;
+  int64_t rest = sz % mpi_size;
+  int64_t ls = sz / mpi_size + (rest > mpi_rank);
+  int64_t gs = (int64_t)mpi_rank * ls + (rest <= mpi_rank) * rest;
+  *size = sz; *local_size = ls; *global_start = gs;
+  return 0;
+}
+
+// src/basis.cpp:192-215 — first element by unranking, then Gosper's hack.
+void orc_generate_basis(int nspins, int nspins_up, int64_t start, int64_t count, uint64_t* out) {
+  if (count <= 0) return;
+  uint64_t elem = orc_search_elem(start, nspins, nspins_up);
+  out[0] = elem;
+  for (int64_t i = 1; i < count; ++i) {
+    uint64_t u = elem & (0 - elem);
+    uint64_t v = u + elem;
+    elem = (((v ^ elem) / u) >> 2) + v;
+    out[i] = elem;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Lattices: src/lattice.cpp:27-264.  Output tables use the reference layout:
+// rows of (site, neigh_1..neigh_num) with stride num+1, plus per-site counts.
+// type 0 = chain1D, 1 = square2D, 2 = honeycomb2D.
+// Returns 0, or 1 on lx*ly != N, 2 on odd honeycomb dims.
+// --------------------------------------------------------------------------
+int orc_lattice(int type, int nspins, int lx, int ly,
+                int64_t* nn, int64_t* nnXsite, int* num_nn,
+                int64_t* nnn, int64_t* nnnXsite, int* num_nnn) {
+  std::vector<int64_t> a, b, ax, bx;
+  if (type == 0) {
+    // lattice.cpp:27-53
+    for (int64_t i = 0; i < nspins; ++i) { a.push_back(i); a.push_back((i + 1) % nspins); ax.push_back(1); }
+    for (int64_t i = 0; i < nspins; ++i) { b.push_back(i); b.push_back((i + 2) % nspins); bx.push_back(1); }
+    *num_nn = 1; *num_nnn = 1;
+  } else if (type == 1) {
+    if ((int64_t)lx * ly != nspins) return 1;
+    // lattice.cpp:86-108
+    for (int64_t ix = 0; ix < lx; ++ix)
+      for (int64_t iy = 0; iy < ly; ++iy) {
+        a.push_back(ix * ly + iy);
+        a.push_back(ix * ly + (iy + 1) % ly);
+        a.push_back(((ix + 1) % lx) * ly + iy);
+        ax.push_back(2);
+      }
+    // lattice.cpp:112-136
+    for (int64_t ix = 0; ix < lx; ++ix)
+      for (int64_t iy = 0; iy < ly; ++iy) {
+        b.push_back(ix * ly + iy);
+        b.push_back(((ix + 1) % lx) * ly + (iy + 1) % ly);
+        b.push_back(((ix + 1) % lx) * ly + (iy - 1 + ly) % ly);
+        bx.push_back(2);
+      }
+    *num_nn = 2; *num_nnn = 2;
+  } else if (type == 2) {
+    if ((int64_t)lx * ly != nspins) return 1;
+    if (lx % 2 != 0 || ly % 2 != 0) return 2;
+    // lattice.cpp:172-231
+    for (int64_t ix = 0; ix < lx; ++ix)
+      for (int64_t iy = 0; iy < ly; ++iy) {
+        int64_t cur = ix * ly + iy;
+        a.push_back(cur);
+        bool two = (ix % 2 == 0) ? (cur % 2 == 0) : (cur % 2 != 0);
+        a.push_back(ix * ly + (iy + 1) % ly);
+        if (two) { a.push_back(((ix + 1) % lx) * ly + iy); ax.push_back(2); }
+        else { a.push_back(-1); ax.push_back(1); }
+      }
+    // lattice.cpp:235-264
+    for (int64_t ix = 0; ix < lx; ++ix)
+      for (int64_t iy = 0; iy < ly; ++iy) {
+        b.push_back(ix * ly + iy);
+        bx.push_back(3);
+        b.push_back(ix * ly + (iy + 2) % ly);
+        b.push_back(((ix + 1) % lx) * ly + (iy + 1) % ly);
+        b.push_back(((ix + 1) % lx) * ly + (iy - 1 + ly) % ly);
+      }
+    *num_nn = 2; *num_nnn = 3;
+  } else {
+    return 3;
+  }
+  std::copy(a.begin(), a.end(), nn);
+  std::copy(ax.begin(), ax.end(), nnXsite);
+  std::copy(b.begin(), b.end(), nnn);
+  std::copy(bx.begin(), bx.end(), nnnXsite);
+  return 0;
+}
+
+}  // extern "C"
+
+// A lattice in the reference's table form.
+struct Lat {
+  int nspins = 0, num_nn = 0, num_nnn = 0;
+  std::vector<int64_t> nn, nnX, nnn, nnnX;
+};
+
+static Lat make_lat(int type, int nspins, int lx, int ly) {
+  Lat L; L.nspins = nspins;
+  L.nn.resize(4 * nspins); L.nnX.resize(nspins); L.nnn.resize(4 * nspins); L.nnnX.resize(nspins);
+  int rc = orc_lattice(type, nspins, lx, ly, L.nn.data(), L.nnX.data(), &L.num_nn,
+                       L.nnn.data(), L.nnnX.data(), &L.num_nnn);
+  if (rc) throw std::invalid_argument("bad lattice");
+  return L;
+}
+
+// include/hamiltonian.tmpl_func.hpp:391-426 with src/hamiltonian.cpp:53-68.
+static int64_t elem_diag(int nt, uint64_t s, const Lat& L) {
+  int64_t d = 0;
+  const std::vector<int64_t>& tab = nt == 0 ? L.nn : L.nnn;
+  const std::vector<int64_t>& cnt = nt == 0 ? L.nnX : L.nnnX;
+  int num = nt == 0 ? L.num_nn : L.num_nnn;
+  for (int64_t i = 0; i < L.nspins; ++i)
+    for (int64_t ng = 1; ng <= cnt[i]; ++ng) {
+      int64_t off = (int64_t)(num + 1) * i;
+      short spin = (short)tab[off + ng];
+      uint64_t a = (s >> i) & 1ull, b = (s >> spin) & 1ull;
+      d += (a ^ b) ? -1 : 1;
+    }
+  return d;
+}
+
+// include/hamiltonian.tmpl_func.hpp:350-387 with src/hamiltonian.cpp:72-99.
+static void coup_elems(int nt, uint64_t s, const Lat& L, std::vector<int64_t>& out) {
+  out.clear();
+  const std::vector<int64_t>& tab = nt == 0 ? L.nn : L.nnn;
+  const std::vector<int64_t>& cnt = nt == 0 ? L.nnX : L.nnnX;
+  int num = nt == 0 ? L.num_nn : L.num_nnn;
+  for (int64_t i = 0; i < L.nspins; ++i)
+    for (int64_t ng = 1; ng <= cnt[i]; ++ng) {
+      int64_t off = (int64_t)(num + 1) * i;
+      short spin = (short)tab[off + ng];
+      uint64_t a = (s >> i) & 1ull, b = (s >> spin) & 1ull;
+      if (a ^ b) {
+        uint64_t sw = s ^ (1ull << i);
+        sw ^= (1ull << spin);
+        out.push_back(orc_search_index(sw, L.nspins));
+      }
+    }
+}
+
+// src/hamiltonian.cpp:31-49 — sequential sum over sites.
+static double disorder_elem(uint64_t s, int nspins, const double* hi) {
+  double d = 0;
+  for (int i = 0; i < nspins; ++i) {
+    if ((s >> i) & 1ull) d += hi[i]; else d -= hi[i];
+  }
+  return d;
+}
+
+extern "C" {
+
+int64_t orc_get_elem_diag(int type, int nspins, int lx, int ly, int nt, uint64_t state) {
+  Lat L = make_lat(type, nspins, lx, ly);
+  return elem_diag(nt, state, L);
+}
+
+// Columns for local row `local_index` of rank `mpi_rank` out of `mpi_size`
+// (the reference tests index int_basis locally).  Returns ncol.
+int orc_get_coup_elems(int type, int nspins, int lx, int ly, int total_mag, int mpi_size, int mpi_rank,
+                       int nt, int64_t local_index, int64_t* out) {
+  int64_t size, ls, gs;
+  if (orc_basis_layout(nspins, total_mag, mpi_size, mpi_rank, &size, &ls, &gs)) return -1;
+  if (local_index < 0 || local_index >= ls) return -2;
+  Lat L = make_lat(type, nspins, lx, ly);
+  int nup = total_mag + nspins / 2;
+  uint64_t s = orc_search_elem(gs + local_index, nspins, nup);
+  std::vector<int64_t> cols;
+  coup_elems(nt, s, L, cols);
+  std::copy(cols.begin(), cols.end(), out);
+  return (int)cols.size();
+}
+
+double orc_get_disorder_elem(uint64_t state, int nspins, const double* hi) {
+  return disorder_elem(state, nspins, hi);
+}
+
+// src/tools/random_disorder.cpp:33-49 — seeds; reprod uses mt19937_64(1),
+// otherwise std::random_device.  PetscInt is 64-bit in the reference build.
+void orc_rd_seeds(int reprod, int64_t rep, int64_t* out) {
+  std::uniform_int_distribution<int64_t> dist(0, 1000);
+  if (!reprod) {
+    std::random_device rd;
+    std::mt19937_64 g(rd());
+    for (int64_t i = 0; i < rep; ++i) out[i] = dist(g);
+  } else {
+    std::mt19937_64 g(1);
+    for (int64_t i = 0; i < rep; ++i) out[i] = dist(g);
+  }
+}
+
+// src/tools/random_disorder.cpp:53-59 — h_i ~ U(min, max) from mt19937_64(seed).
+void orc_rd_hi(int64_t seed, int nspins, double mn, double mx, double* hi) {
+  std::mt19937_64 g((uint64_t)seed);
+  std::uniform_real_distribution<double> dist(mn, mx);
+  for (int i = 0; i < nspins; ++i) hi[i] = dist(g);
+}
+
+// Seeded N(0,1) draws from mt19937_64(seed) (std::normal_distribution), used
+// for per-bond coupling disorder J_ij = base*(1 + 0.1*N(0,1)).
+void orc_normal(int64_t seed, int64_t n, double* out) {
+  std::mt19937_64 g((uint64_t)seed);
+  std::normal_distribution<double> dist(0.0, 1.0);
+  for (int64_t i = 0; i < n; ++i) out[i] = dist(g);
+}
+
+}  // extern "C"
+
+// --------------------------------------------------------------------------
+// Model: basis + bonds + couplings; explicit CSR in the reference layout
+// (int64 columns, complex128 values, columns sorted per row as PETSc AIJ
+// stores them).
+// --------------------------------------------------------------------------
+struct OrcModel {
+  int nspins = 0, nup = 0;
+  int64_t dim = 0;
+  std::vector<uint64_t> states;
+  Lat lat;
+  bool per_bond = false;
+  // uniform couplings (reference)
+  double J1 = 0, D1 = 0, J2 = 0, D2 = 0;
+  // per-bond couplings: bond (i, j) with J, D (generalisation for gradients)
+  std::vector<int> bi, bj;
+  std::vector<double> bJ, bD;
+  // CSR
+  std::vector<int64_t> rowptr, cols;
+  std::vector<cplx> vals;
+  std::vector<double> diag;  // diagonal as assembled
+};
+
+// flags: 1 = build_diag, 2 = build_off_diag, 4 = build_disorder(hi).
+static void build_csr(OrcModel& M, int flags, const double* hi) {
+  const int64_t dim = M.dim;
+  M.rowptr.assign(dim + 1, 0);
+  M.diag.assign(dim, 0.0);
+  // count pass + fill pass, per row (rows are independent)
+  std::vector<std::vector<std::pair<int64_t, double>>> rows(dim);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t r = 0; r < dim; ++r) {
+    uint64_t s = M.states[r];
+    std::vector<std::pair<int64_t, double>>& row = rows[r];
+    std::vector<int64_t> cols;
+    auto add = [&](int64_t c, double v) {
+      for (auto& e : row) if (e.first == c) { e.second += v; return; }
+      row.push_back({c, v});
+    };
+    double dval = 0.0;
+    bool has_diag = false;
+    if (!M.per_bond) {
+      // build_diag: tmpl_func.hpp:129-225 (ADD_VALUES onto zeroed entry)
+      if ((flags & 1) && !(std::fabs(M.D1) < 1e-14 && std::fabs(M.D2) < 1e-14)) {
+        if (std::fabs(M.D1) >= 1e-14) {
+          int64_t t = elem_diag(0, s, M.lat);
+          if (t != 0) { dval += M.D1 * 0.25 * t; has_diag = true; }
+        }
+        if (std::fabs(M.D2) >= 1e-14) {
+          int64_t t = elem_diag(1, s, M.lat);
+          if (t != 0) { dval += M.D2 * 0.25 * t; has_diag = true; }
+        }
+      }
+      if ((flags & 4) && hi) {
+        // build_disorder: tmpl_func.hpp:97-125 (INSERT_VALUES replaces)
+        int64_t t1 = elem_diag(0, s, M.lat), t2 = elem_diag(1, s, M.lat);
+        dval = M.D1 * 0.25 * t1 + M.D2 * 0.25 * t2 + 0.5 * disorder_elem(s, M.nspins, hi);
+        has_diag = true;
+      }
+      if (has_diag) add(r, dval);
+      // build_off_diag: tmpl_func.hpp:229-344 — nn pass, then nnn pass
+      if ((flags & 2) && std::fabs(M.J1) >= 1e-14) {
+        coup_elems(0, s, M.lat, cols);
+        for (int64_t c : cols) add(c, M.J1 * 0.5);
+      }
+      if ((flags & 2) && std::fabs(M.J2) >= 1e-14) {
+        coup_elems(1, s, M.lat, cols);
+        for (int64_t c : cols) add(c, M.J2 * 0.5);
+      }
+    } else {
+      // per-bond generalisation: diag = sum_b D_b*0.25*(+-1) + 0.5*sum(+-h_i),
+      // off-diagonal J_b*0.5 per antiparallel bond, in bond order.
+      for (size_t b = 0; b < M.bi.size(); ++b) {
+        uint64_t a = (s >> M.bi[b]) & 1ull, c = (s >> M.bj[b]) & 1ull;
+        dval += M.bD[b] * 0.25 * ((a ^ c) ? -1.0 : 1.0);
+      }
+      if ((flags & 4) && hi) dval += 0.5 * disorder_elem(s, M.nspins, hi);
+      add(r, dval); has_diag = true;
+      for (size_t b = 0; b < M.bi.size(); ++b) {
+        uint64_t a = (s >> M.bi[b]) & 1ull, c = (s >> M.bj[b]) & 1ull;
+        if (a ^ c) {
+          uint64_t sw = s ^ (1ull << M.bi[b]) ^ (1ull << M.bj[b]);
+          add(orc_search_index(sw, M.nspins), M.bJ[b] * 0.5);
+        }
+      }
+    }
+    std::sort(row.begin(), row.end(), [](const std::pair<int64_t, double>& x, const std::pair<int64_t, double>& y) {
+      return x.first < y.first;
+    });
+    for (auto& e : row) if (e.first == r) M.diag[r] = e.second;
+  }
+  for (int64_t r = 0; r < dim; ++r) M.rowptr[r + 1] = M.rowptr[r] + (int64_t)rows[r].size();
+  M.cols.resize(M.rowptr[dim]);
+  M.vals.resize(M.rowptr[dim]);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < dim; ++r) {
+    int64_t o = M.rowptr[r];
+    for (auto& e : rows[r]) { M.cols[o] = e.first; M.vals[o] = cplx(e.second, 0.0); ++o; }
+  }
+}
+
+// CSR SpMV, y = H x (OpenMP over rows).
+static void spmv(const OrcModel& M, const cplx* x, cplx* y) {
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < M.dim; ++r) {
+    cplx acc(0, 0);
+    for (int64_t k = M.rowptr[r]; k < M.rowptr[r + 1]; ++k) acc += M.vals[k] * x[M.cols[k]];
+    y[r] = acc;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Deterministic start vector: re, im ~ U[-1, 1) from a counter hash, so the
+// same vector is produced bit-for-bit on any host or device.
+// --------------------------------------------------------------------------
+static inline uint64_t splitmix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static inline double u01(uint64_t h) { return (double)(h >> 11) * (1.0 / 9007199254740992.0); }
+static void start_vector(uint64_t seed, int64_t n, cplx* v) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    uint64_t h1 = splitmix64(seed * 0xD1B54A32D192ED03ull + 2 * (uint64_t)i);
+    uint64_t h2 = splitmix64(seed * 0xD1B54A32D192ED03ull + 2 * (uint64_t)i + 1);
+    v[i] = cplx(2.0 * u01(h1) - 1.0, 2.0 * u01(h2) - 1.0);
+  }
+}
+
+// --------------------------------------------------------------------------
+// Small dense symmetric eigensolver (cyclic Jacobi), ascending order.
+// A is m x m row-major (destroyed); Y receives eigenvectors as columns.
+// --------------------------------------------------------------------------
+static void jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, std::vector<double>& Y) {
+  Y.assign((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) Y[(size_t)i * m + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0, tot = 0;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        double a = A[(size_t)i * m + j] * A[(size_t)i * m + j];
+        tot += a; if (i != j) off += a;
+      }
+    if (off <= 1e-32 * tot || off == 0.0) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        double apq = A[(size_t)p * m + q];
+        if (apq == 0.0) continue;
+        double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
+        double tau = (aqq - app) / (2.0 * apq);
+        double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+        for (int k = 0; k < m; ++k) {
+          double akp = A[(size_t)k * m + p], akq = A[(size_t)k * m + q];
+          A[(size_t)k * m + p] = c * akp - s * akq;
+          A[(size_t)k * m + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          double apk = A[(size_t)p * m + k], aqk = A[(size_t)q * m + k];
+          A[(size_t)p * m + k] = c * apk - s * aqk;
+          A[(size_t)q * m + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          double ykp = Y[(size_t)k * m + p], ykq = Y[(size_t)k * m + q];
+          Y[(size_t)k * m + p] = c * ykp - s * ykq;
+          Y[(size_t)k * m + q] = s * ykp + c * ykq;
+        }
+      }
+  }
+  std::vector<int> idx(m);
+  for (int i = 0; i < m; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return A[(size_t)a * m + a] < A[(size_t)b * m + b]; });
+  theta.resize(m);
+  std::vector<double> Ys((size_t)m * m);
+  for (int c = 0; c < m; ++c) {
+    theta[c] = A[(size_t)idx[c] * m + idx[c]];
+    for (int r = 0; r < m; ++r) Ys[(size_t)r * m + c] = Y[(size_t)r * m + idx[c]];
+  }
+  Y.swap(Ys);
+}
+
+// --------------------------------------------------------------------------
+// Krylov-Schur for Hermitian operators (lowest eigenvalues), the CPU
+// counterpart of the device solver: thick-restart Lanczos with full
+// classical Gram-Schmidt and one conditional refinement (eta = 1/sqrt(2)),
+// convergence on the relative residual estimate |beta*y_m|/|theta| <= tol,
+// restart keeping nconv + max(1, (m - nconv)/2) Ritz vectors.  This restates
+// the published Krylov-Schur method (Stewart 2001) that SLEPc's EPS
+// KRYLOVSCHUR implements for EPS_HEP (src/solver.cpp:7-24 configures it).
+// --------------------------------------------------------------------------
+struct KSResult {
+  std::vector<double> evals, errs;
+  std::vector<cplx> evecs;  // n x nconv, column-major
+  int nconv = 0, its = 0;
+  int64_t nhv = 0;
+};
+
+template <class Apply>
+static void ks_solve(int64_t n, Apply apply, int nev, int ncv, int mpd, double tol, int max_it,
+                     uint64_t seed, KSResult& R, int want_vecs) {
+  (void)mpd;
+  if (ncv <= 0) ncv = std::max(2 * nev, nev + 15);
+  if (ncv > n) ncv = (int)n;
+  if (nev > ncv) nev = ncv;
+  if (tol <= 0) tol = 1e-8;
+  if (max_it <= 0) max_it = std::max<int64_t>(100, 2 * n / std::max(ncv, 1));
+  const int m = ncv;
+  std::vector<cplx> V((size_t)(m + 1) * n), w(n);
+  std::vector<double> alpha(m + 1, 0.0), beta(m + 1, 0.0), arrow(m + 1, 0.0);
+  start_vector(seed, n, V.data());
+  auto dotc = [&](const cplx* a, const cplx* b) {  // a^H b
+    double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+      cplx t = std::conj(a[i]) * b[i];
+      re += t.real(); im += t.imag();
+    }
+    return cplx(re, im);
+  };
+  auto nrm = [&](const cplx* a) { return std::sqrt(dotc(a, a).real()); };
+  {
+    double nv = nrm(V.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) V[i] /= nv;
+  }
+  uint64_t rseed = seed + 0x51ED2701ull;
+  // Orthogonalise w against V[0..j] (CGS + refinement if needed); returns h.
+  auto orthog = [&](int j, std::vector<cplx>& h, double& nw, double& norig) {
+    h.assign(j + 1, cplx(0, 0));
+    double n0 = nrm(w.data());
+    norig = n0;
+    for (int pass = 0; pass < 2; ++pass) {
+      std::vector<cplx> c(j + 1);
+      for (int i = 0; i <= j; ++i) c[i] = dotc(&V[(size_t)i * n], w.data());
+#pragma omp parallel for schedule(static)
+      for (int64_t r = 0; r < n; ++r) {
+        cplx acc = w[r];
+        for (int i = 0; i <= j; ++i) acc -= V[(size_t)i * n + r] * c[i];
+        w[r] = acc;
+      }
+      for (int i = 0; i <= j; ++i) h[i] += c[i];
+      nw = nrm(w.data());
+      if (nw >= 0.7071067811865476 * n0) break;
+      n0 = nw;
+    }
+  };
+  int k = 0;      // expansion start (kept vectors)
+  int nconv = 0;
+  std::vector<double> theta, Y;
+  std::vector<cplx> h;
+  int its = 0;
+  bool done = false;
+  while (!done) {
+    ++its;
+    for (int j = k; j < m; ++j) {
+      apply(&V[(size_t)j * n], w.data());
+      R.nhv++;
+      double nw, norig;
+      orthog(j, h, nw, norig);
+      alpha[j] = h[j].real();
+      if (nw <= 1e-13 * norig) {
+        // invariant subspace: continue with a random vector orthogonal to V
+        start_vector(rseed++, n, w.data());
+        double nw2, no2;
+        std::vector<cplx> h2;
+        orthog(j, h2, nw2, no2);
+        for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = w[r] / nw2;
+        beta[j] = 0.0;
+      } else {
+        for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = w[r] / nw;
+        beta[j] = nw;
+      }
+    }
+    // projected matrix: arrow (rows 0..k-1 coupled to k) + tridiagonal
+    std::vector<double> T((size_t)m * m, 0.0);
+    for (int i = 0; i < k; ++i) {
+      T[(size_t)i * m + i] = alpha[i];
+      T[(size_t)i * m + k] = T[(size_t)k * m + i] = arrow[i];
+    }
+    for (int j = k; j < m; ++j) {
+      T[(size_t)j * m + j] = alpha[j];
+      if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = beta[j];
+    }
+    jacobi_eig(m, T, theta, Y);
+    double bm = beta[m - 1];
+    nconv = 0;
+    for (int i = 0; i < m; ++i) {
+      double res = std::fabs(bm * Y[(size_t)(m - 1) * m + i]);
+      double rel = res / std::max(std::fabs(theta[i]), 1e-300);
+      if (rel < tol) nconv++; else break;
+    }
+    if (nconv >= nev || its >= max_it) done = true;
+    int l;
+    if (done) l = std::min(m, std::max(nconv, nev));
+    else {
+      l = nconv + std::max(1, (m - nconv) / 2);
+      if (l > m - 1) l = m - 1;
+    }
+    // V[:, 0..l) = V[:, 0..m) * Y[:, 0..l)
+    {
+      std::vector<cplx> Vn((size_t)l * n);
+#pragma omp parallel for schedule(static)
+      for (int64_t r = 0; r < n; ++r)
+        for (int c = 0; c < l; ++c) {
+          cplx acc(0, 0);
+          for (int i = 0; i < m; ++i) acc += V[(size_t)i * n + r] * Y[(size_t)i * m + c];
+          Vn[(size_t)c * n + r] = acc;
+        }
+      std::copy(Vn.begin(), Vn.end(), V.begin());
+    }
+    if (done) {
+      R.nconv = std::min(nconv, l);
+      R.evals.assign(theta.begin(), theta.begin() + l);
+      R.errs.assign(l, 0.0);
+      // true relative residuals ||H x - theta x|| / |theta|
+      for (int c = 0; c < l; ++c) {
+        apply(&V[(size_t)c * n], w.data());
+        double nx = nrm(&V[(size_t)c * n]);
+        double rr = 0;
+#pragma omp parallel for reduction(+ : rr) schedule(static)
+        for (int64_t r = 0; r < n; ++r) rr += std::norm(w[r] - theta[c] * V[(size_t)c * n + r]);
+        R.errs[c] = std::sqrt(rr) / std::max(std::fabs(theta[c]) * nx, 1e-300);
+      }
+      if (want_vecs) R.evecs.assign(V.begin(), V.begin() + (size_t)l * n);
+      break;
+    }
+    // V[l] = V[m]; arrow couplings; kept Ritz values on the diagonal
+    std::copy(V.begin() + (size_t)m * n, V.begin() + (size_t)(m + 1) * n, V.begin() + (size_t)l * n);
+    for (int i = 0; i < l; ++i) { alpha[i] = theta[i]; arrow[i] = bm * Y[(size_t)(m - 1) * m + i]; }
+    k = l;
+  }
+  R.its = its;
+}
+
+extern "C" {
+
+void* orc_model_create(int ltype, int nspins, int lx, int ly, int total_mag,
+                       double J1, double D1, double J2, double D2) {
+  binom_init();
+  OrcModel* M = new OrcModel();
+  M->nspins = nspins;
+  M->nup = total_mag + nspins / 2;
+  M->dim = orc_compute_size(nspins, M->nup);
+  M->states.resize(M->dim);
+  orc_generate_basis(nspins, M->nup, 0, M->dim, M->states.data());
+  try { M->lat = make_lat(ltype, nspins, lx, ly); } catch (...) { delete M; return nullptr; }
+  M->J1 = J1; M->D1 = D1; M->J2 = J2; M->D2 = D2;
+  return M;
+}
+
+// Per-bond model: bonds (i_b, j_b) with couplings J_b, D_b.
+void* orc_model_create_bonds(int nspins, int total_mag, int64_t nb, const int32_t* pairs,
+                             const double* J, const double* D) {
+  binom_init();
+  OrcModel* M = new OrcModel();
+  M->nspins = nspins;
+  M->nup = total_mag + nspins / 2;
+  M->dim = orc_compute_size(nspins, M->nup);
+  M->states.resize(M->dim);
+  orc_generate_basis(nspins, M->nup, 0, M->dim, M->states.data());
+  M->per_bond = true;
+  for (int64_t b = 0; b < nb; ++b) {
+    M->bi.push_back(pairs[2 * b]); M->bj.push_back(pairs[2 * b + 1]);
+    M->bJ.push_back(J[b]); M->bD.push_back(D[b]);
+  }
+  return M;
+}
+
+void orc_model_destroy(void* m) { delete (OrcModel*)m; }
+int64_t orc_model_dim(void* m) { return ((OrcModel*)m)->dim; }
+void orc_model_states(void* m, uint64_t* out) {
+  OrcModel* M = (OrcModel*)m;
+  std::copy(M->states.begin(), M->states.end(), out);
+}
+void orc_set_threads(int nt) { if (nt > 0) omp_set_num_threads(nt); }
+int orc_get_threads() { return omp_get_max_threads(); }
+
+// Build the explicit matrix; flags as build_csr (the reference drivers use
+// 1|2, or 2|4 with disorder).  Returns nnz.
+int64_t orc_model_build(void* m, int flags, const double* hi) {
+  OrcModel* M = (OrcModel*)m;
+  build_csr(*M, flags, hi);
+  return M->rowptr[M->dim];
+}
+void orc_model_csr(void* m, int64_t* rowptr, int64_t* cols, double* vals_re) {
+  OrcModel* M = (OrcModel*)m;
+  std::copy(M->rowptr.begin(), M->rowptr.end(), rowptr);
+  std::copy(M->cols.begin(), M->cols.end(), cols);
+  for (size_t k = 0; k < M->vals.size(); ++k) vals_re[k] = M->vals[k].real();
+}
+void orc_model_diag(void* m, double* out) {
+  OrcModel* M = (OrcModel*)m;
+  std::copy(M->diag.begin(), M->diag.end(), out);
+}
+// y = H x, interleaved complex128.
+void orc_model_apply(void* m, const double* x, double* y) {
+  OrcModel* M = (OrcModel*)m;
+  spmv(*M, (const cplx*)x, (cplx*)y);
+}
+void orc_start_vector(uint64_t seed, int64_t n, double* v) { start_vector(seed, n, (cplx*)v); }
+
+// Krylov-Schur on the explicit matrix.  evals/errs sized >= ncv; evecs
+// (nullable) n x ncv complex column-major.  Returns the number of Ritz pairs
+// reported (>= nconv).
+int orc_eps_solve(void* m, int nev, int ncv, int mpd, double tol, int max_it, uint64_t seed,
+                  double* evals, double* errs, double* evecs, int* nconv, int* its, int64_t* nhv) {
+  OrcModel* M = (OrcModel*)m;
+  KSResult R;
+  auto ap = [&](const cplx* x, cplx* y) { spmv(*M, x, y); };
+  ks_solve(M->dim, ap, nev, ncv, mpd, tol, max_it, seed, R, evecs != nullptr);
+  int l = (int)R.evals.size();
+  for (int i = 0; i < l; ++i) { evals[i] = R.evals[i]; errs[i] = R.errs[i]; }
+  if (evecs) std::copy(R.evecs.begin(), R.evecs.end(), (cplx*)evecs);
+  *nconv = R.nconv; *its = R.its; *nhv = R.nhv;
+  return l;
+}
+
+// --------------------------------------------------------------------------
+// Correlations: src/spinOperators/correlation.cpp.  op: 0 SzSz, 1 SpSm,
+// 2 SmSp, 3 SiSj.  Result = VecDot(state, O state) = sum_s psi_s *
+// conj((O psi)_s)  (PETSc VecDot(x, y) = y^H x).
+// --------------------------------------------------------------------------
+static cplx expect_op(const OrcModel& M, int op, int i, int j, const cplx* psi) {
+  const int64_t dim = M.dim;
+  double re = 0, im = 0;
+  if (op == 3) {
+    // correlation.cpp:276-299
+    cplx e = expect_op(M, 1, i, j, psi);
+    e += expect_op(M, 2, i, j, psi);
+    e /= 2.0;
+    e += expect_op(M, 0, i, j, psi);
+    return e;
+  }
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+  for (int64_t r = 0; r < dim; ++r) {
+    uint64_t s = M.states[r];
+    uint64_t a = (s >> i) & 1ull, b = (s >> j) & 1ull;
+    cplx rhs(0, 0);
+    bool set = false;
+    if (op == 0) {
+      // correlation.cpp:86-139: copy, scale 0.25, times +-1
+      rhs = psi[r] * 0.25;
+      rhs *= (a ^ b) ? -1.0 : 1.0;
+      set = true;
+    } else {
+      // correlation.cpp:154-178 (SpSm), 237-261 (SmSp): row r takes
+      // psi[rank(swapped)], value 1.0
+      bool sw;
+      if (i == j) sw = (op == 1) ? (a == 1) : (a == 0);
+      else sw = (op == 1) ? (a == 0 && b == 1) : (a == 1 && b == 0);
+      if (sw) {
+        uint64_t t = (i == j) ? s : (s ^ (1ull << i) ^ (1ull << j));
+        rhs = psi[orc_search_index(t, M.nspins)];
+        set = true;
+      }
+    }
+    if (set) {
+      cplx t = psi[r] * std::conj(rhs);
+      re += t.real(); im += t.imag();
+    }
+  }
+  return cplx(re, im);
+}
+
+void orc_expect(void* m, int op, int i, int j, const double* psi, double* out) {
+  cplx e = expect_op(*(OrcModel*)m, op, i, j, (const cplx*)psi);
+  out[0] = e.real(); out[1] = e.imag();
+}
+
+// S^z_i |psi> as Sqz::OpOnStateVector (include/spinOperators/spinOPft.tmpl_func.hpp:28-60):
+// copy, scale 0.5, times (+1 if bit set else -1).
+void orc_sqz(void* m, int spin, const double* psi, double* rhs) {
+  OrcModel* M = (OrcModel*)m;
+  const cplx* p = (const cplx*)psi; cplx* o = (cplx*)rhs;
+  for (int64_t r = 0; r < M->dim; ++r) {
+    cplx v = p[r] * 0.5;
+    double val = 1.0;
+    if (!((M->states[r] >> spin) & 1ull)) val *= -1.0;
+    o[r] = v * val;
+  }
+}
+
+// S^+_i |psi> from sector m (model m0) into sector m+1 (model m1), as
+// Sqp::OpOnStateVector (spinOPft.tmpl_func.hpp:77-143): ADD_VALUES of psi
+// at rank(s ^ (1<<i)) for every state with bit i clear.
+void orc_sqp(void* m0, void* m1, int spin, const double* psi, double* rhs) {
+  OrcModel* A = (OrcModel*)m0; OrcModel* B = (OrcModel*)m1;
+  const cplx* p = (const cplx*)psi; cplx* o = (cplx*)rhs;
+  for (int64_t r = 0; r < B->dim; ++r) o[r] = 0;
+  for (int64_t r = 0; r < A->dim; ++r) {
+    uint64_t s = A->states[r];
+    if (!((s >> spin) & 1ull)) {
+      int64_t t = orc_search_index(s ^ (1ull << spin), B->nspins);
+      o[t] += p[r];
+    }
+  }
+}
+
+// PETSc VecDot(x, y) = y^H x.
+void orc_vecdot(int64_t n, const double* x, const double* y, double* out) {
+  const cplx* a = (const cplx*)x; const cplx* b = (const cplx*)y;
+  double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    cplx t = a[i] * std::conj(b[i]);
+    re += t.real(); im += t.imag();
+  }
+  out[0] = re; out[1] = im;
+}
+
+}  // extern "C"
