@@ -1,0 +1,414 @@
+#!/usr/bin/env python3
+"""Benchmark: N=30 (6x5 square, J1=1, J2=0.55, Delta=1, Sz=0) Krylov-Schur
+eigensolve, lowest 4 eigenpairs, ncv=16, eps_tol=1e-9, matrix-free H.v.
+
+One step = one full eigensolve (start vector to converged eigenpairs) with the
+Hamiltonian resident in HBM.  Prints one JSON line (see the keys below).
+
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--workload c5|c2|c1]
+
+--impl reference times the CPU restatement of the reference path (the oracle
+port; the PETSc/SLEPc reference cannot be built here) on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'eigensolve s & H·v GB/s at N=30; disorder samples/s batched vs plain @res1e-9'
+
+WORKLOADS = {
+    # name: (lattice, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol)
+    'c5': ('square2D', 30, 6, 5, 1.0, 1.0, 0.55, 0.55, 0, 4, 16, 1e-9),
+    'c2': ('square2D', 20, 4, 5, 1.0, 1.0, 0.5, 0.5, 0, 10, 0, 1e-9),
+    'c1': ('chain1D', 16, 1, 16, 1.0, 1.0, 0.0, 0.0, 0, 1, 0, 1e-9),
+}
+# H.v applications the Krylov-Schur run needs on each workload (seed 0), as
+# measured by the device run; the CPU restatement runs the same algorithm from
+# the same start vector, so its count is the same.  Used only to extrapolate
+# the bounded CPU sample of the reference arm.
+NHV = {}
+
+
+def _rank_info():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rk = int(os.environ.get('RANK', '0'))
+    lr = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rk, lr
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def kbar(N, nup, pairs):
+    """Mean off-diagonal entries per row: sum over distinct bonds of
+    P(bond antiparallel) = 2 C(N-2, nup-1) / C(N, nup)."""
+    masks = {(min(i, j), max(i, j)) for i, j in pairs if i != j}
+    p = 2 * math.comb(N - 2, nup - 1) / math.comb(N, nup)
+    return len(masks) * p
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix='.csv')
+            os.close(fd)
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.device), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': []}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(',')]
+            if len(f) < 8:
+                continue
+            try:
+                rows.append((float(f[0]), float(f[1]), f[4], f[5], f[6], f[7]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = sorted(r[0] for r in rows)
+        out['sm_mhz'] = sm[len(sm) // 2]
+        out['sm_max_mhz'] = max(r[1] for r in rows)
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for k, nm in enumerate(names):
+            if any(r[2 + k].lower().startswith('active') for r in rows):
+                out['reasons'].append(nm)
+        out['samples'] = len(rows)
+        return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port on the host cores, bounded sample.
+# ---------------------------------------------------------------------------
+class CpuSample:
+    """CSR SpMV (int64 columns, complex128 values, the reference's matrix
+    layout) and one CGS pass over 12 vectors on all host threads, at the
+    largest size of the same family whose explicit matrix fits host memory
+    (N=24 4x6 for the N=30 workload).  Per-row costs are scaled to the
+    workload's basis and multiplied by the solver's H.v count.  The matrix
+    build is setup, not timed (as the device run excludes its own setup)."""
+
+    def __init__(self, wl):
+        import numpy as np
+        import oracle
+        self.wl = wl
+        ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+        self.N, self.mag = N, mag
+        self.sN, self.slx, self.sly = (24, 4, 6) if N > 24 else (N, lx, ly)
+        self.lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
+        self.M = oracle.Model(self.lt, self.sN, self.slx, self.sly, 0, J1, D1, J2, D2)
+        self.nnz = self.M.build(3)
+        n = self.M.dim
+        self.x = oracle.start_vector(1, n)
+        self.V = np.ascontiguousarray(np.stack([oracle.start_vector(10 + i, n) for i in range(12)]))
+        self.w = oracle.start_vector(2, n)
+        nn, nnn = oracle.bond_pairs(self.lt, N, lx, ly)
+        self.nnz_row_f = 1 + kbar(N, mag + N // 2, list(map(tuple, nn)) + (list(map(tuple, nnn)) if J2 else []))
+        self.M.apply(self.x)  # warm
+
+    def run(self, nhv, budget_s=8.0):
+        import oracle
+        n = self.M.dim
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            self.M.apply(self.x)
+            reps += 1
+            if time.perf_counter() - t0 > budget_s / 2 or reps >= 50:
+                break
+        t_spmv = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        creps = 0
+        while True:
+            oracle.cgs_step(self.V, self.w)
+            creps += 1
+            if time.perf_counter() - t0 > budget_s / 4 or creps >= 20:
+                break
+        t_cgs = (time.perf_counter() - t0) / creps
+        full_dim = math.comb(self.N, self.mag + self.N // 2)
+        nnz_row_s = self.nnz / n
+        t_hv_full = t_spmv * (full_dim / n) * (self.nnz_row_f / nnz_row_s)
+        # CGS with one refinement: two passes per step over ~12 vectors on average
+        t_step = t_hv_full + 2 * t_cgs * (full_dim / n)
+        return {
+            'value': t_step * nhv, 'unit': 's', 'cores': oracle.get_threads(), 'kind': 'port',
+            'sample': ('N=%d %dx%d explicit-CSR SpMV (%d reps, %.4f s each) + CGS pass over 12 vectors '
+                       '(%.4f s), scaled to N=%d rows (x%.2f) and nnz/row (x%.3f), times %d H.v per solve'
+                       % (self.sN, self.slx, self.sly, reps, t_spmv, t_cgs, self.N, full_dim / n,
+                          self.nnz_row_f / nnz_row_s, nhv)),
+        }
+
+
+def run_reference(args):
+    ws, rk, lr = _rank_info()
+    if rk != 0:
+        return 0
+    wl = args.workload
+    import oracle
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    nhv = NHV.get(wl)
+    times = []
+    res = None
+    sample = CpuSample(wl) if N > 24 else None
+    for step in range(args.warmup + args.steps):
+        if sample is not None:
+            res = sample.run(nhv or 300)
+        else:
+            t0 = time.perf_counter()
+            lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
+            M = oracle.Model(lt, N, lx, ly, mag, J1, D1, J2, D2)
+            M.build(3)
+            r = M.eps_solve(nev=nev, ncv=ncv, tol=tol, seed=0, vectors=False)
+            res = {'value': time.perf_counter() - t0, 'unit': 's', 'cores': oracle.get_threads(), 'kind': 'port',
+                   'sample': 'full CPU eigensolve (CSR build + Krylov-Schur), nhv=%d' % r['nhv']}
+        if step >= args.warmup:
+            times.append(res['value'])
+    v = sum(times) / len(times)
+    res['value'] = v
+    line = {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': v * 1e3, 'higher_is_better': False, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'c128', 'data': 'synthetic',
+            'config': workload_config(wl), 'impl': 'reference', 'cpu_baseline': res,
+            'e2e': {'value': v, 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(wl):
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    return {'workload': '%s %s N=%d (%dx%d) J1=%g J2=%g Delta=1 Sz=%d: lowest %d eigenpairs, ncv=%s, eps_tol=%g, '
+                        'matrix-free complex128 H.v' % (wl, ltype, N, lx, ly, J1, J2, mag, nev, ncv or 'decide', tol),
+            'nspins': N, 'lattice': ltype, 'lx': lx, 'ly': ly, 'J1': J1, 'J2': J2, 'Delta': 1.0, 'sz': mag,
+            'nev': nev, 'ncv': ncv, 'eps_tol': tol, 'dim': math.comb(N, mag + N // 2), 'seed': 0,
+            'l2': 'inputs larger than L2 (each vector %.2f GB)' % (16 * math.comb(N, mag + N // 2) / 1e9)}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from lsquantumed_gb300.build import build
+    build()
+    import lsquantumed_gb300 as ed
+
+    ws, rk, lr = _rank_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    torch.cuda.set_device(lr)
+    wl = args.workload
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    env = ed.Environment(nspins=N, device=lr)
+    b = ed.Basis(env, mag)
+    lat = ed.square2D(env, lx, ly) if ltype == 'square2D' else ed.chain1D(env)
+    H = ed.Hamiltonian(env, b, lat, J1, D1, J2, D2)
+    H.build_diag(env)
+    H.build_off_diag(env)
+    dim = b.size
+
+    def one_solve():
+        eps = ed.Solver.SolverInit(H, nev, ncv if ncv else ed.PETSC_DEFAULT)
+        ed.Solver.EPSSetTolerances(eps, tol, 0)
+        nconv = ed.Solver.solve(env, eps)
+        return eps, nconv
+
+    for _ in range(args.warmup):
+        eps, _ = one_solve()
+        ed.Solver.SolverClean(eps)
+    stream = torch.cuda.current_stream()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(lr)
+    sampler.start()
+    k0 = env.kernel_count()
+    env.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    last = None
+    for _ in range(args.steps):
+        if last is not None:
+            ed.Solver.SolverClean(last[0])
+        last = one_solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    n_hv, ms_hv = env.profile_read()
+    env.profile(False)
+    launches = env.kernel_count() - k0
+    eps, nconv = last
+    st = eps.stats()
+    evals, errs = [], []
+    for i in range(min(nev, st['nreported'])):
+        e, err = ed.Solver.eigenvalue(eps, i)
+        evals.append(e)
+        errs.append(err)
+    ed.Solver.SolverClean(eps)
+    ms_step = ms / args.steps
+    if ws > 1:
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t[0])
+
+    # roofline of the dominant kernel (H.v): algorithmic bytes per launch
+    pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
+    kb = kbar(N, b.nspins_up, pairs)
+    bytes_row = 16 + 16 * kb + 16 + 4 + 8
+    hv_ms = ms_hv / max(n_hv, 1)
+    achieved = dim * bytes_row / (hv_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tp = os.path.join(ROOT, 'profiles', 'hv_traffic.json')
+    if os.path.exists(tp):
+        try:
+            tj = json.load(open(tp))
+            if tj.get('workload') == wl:
+                traffic = tj.get('dram_bytes_per_launch')
+        except Exception:
+            traffic = None
+
+    # e2e through the public API with host buffers (pinned), one step: basis,
+    # Hamiltonian, start vector uploaded from host memory, solve, eigenvectors
+    # read back into host memory.
+    e2e = None
+    if not args.no_e2e:
+        start_host = torch.empty(dim, dtype=torch.complex128, pin_memory=True)
+        start_host.numpy()[:] = start_vector_host(dim)
+        out_host = [torch.empty(dim, dtype=torch.complex128, pin_memory=True) for _ in range(nev)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b2 = ed.Basis(env, mag)
+        lat2 = ed.square2D(env, lx, ly) if ltype == 'square2D' else ed.chain1D(env)
+        H2 = ed.Hamiltonian(env, b2, lat2, J1, D1, J2, D2)
+        H2.build_diag(env)
+        H2.build_off_diag(env)
+        eps2 = ed.Solver.SolverInit(H2, nev, ncv if ncv else ed.PETSC_DEFAULT)
+        ed.Solver.EPSSetTolerances(eps2, tol, 0)
+        eps2.set_initial_vector(start_host)
+        ed.Solver.solve(env, eps2)
+        vals2 = []
+        for i in range(nev):
+            e, err = ed.Solver.eigenvalue(eps2, i)
+            vals2.append(e)
+            ed.Solver.solution_host(eps2, i, out=out_host[i])
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        ed.Solver.SolverClean(eps2)
+        del H2, b2
+        e2e = {'value': t_e2e, 'unit': 's', 'h2d_bytes_per_step': int(16 * dim + 8 * 2 * len(pairs)),
+               'd2h_bytes_per_step': int(16 * dim * nev), 'steps': 1,
+               'eigenvalues_match_device_run': bool(np.allclose(vals2, evals, rtol=1e-10, atol=0))}
+
+    cpu = None
+    if rk == 0 and not args.no_cpu:
+        try:
+            cpu = CpuSample(wl).run(st['nhv']) if N > 24 else None
+            if cpu is None:
+                import oracle
+                lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
+                t0 = time.perf_counter()
+                M = oracle.Model(lt, N, lx, ly, mag, J1, D1, J2, D2)
+                M.build(3)
+                r = M.eps_solve(nev=nev, ncv=ncv, tol=tol, seed=0, vectors=False)
+                cpu = {'value': time.perf_counter() - t0, 'unit': 's', 'cores': oracle.get_threads(),
+                       'kind': 'port', 'sample': 'full CPU eigensolve, nhv=%d' % r['nhv']}
+        except Exception as ex:  # reported, never fatal
+            cpu = {'value': None, 'unit': 's', 'cores': None, 'kind': 'port', 'sample': 'failed: %s' % ex}
+
+    if rk != 0:
+        return 0
+    line = {
+        'metric': METRIC, 'value': ms_step / 1e3, 'unit': 's', 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': False, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'c128', 'data': 'synthetic', 'config': workload_config(wl),
+        'e2e': e2e, 'gpu_launches': launches,
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                     'traffic': traffic, 'kernel': 'k_hv_gather (matrix-free H.v)', 'peak_kind': peak_kind,
+                     'bytes_per_row': bytes_row, 'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
+                     'launches_timed': n_hv},
+        'hv_gbs': achieved,
+        'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'eigenvalues': evals,
+                   'rel_residuals': errs},
+        'clocks': clocks, 'cpu_baseline': cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def start_vector_host(n, seed=0):
+    """The solver's seeded start vector (re, im ~ U[-1,1) from splitmix64),
+    generated on the host for the end-to-end run."""
+    import numpy as np
+    i = np.arange(n, dtype=np.uint64)
+    base = np.uint64((seed * 0xD1B54A32D192ED03) & 0xFFFFFFFFFFFFFFFF)
+
+    def sm(z):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+    with np.errstate(over='ignore'):
+        h1 = sm(base + np.uint64(2) * i)
+        h2 = sm(base + np.uint64(2) * i + np.uint64(1))
+    u1 = (h1 >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    u2 = (h2 >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return (2.0 * u1 - 1.0) + 1j * (2.0 * u2 - 1.0)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=2)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='c5', choices=sorted(WORKLOADS))
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

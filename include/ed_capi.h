@@ -1,0 +1,197 @@
+/*
+ * ed_capi.h — C ABI of the GB300 exact-diagonalization engine (libedgb300.so).
+ *
+ * The engine replaces LSQuantumED's hot path (fixed-Sz basis -> Hamiltonian
+ * application -> Krylov-Schur eigensolve -> correlations / DSF) on one GPU.
+ * Every entry point names the reference interface it replaces (paths are
+ * relative to the LSQuantumED source tree).
+ *
+ * Conventions
+ *  - Return value: ED_OK (0) or an ED_E* code; ed_last_error() gives the
+ *    message of the most recent failure on the calling thread.
+ *  - Pointers whose name ends in _dev are device pointers on the context's
+ *    device; _host pointers are host memory.  Vectors are complex128,
+ *    interleaved (re, im), length = basis size, in basis (rank) order.
+ *  - States are bit strings (bit i set = site i up), exactly as
+ *    Basis::int_basis (include/basis.hpp:67-75).
+ *  - All work is issued on the context's stream; calls returning host data
+ *    synchronize that stream.
+ */
+#ifndef ED_CAPI_H
+#define ED_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  ED_OK = 0,
+  ED_EINVAL = 1,    /* bad argument (std::invalid_argument in the reference) */
+  ED_ECUDA = 2,     /* CUDA runtime error */
+  ED_ENOMEM = 3,    /* device allocation failed */
+  ED_ESTATE = 4,    /* call out of order (e.g. eigenpair before solve) */
+  ED_ENOTCONV = 5,  /* solver hit max_it before nev pairs converged */
+  ED_ENOTSUP = 6    /* size outside what the device path supports */
+};
+
+enum { ED_CHAIN1D = 0, ED_SQUARE2D = 1, ED_HONEYCOMB2D = 2 };  /* lattice_type, include/lattice.hpp */
+enum { ED_OP_SZSZ = 0, ED_OP_SPSM = 1, ED_OP_SMSP = 2, ED_OP_SISJ = 3 };  /* spinOperators/correlation.hpp */
+enum { ED_HAM_MATRIX_FREE = 0, ED_HAM_CSR = 1 };
+enum { ED_ACC_FP64 = 0, ED_ACC_EXACT = 1 };
+
+typedef struct { double re, im; } ed_cplx;
+typedef struct ed_ctx ed_ctx;
+typedef struct ed_basis ed_basis;
+typedef struct ed_ham ed_ham;
+typedef struct ed_eps ed_eps;
+
+/* ---- errors / version ---------------------------------------------------- */
+int ed_last_error(char* buf, size_t len);
+int ed_version(void);
+
+/* ---- context: replaces Environment (src/environment.cpp:8-49) ------------- */
+/* device < 0 selects the current device.  stream may be NULL (the context
+ * creates its own non-blocking stream) or a cudaStream_t owned by the caller. */
+int ed_ctx_create(int device, void* stream, ed_ctx** out);
+int ed_ctx_destroy(ed_ctx* ctx);
+int ed_ctx_synchronize(ed_ctx* ctx);
+/* Number of kernels this context launched so far (for launch accounting). */
+int ed_ctx_kernel_count(const ed_ctx* ctx, int64_t* count);
+/* Per-launch timing of the H.v kernels with CUDA events on the context's
+ * stream (the reference's -log_view / TIME_CODE timers,
+ * include/tools/time_monitor.hpp:45-112).  enable != 0 clears and starts. */
+int ed_ctx_profile(ed_ctx* ctx, int enable);
+/* H.v launches recorded and their summed device time in milliseconds. */
+int ed_ctx_profile_read(ed_ctx* ctx, int64_t* n_hv, double* ms_hv);
+
+/* ---- device vectors: replace MatCreateVecs / VecDestroy / VecGetArray ---- */
+/* n complex128 entries on the context's device (uninitialised). */
+int ed_vec_create(ed_ctx* ctx, int64_t n, ed_cplx** vec_dev);
+int ed_vec_destroy(ed_cplx* vec_dev);
+/* Copies on the context's stream; the host side returns after completion. */
+int ed_vec_to_host(ed_ctx* ctx, const ed_cplx* vec_dev, ed_cplx* host, int64_t n);
+int ed_vec_from_host(ed_ctx* ctx, const ed_cplx* host, ed_cplx* vec_dev, int64_t n);
+
+/* ---- basis: replaces Basis(env, total_mag) (src/basis.cpp:56-94) ---------- */
+/* Validates like basis.cpp:66-76 (|total_mag| <= N/2; N even, > 0 like
+ * environment.cpp:31-35); N <= 32 on the device path (ED_ENOTSUP otherwise). */
+int ed_basis_create(ed_ctx* ctx, int nspins, int total_mag, ed_basis** out);
+int ed_basis_destroy(ed_basis* b);
+/* size = C(N, nspins_up) (basis.cpp:38-46). */
+int ed_basis_info(const ed_basis* b, int64_t* size, int* nspins, int* nspins_up, int* total_mag);
+/* int_basis[start .. start+count) (basis.cpp:192-215) into host memory. */
+int ed_basis_states_host(const ed_basis* b, int64_t start, int64_t count, uint64_t* out_host);
+/* Rank of each state: HamiltHelper::search_index (src/hamiltonian.cpp:9-27). */
+int ed_basis_rank_host(const ed_basis* b, const uint64_t* states_host, int64_t* ranks_host, int64_t n);
+/* Unrank: BasisHelper::search_elem (src/basis.cpp:9-36). */
+int ed_basis_unrank_host(const ed_basis* b, const int64_t* ranks_host, uint64_t* states_host, int64_t n);
+/* Device array of the basis states (uint32 words, one per state). */
+int ed_basis_device_states(const ed_basis* b, const uint32_t** states_dev);
+
+/* ---- lattice: replaces chain1D / square2D / honeycomb2D (src/lattice.cpp) -- */
+/* Flattened ordered bond lists (i, j) for nn and nnn, in the order
+ * get_coup_elems / get_elem_diag visit them (site-major, neighbour order;
+ * hamiltonian.tmpl_func.hpp:350-426).  Capacities in pairs; n_* receive the
+ * counts.  Returns ED_EINVAL on lx*ly != N (lattice.cpp:67-68). */
+int ed_lattice_bonds(int ltype, int nspins, int lx, int ly,
+                     int32_t* nn_pairs, int64_t nn_cap, int64_t* n_nn,
+                     int32_t* nnn_pairs, int64_t nnn_cap, int64_t* n_nnn);
+
+/* ---- Hamiltonian: replaces Hamiltonian<L> (include/hamiltonian.hpp:187-249) */
+/* Hamiltonian<L>(env, basis, lattice, J1, Delta1, J2, Delta2)
+ * (hamiltonian.tmpl_func.hpp:70-91): nn and nnn bond lists plus couplings. */
+int ed_ham_create(ed_ctx* ctx, const ed_basis* b,
+                  const int32_t* nn_pairs, int64_t n_nn, const int32_t* nnn_pairs, int64_t n_nnn,
+                  double J1, double D1, double J2, double D2, ed_ham** out);
+/* Generalisation with one (J_b, D_b) per bond (per-bond couplings; the
+ * reference has only the uniform J1/J2).  Diagonal = sum_b D_b*0.25*(+-1). */
+int ed_ham_create_bonds(ed_ctx* ctx, const ed_basis* b, const int32_t* pairs, int64_t nbonds,
+                        const double* J_host, const double* D_host, ed_ham** out);
+int ed_ham_destroy(ed_ham* h);
+/* build_diag (hamiltonian.tmpl_func.hpp:129-225). */
+int ed_ham_build_diag(ed_ham* h);
+/* build_off_diag (hamiltonian.tmpl_func.hpp:229-344): enables the J terms. */
+int ed_ham_build_off_diag(ed_ham* h);
+/* build_disorder (hamiltonian.tmpl_func.hpp:97-125): the diagonal becomes
+ * D1*0.25*E_nn + D2*0.25*E_nnn + 0.5*sum_i(+-h_i).  hi has N entries. */
+int ed_ham_build_disorder(ed_ham* h, const double* hi_host);
+/* y = H x (PETSc MatMult on Hamiltonian::hamilt).  Device vectors. */
+int ed_ham_apply(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev);
+/* Same with host buffers (copies in and out on the context's stream). */
+int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host);
+/* Explicit CSR on the device (when it fits); then ed_ham_set_mode(ED_HAM_CSR)
+ * makes ed_ham_apply / the solver use the CSR SpMV. */
+int ed_ham_build_csr(ed_ham* h, int64_t* nnz);
+int ed_ham_set_mode(ed_ham* h, int mode);
+/* Export the assembled matrix (rows sorted by column, duplicates summed in
+ * the reference's order) — the parity view of Hamiltonian::hamilt. */
+int ed_ham_export_csr_host(ed_ham* h, int64_t* rowptr_host, int64_t* cols_host, double* vals_host, int64_t cap);
+/* Matrix-free H.v accumulation: ED_ACC_EXACT (default) sums the gathered
+ * entries exactly in 128-bit integers (block floating point input, 2^-61
+ * relative to each 32-state block's largest entry) and rounds once to FP64;
+ * ED_ACC_FP64 adds them in FP64.  Per-bond Hamiltonians always use FP64.
+ * (No counterpart in the reference: PETSc MatMult adds in FP64.) */
+int ed_ham_set_accumulation(ed_ham* h, int kind);
+/* Diagonal of the assembled matrix (MatGetDiagonal). */
+int ed_ham_diag_host(ed_ham* h, double* out_host);
+int ed_ham_size(const ed_ham* h, int64_t* size);
+
+/* ---- eigensolver: replaces Solver:: (src/solver.cpp:7-68) ----------------- */
+/* SolverInit(eps, H, nev, ncv, mpd): Hermitian, Krylov-Schur, smallest real.
+ * ncv/mpd <= 0 mean PETSC_DECIDE (ncv = max(2 nev, nev + 15), capped at n). */
+int ed_eps_create(ed_ham* h, int nev, int ncv, int mpd, ed_eps** out);
+/* EPSSetDimensions */
+int ed_eps_set_dimensions(ed_eps* e, int nev, int ncv, int mpd);
+/* -eps_tol / -eps_max_it (tol <= 0: 1e-8, max_it <= 0: max(100, 2n/ncv)). */
+int ed_eps_set_tolerances(ed_eps* e, double tol, int max_it);
+/* Seed of the deterministic start vector (re, im ~ U[-1,1) per entry). */
+int ed_eps_set_seed(ed_eps* e, uint64_t seed);
+/* EPSSetInitialSpace with one vector (normalised by the solver); on_device
+ * selects whether v points to device or host memory.  NULL clears it. */
+int ed_eps_set_initial_vector(ed_eps* e, const ed_cplx* v, int on_device);
+/* Solver::solve: returns nconv. */
+int ed_eps_solve(ed_eps* e, int* nconv);
+/* Solver::solution(i): eigenvalue, relative error ||Hx - lx|| / |l|, and
+ * (optionally) the eigenvector into a device or host buffer. */
+int ed_eps_get_eigenpair(ed_eps* e, int i, double* eig, double* rel_err, ed_cplx* vec_dev);
+int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host);
+/* Iterations (restarts), H.v applications, eigenvalues reported. */
+int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported);
+int ed_eps_destroy(ed_eps* e);  /* Solver::SolverClean */
+
+/* ---- measurements: replace SiSj/SzSz/SpSm/SmSp::ExpectVal
+ *      (src/spinOperators/correlation.cpp:38-299) --------------------------- */
+/* out[p] = ExpectVal(op, i_p, j_p, psi) for npairs pairs in one fused pass
+ * (PETSc VecDot convention: sum_s psi_s * conj((O psi)_s)). */
+int ed_expect_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, const int32_t* pairs_host,
+                    int64_t npairs, ed_cplx* out_host);
+/* All N*N <S_i.S_j> (op = ED_OP_SISJ) into out_host[i*N + j]. */
+int ed_expect_all_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, ed_cplx* out_host);
+
+/* ---- DSF: replaces Phys::DynStructFactor's coefficient loop
+ *      (include/phys.tmpl_func.hpp:161-186) --------------------------------- */
+/* c[i*nev + n] = VecDot(S_i |psi0>, v_n) = v_n^H S_i psi0, for all sites i
+ * and nev target vectors v_n (device, column n at vecs_dev + n*dim1).
+ * op 0 = Sqz (same sector, spinOPft.tmpl_func.hpp:28-60),
+ * op 1 = Sqp (S+ into sector m+1, spinOPft.tmpl_func.hpp:77-143). */
+int ed_dsf_coefficients(const ed_basis* b0, const ed_basis* b1, int op, const ed_cplx* psi0_dev,
+                        const ed_cplx* vecs_dev, int nev, ed_cplx* c_host);
+
+/* ---- disorder: replaces Tools::RandomDisorder
+ *      (src/tools/random_disorder.cpp:33-59), host only --------------------- */
+/* srand_seq_init: rep seeds ~ uniform_int(0, 1000) from mt19937_64(1) when
+ * reprod != 0, else from std::random_device. */
+int ed_random_seeds(int reprod, int64_t rep, int64_t* seeds_host);
+/* hi_init: h_i ~ uniform_real(min, max) from mt19937_64(seed), i < nspins. */
+int ed_random_fields(int64_t seed, int nspins, double min, double max, double* hi_host);
+/* n draws of std::normal_distribution(0, 1) from mt19937_64(seed) (per-bond
+ * coupling disorder; no counterpart in the reference). */
+int ed_random_normal(int64_t seed, int64_t n, double* out_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ED_CAPI_H */

@@ -1,0 +1,321 @@
+// lsqed.hpp — header-only C++ shim that re-creates LSQuantumED's hot-path
+// class interfaces on top of the C ABI in ed_capi.h, so drivers written
+// against the reference (examples/main.cpp, main_disorder.cpp, ex1-4.cpp)
+// keep their structure.  PETSc types map as: PetscInt -> int64_t,
+// PetscReal -> double, PetscScalar -> std::complex<double>,
+// PetscErrorCode -> int, Mat -> the Hamiltonian itself, Vec -> lsqed::Vec
+// (a device vector), EPS -> lsqed::EPS.
+//
+// Link with -ledgb300 (lsquantumed_gb300/_lib/libedgb300.so).
+#pragma once
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../ed_capi.h"
+
+namespace lsqed {
+
+typedef int64_t PetscInt;
+typedef double PetscReal;
+typedef std::complex<double> PetscScalar;
+typedef int PetscErrorCode;
+static const PetscInt PETSC_DECIDE = -1;
+static const PetscInt PETSC_DEFAULT = -2;
+
+inline std::string last_error() {
+  char buf[1024];
+  ed_last_error(buf, sizeof(buf));
+  return buf;
+}
+
+// Map C ABI status to the reference's behaviour: constructors throw
+// std::invalid_argument / std::runtime_error, other calls return codes.
+inline void throw_on(int rc) {
+  if (rc == ED_OK) return;
+  if (rc == ED_EINVAL) throw std::invalid_argument(last_error());
+  throw std::runtime_error(last_error());
+}
+
+// ---------------------------------------------------------------------------
+// Environment (include/environment.hpp:20-53)
+// ---------------------------------------------------------------------------
+class Environment {
+ public:
+  PetscInt nspins = 0;
+  int mpi_rank = 0, mpi_size = 1;
+  bool disorder_flg = false;
+  ed_ctx* ctx = nullptr;
+
+  Environment(int /*argc*/, char** /*argv*/, const char* /*help*/ = nullptr) { throw_on(ed_ctx_create(0, nullptr, &ctx)); }
+  Environment(int /*argc*/, char** /*argv*/, PetscInt m_nspins, const char* /*help*/ = nullptr) {
+    if (m_nspins % 2 != 0) throw std::invalid_argument("The total number of spins has to be EVEN.");
+    if (m_nspins <= 0) throw std::invalid_argument("The total number of spins has to be POSITIVE.");
+    nspins = m_nspins;
+    throw_on(ed_ctx_create(0, nullptr, &ctx));
+  }
+  ~Environment() { ed_ctx_destroy(ctx); }
+  Environment(const Environment&) = delete;
+  Environment& operator=(const Environment&) = delete;
+};
+
+// ---------------------------------------------------------------------------
+// Basis (include/basis.hpp:67-93)
+// ---------------------------------------------------------------------------
+class Basis {
+ public:
+  PetscInt nspins, total_mag, nspins_up, max_mag, size, local_size, global_start_index;
+  int mpi_size = 1, mpi_rank = 0;
+  ed_basis* h = nullptr;
+
+  Basis(Environment& env, PetscInt m_total_mag) {
+    throw_on(ed_basis_create(env.ctx, (int)env.nspins, (int)m_total_mag, &h));
+    int ns, nup, tm;
+    int64_t sz;
+    throw_on(ed_basis_info(h, &sz, &ns, &nup, &tm));
+    nspins = ns; nspins_up = nup; total_mag = tm; max_mag = ns / 2;
+    size = sz; local_size = sz; global_start_index = 0;
+  }
+  ~Basis() { ed_basis_destroy(h); }
+  Basis(const Basis&) = delete;
+  Basis& operator=(const Basis&) = delete;
+  // int_basis (basis.cpp:192-215), fetched on demand
+  std::vector<PetscInt> int_basis() const {
+    std::vector<uint64_t> s((size_t)size);
+    throw_on(ed_basis_states_host(h, 0, size, s.data()));
+    return std::vector<PetscInt>(s.begin(), s.end());
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Lattices (include/lattice.hpp:166-329)
+// ---------------------------------------------------------------------------
+class Lattice {
+ public:
+  PetscInt nspins, nspins_x, nspins_y;
+  std::vector<int32_t> nn, nnn;  // flattened (i, j) pairs in visiting order
+ protected:
+  Lattice(Environment& env, int ltype, PetscInt lx, PetscInt ly) : nspins(env.nspins), nspins_x(lx), nspins_y(ly) {
+    int64_t na = 0, nb = 0;
+    throw_on(ed_lattice_bonds(ltype, (int)nspins, (int)lx, (int)ly, nullptr, 0, &na, nullptr, 0, &nb));
+    nn.resize(2 * na);
+    nnn.resize(2 * nb);
+    throw_on(ed_lattice_bonds(ltype, (int)nspins, (int)lx, (int)ly, nn.data(), na, &na, nnn.data(), nb, &nb));
+  }
+ public:
+  PetscInt num_spins() const { return nspins; }
+};
+class chain1D : public Lattice {
+ public:
+  explicit chain1D(Environment& env) : Lattice(env, ED_CHAIN1D, 1, env.nspins) {}
+};
+class square2D : public Lattice {
+ public:
+  square2D(Environment& env, PetscInt lx, PetscInt ly) : Lattice(env, ED_SQUARE2D, lx, ly) {}
+};
+class honeycomb2D : public Lattice {
+ public:
+  honeycomb2D(Environment& env, PetscInt lx, PetscInt ly) : Lattice(env, ED_HONEYCOMB2D, lx, ly) {}
+};
+
+// ---------------------------------------------------------------------------
+// Device vector (PETSc Vec), created by MatCreateVecs(h)
+// ---------------------------------------------------------------------------
+class Vec {
+ public:
+  ed_ctx* ctx = nullptr;
+  ed_cplx* d = nullptr;
+  PetscInt n = 0;
+  Vec() {}
+  Vec(Environment& env, PetscInt size) : ctx(env.ctx), n(size) { throw_on(ed_vec_create(ctx, n, &d)); }
+  ~Vec() { ed_vec_destroy(d); }
+  Vec(const Vec&) = delete;
+  Vec& operator=(const Vec&) = delete;
+  std::vector<PetscScalar> to_host() const {
+    std::vector<PetscScalar> out((size_t)n);
+    throw_on(ed_vec_to_host(ctx, d, reinterpret_cast<ed_cplx*>(out.data()), n));
+    return out;
+  }
+  void from_host(const std::vector<PetscScalar>& v) {
+    throw_on(ed_vec_from_host(ctx, reinterpret_cast<const ed_cplx*>(v.data()), d, n));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Hamiltonian<L> (include/hamiltonian.hpp:187-299)
+// ---------------------------------------------------------------------------
+template <typename L>
+class Hamiltonian {
+ public:
+  ed_ham* hamilt = nullptr;  // the reference's `Mat hamilt`
+  Basis& basis;
+  L& lattice;
+  PetscReal J1, Delta1, J2, Delta2;
+
+  Hamiltonian(Environment& env, Basis& b, L& lat, PetscReal m_J1, PetscReal m_D1, PetscReal m_J2, PetscReal m_D2)
+      : basis(b), lattice(lat), J1(m_J1), Delta1(m_D1), J2(m_J2), Delta2(m_D2) {
+    int rc = ed_ham_create(env.ctx, b.h, lat.nn.data(), (int64_t)lat.nn.size() / 2, lat.nnn.data(),
+                           (int64_t)lat.nnn.size() / 2, J1, Delta1, J2, Delta2, &hamilt);
+    if (rc != ED_OK) throw std::runtime_error("The matrix has not been properly initialized.\n" + last_error());
+  }
+  ~Hamiltonian() { ed_ham_destroy(hamilt); }
+  Hamiltonian(const Hamiltonian&) = delete;
+  Hamiltonian& operator=(const Hamiltonian&) = delete;
+
+  PetscErrorCode build_diag(Environment&) { return ed_ham_build_diag(hamilt); }
+  PetscErrorCode build_off_diag(Environment&) { return ed_ham_build_off_diag(hamilt); }
+  PetscErrorCode build_disorder(Environment& env, PetscReal* hi) {
+    env.disorder_flg = true;
+    return ed_ham_build_disorder(hamilt, hi);
+  }
+  PetscInt hamilt_size() const { return basis.size; }
+  PetscReal hamilt_J1() const { return J1; }
+  PetscReal hamilt_J2() const { return J2; }
+  PetscReal hamilt_D1() const { return Delta1; }
+  PetscReal hamilt_D2() const { return Delta2; }
+};
+
+// ---------------------------------------------------------------------------
+// Solver:: (include/solver.hpp:27-66)
+// ---------------------------------------------------------------------------
+struct EPS {
+  ed_eps* e = nullptr;
+};
+
+namespace Solver {
+template <typename L>
+inline PetscErrorCode SolverInit(EPS& solver, Hamiltonian<L>& h, PetscInt nev, PetscInt ncv = PETSC_DEFAULT,
+                                 PetscInt mpd = PETSC_DEFAULT) {
+  return ed_eps_create(h.hamilt, (int)nev, (int)ncv, (int)mpd, &solver.e);
+}
+inline PetscErrorCode EPSSetDimensions(EPS& solver, PetscInt nev, PetscInt ncv, PetscInt mpd) {
+  return ed_eps_set_dimensions(solver.e, (int)nev, (int)ncv, (int)mpd);
+}
+inline PetscErrorCode EPSSetTolerances(EPS& solver, PetscReal tol, PetscInt max_it) {
+  return ed_eps_set_tolerances(solver.e, tol, (int)max_it);
+}
+inline PetscErrorCode solve(Environment&, EPS& solver, PetscInt& nconv) {
+  int n = 0;
+  int rc = ed_eps_solve(solver.e, &n);
+  nconv = n;
+  return rc;
+}
+// Solver::solution (src/solver.cpp:58-68): eigenvalue, relative error, and
+// the eigenvector copied into the device vector x.
+inline PetscErrorCode solution(EPS& solver, PetscInt index, PetscScalar& value, Vec& x, PetscReal& error) {
+  double ev = 0.0, err = 0.0;
+  int rc = ed_eps_get_eigenpair(solver.e, (int)index, &ev, &err, x.d);
+  value = PetscScalar(ev, 0.0);
+  error = err;
+  return rc;
+}
+inline PetscErrorCode SolverClean(EPS& solver) {
+  int rc = ed_eps_destroy(solver.e);
+  solver.e = nullptr;
+  return rc;
+}
+}  // namespace Solver
+
+// ---------------------------------------------------------------------------
+// Correlations (include/spinOperators/correlation.hpp:80-194)
+// ---------------------------------------------------------------------------
+class Correlation {
+ protected:
+  Basis& basis;
+  int op;
+  Correlation(Basis& b, int o) : basis(b), op(o) {}
+ public:
+  PetscScalar ExpectVal(Environment&, PetscInt spin_i, PetscInt spin_j, Vec& state) {
+    int32_t pr[2] = {(int32_t)spin_i, (int32_t)spin_j};
+    ed_cplx out;
+    throw_on(ed_expect_pairs(basis.h, op, state.d, pr, 1, &out));
+    return PetscScalar(out.re, out.im);
+  }
+  // All N*N values in one fused pass (row-major [i][j]).
+  std::vector<PetscScalar> AllPairs(Vec& state) {
+    std::vector<PetscScalar> out((size_t)(basis.nspins * basis.nspins));
+    throw_on(ed_expect_all_pairs(basis.h, op, state.d, reinterpret_cast<ed_cplx*>(out.data())));
+    return out;
+  }
+};
+class SzSz : public Correlation { public: SzSz(Environment&, Basis& b) : Correlation(b, ED_OP_SZSZ) {} };
+class SpSm : public Correlation { public: SpSm(Environment&, Basis& b) : Correlation(b, ED_OP_SPSM) {} };
+class SmSp : public Correlation { public: SmSp(Environment&, Basis& b) : Correlation(b, ED_OP_SMSP) {} };
+class SiSj : public Correlation { public: SiSj(Environment&, Basis& b) : Correlation(b, ED_OP_SISJ) {} };
+
+// ---------------------------------------------------------------------------
+// Sublattices (src/sublattice.cpp:5-91) and order parameters
+// (include/phys.tmpl_func.hpp:5-81)
+// ---------------------------------------------------------------------------
+template <typename L>
+class AF {
+ public:
+  std::vector<std::vector<PetscInt>> sublat{{}, {}};
+  AF(L& lat, PetscInt /*size*/ = 2) {
+    if (lat.nspins_x == 1) {
+      for (PetscInt i = 0; i < lat.nspins; ++i) sublat[(i % 2) ? 1 : 0].push_back(i);
+    } else {
+      int tagx = 0;
+      for (PetscInt ix = 0; ix < lat.nspins_x; ++ix) {
+        int tagy = tagx;
+        for (PetscInt iy = 0; iy < lat.nspins_y; ++iy) {
+          sublat[(tagy % 2) ? 1 : 0].push_back(ix * lat.nspins_y + iy);
+          tagy ^= 1;
+        }
+        tagx ^= 1;
+      }
+    }
+  }
+  PetscInt get_size() const { return 2; }
+  const std::vector<PetscInt>& get_sl(PetscInt i) const { return sublat[(size_t)i]; }
+};
+
+template <typename L>
+class Striped {
+ public:
+  std::vector<std::vector<PetscInt>> sublat{{}, {}, {}, {}};
+  Striped(L& lat, PetscInt /*size*/ = 4) {
+    int tagx = 0;
+    for (PetscInt ix = 0; ix < lat.nspins_x; ++ix) {
+      int tagy = 0;
+      for (PetscInt iy = 0; iy < lat.nspins_y; ++iy) {
+        PetscInt cur = ix * lat.nspins_y + iy;
+        sublat[(tagy % 2) ? 1 : 0].push_back(cur);
+        sublat[(tagx % 2) ? 3 : 2].push_back(cur);
+        tagy ^= 1;
+      }
+      tagx ^= 1;
+    }
+  }
+  PetscInt get_size() const { return 4; }
+  const std::vector<PetscInt>& get_sl(PetscInt i) const { return sublat[(size_t)i]; }
+};
+
+namespace Phys {
+inline PetscScalar sublattice_sum(Basis& b, const std::vector<const std::vector<PetscInt>*>& lists, Vec& state) {
+  std::vector<int32_t> pairs;
+  for (auto* sl : lists)
+    for (PetscInt i : *sl)
+      for (PetscInt j : *sl) { pairs.push_back((int32_t)i); pairs.push_back((int32_t)j); }
+  std::vector<ed_cplx> out(pairs.size() / 2);
+  throw_on(ed_expect_pairs(b.h, ED_OP_SISJ, state.d, pairs.data(), (int64_t)out.size(), out.data()));
+  PetscScalar e = 0.0;
+  for (auto& v : out) e += PetscScalar(v.re, v.im);
+  return e;
+}
+template <typename L>
+inline PetscScalar SquaredSubLattMagAF(Environment& env, Basis& b, AF<L>& sl, Vec& state) {
+  PetscScalar e = sublattice_sum(b, {&sl.get_sl(0), &sl.get_sl(1)}, state);
+  return e * 8.0 / PetscScalar((double)env.nspins) / PetscScalar(env.nspins + 4.0);
+}
+template <typename L>
+inline PetscScalar SquaredSubLattMagSTR(Environment& env, Basis& b, Striped<L>& sl, Vec& state) {
+  PetscScalar e = sublattice_sum(b, {&sl.get_sl(0), &sl.get_sl(1), &sl.get_sl(2), &sl.get_sl(3)}, state);
+  return e * 4.0 / PetscScalar((double)env.nspins) / PetscScalar(env.nspins + 4.0);
+}
+}  // namespace Phys
+
+}  // namespace lsqed

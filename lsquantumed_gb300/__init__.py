@@ -1,0 +1,16 @@
+"""GB300-native exact diagonalization of spin-1/2 J1-J2 Heisenberg models.
+
+The compute path is libedgb300.so (hand-written sm_103a CUDA kernels behind
+the C ABI in include/ed_capi.h); this package is the host-side mirror of the
+LSQuantumED interfaces (Basis, Hamiltonian, Solver, SiSj, Phys, ...).
+"""
+from . import capi  # noqa: F401
+from .capi import EDError, InvalidArgument  # noqa: F401
+from .ed import (AF, DSF_data, EPS, PETSC_DECIDE, PETSC_DEFAULT, Basis, Environment, Hamiltonian,  # noqa: F401
+                 Phys, RandomDisorder, SiSj, SmSp, Solver, SpSm, Striped, SzSz, chain1D, honeycomb2D,
+                 random_fields, random_normal, square2D)
+
+
+def build(force=False):
+    from .build import build as _b
+    return _b(force=force)

@@ -1,0 +1,164 @@
+// Internal declarations shared by the libedgb300 translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/ed_capi.h"
+
+#define ED_MAX_BONDS 256
+#define ED_MAX_TYPES 256
+#define ED_MAX_SPINS 32
+#define ED_RANK_MAX_CHUNKS 4
+
+// ---------------------------------------------------------------------------
+// Error state (thread local) and helpers.
+// ---------------------------------------------------------------------------
+void ed_set_error(const std::string& msg);
+int ed_fail(int code, const std::string& msg);
+int ed_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define ED_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess) return ed_cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+#define ED_CHECK_LAUNCH(ctx)                                                  \
+  do {                                                                        \
+    cudaError_t _e = cudaGetLastError();                                      \
+    if (_e != cudaSuccess) return ed_cuda_fail(_e, "kernel launch", __FILE__, __LINE__); \
+    (ctx)->kernels++;                                                         \
+  } while (0)
+#define ED_TRY(expr)            \
+  do {                          \
+    int _rc = (expr);           \
+    if (_rc != ED_OK) return _rc; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Combinadic rank tables.  The N-bit state is split into K chunks (bottom to
+// top, widths w[k] at bit offsets off[k]).  rank(s) = sum_k T_k[c_k][chunk_k]
+// where c_k = number of set bits below chunk k; T_0 is indexed by the chunk
+// only (c = 0) and the top chunk's c is fixed by nup - popc(top chunk).  Each
+// entry is sum over the chunk's set bits (t-th from the bottom) of
+// C(off + q, c + t) — the combinadic sum of src/hamiltonian.cpp:9-27 split by
+// chunks, exact in integers.
+// ---------------------------------------------------------------------------
+struct RankTables {
+  int K;                          // number of chunks (1..4)
+  int nup;
+  int w[ED_RANK_MAX_CHUNKS];      // chunk widths
+  int off[ED_RANK_MAX_CHUNKS];    // bit offset of each chunk
+  int base[ED_RANK_MAX_CHUNKS];   // entry offset of each chunk's table
+  int total;                      // total entries
+  const uint32_t* tab;            // device pointer (total entries)
+};
+
+// Bonds in the order the reference visits them, with coupling types.
+// mask = (1 << i) | (1 << j); type indexes the per-type coefficients.
+struct BondSet {
+  int nb;
+  int ntypes;
+  int per_bond;                   // 1: one type per bond (J_b, D_b)
+  uint32_t mask[ED_MAX_BONDS];
+  uint8_t type[ED_MAX_BONDS];
+  double chalf[ED_MAX_TYPES];     // J_t * 0.5 (off-diagonal element per bond)
+};
+
+struct ed_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t kernels = 0;
+  // reduction scratch (device) and pinned host mirror
+  double* d_red = nullptr;
+  size_t red_cap = 0;             // doubles
+  double* h_red = nullptr;
+  int reduce_blocks = 0;
+  // H.v launch timing (events on the stream)
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;  // pairs (start, stop)
+};
+
+struct ed_basis {
+  ed_ctx* ctx = nullptr;
+  int nspins = 0, nup = 0, total_mag = 0;
+  int64_t dim = 0;
+  uint32_t* d_states = nullptr;
+  RankTables rt{};
+  uint32_t* d_tab = nullptr;
+  std::vector<uint32_t> h_tab;    // host copy of the rank tables
+};
+
+struct ed_ham {
+  ed_ctx* ctx = nullptr;
+  const ed_basis* basis = nullptr;
+  // reference parameters (uniform mode)
+  bool per_bond = false;
+  double J1 = 0, D1 = 0, J2 = 0, D2 = 0;
+  std::vector<int32_t> bi, bj;    // ordered bonds (nn first, then nnn in uniform mode)
+  std::vector<int> btype;         // 0 = nn, 1 = nnn (uniform) / bond index (per-bond)
+  std::vector<double> bJ, bD;     // per-bond couplings (per-bond mode)
+  int n_nn = 0;
+  bool diag_built = false, offdiag_built = false, disorder = false;
+  std::vector<double> hi;
+  double* d_diag = nullptr;       // assembled diagonal
+  BondSet bs{};                   // off-diagonal bond set (empty until build_off_diag)
+  int mode = ED_HAM_MATRIX_FREE;
+  // explicit CSR (real values; H is real symmetric)
+  int64_t* d_rowptr = nullptr;
+  uint32_t* d_cols = nullptr;
+  double* d_vals = nullptr;
+  int64_t nnz = 0;
+  // scratch for the host-buffer apply
+  double2* d_x = nullptr;
+  double2* d_y = nullptr;
+  // block floating point copy of the H.v input (integer accumulation path)
+  longlong2* d_xq = nullptr;      // 62-bit mantissas, (re, im) per state
+  uint16_t* d_xe = nullptr;       // biased exponent per 32-state block
+  int* d_gmax = nullptr;          // largest block exponent
+  int hv_kernel = 1;              // 0: FP64 accumulation, 1: exact integer accumulation
+};
+
+// ---------------------------------------------------------------------------
+// Launchers implemented in the .cu files.
+// ---------------------------------------------------------------------------
+int ed_build_rank_tables(int nspins, int nup, RankTables& rt, std::vector<uint32_t>& tab);
+int ed_launch_basis_states(ed_ctx* ctx, int nspins, int nup, int64_t dim, uint32_t* states);
+int ed_launch_rank(ed_ctx* ctx, const ed_basis* b, const uint32_t* states_dev, int64_t n, int64_t* ranks_dev);
+int ed_launch_unrank(ed_ctx* ctx, const ed_basis* b, const int64_t* ranks_dev, int64_t n, uint32_t* states_dev);
+
+int ed_launch_build_diag(ed_ham* h);
+int ed_launch_hv(ed_ham* h, const double2* x, double2* y);
+int ed_launch_csr_build(ed_ham* h);
+int ed_launch_csr_spmv(ed_ham* h, const double2* x, double2* y);
+void ed_ham_make_bondset(ed_ham* h);
+// Unique-mask coefficients for the assembled matrix (duplicates summed in
+// the reference's ADD_VALUES order).
+void ed_ham_unique_masks(const ed_ham* h, std::vector<uint32_t>& masks, std::vector<double>& vals);
+
+// linear algebra on device vectors (complex128)
+int ed_ensure_reduce(ed_ctx* ctx, size_t doubles);
+int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v);
+int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* w, int64_t n,
+                double2* h_host, double* wnorm2_host);
+int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_host, double2* w, int64_t n,
+              double* wnorm2_host);
+int ed_scale_copy(ed_ctx* ctx, const double2* src, double2* dst, double s, int64_t n);
+int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const double* Y, int ldY, int l,
+                       double2* const* out, int64_t n);
+int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double theta, int64_t n, double* r2_host,
+                      double* x2_host);
+int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);
+
+// measurements
+int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const int32_t* pairs_host, int64_t np,
+                           double2* out_host);
+int ed_launch_dsf(const ed_basis* b0, const ed_basis* b1, int op, const double2* psi0, const double2* vecs, int nev,
+                  double2* c_host);
+
+// small dense symmetric eigensolver (host)
+void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, std::vector<double>& Y);
+
+uint64_t ed_binom(int n, int k);

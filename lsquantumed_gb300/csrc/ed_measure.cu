@@ -1,0 +1,236 @@
+// Measurements: correlation expectation values (SzSz / SpSm / SmSp / SiSj,
+// src/spinOperators/correlation.cpp:38-299) and DSF coefficients
+// c_{i,n} = <v_n | S_i | psi0> (include/phys.tmpl_func.hpp:161-186 with
+// Sqz / Sqp from include/spinOperators/spinOPft.tmpl_func.hpp).
+//
+// The reference builds a sparse operator matrix per (i, j) and runs MatMult +
+// VecDot; here each pass over the basis evaluates a group of pairs at once,
+// gathering psi at the rank of the flipped state.  The PETSc VecDot
+// convention is kept: ExpectVal = sum_s psi_s * conj((O psi)_s).
+#include "ed_internal.h"
+#include "ed_device.cuh"
+#include <algorithm>
+
+#define MEAS_G 8
+
+struct PairGroup {
+  int n;
+  int32_t i[MEAS_G], j[MEAS_G];
+};
+
+template <int K>
+__global__ void __launch_bounds__(256) k_expect(const uint32_t* __restrict__ states, const double2* __restrict__ psi,
+                                                int64_t dim, const RankTables rt, int op, const PairGroup pg,
+                                                double* __restrict__ partial, int nblk) {
+  extern __shared__ uint32_t stab[];
+  ed_load_tables(stab, rt);
+  double acc[2 * MEAS_G];
+#pragma unroll
+  for (int k = 0; k < 2 * MEAS_G; ++k) acc[k] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const uint32_t s = states[r];
+    const double2 p = psi[r];
+    const double w = fma(p.x, p.x, p.y * p.y);
+#pragma unroll
+    for (int g = 0; g < MEAS_G; ++g) {
+      if (g >= pg.n) break;
+      const int i = pg.i[g], j = pg.j[g];
+      const uint32_t a = (s >> i) & 1u, b = (s >> j) & 1u;
+      double cr = 0.0, ci = 0.0;
+      // S^z_i S^z_j part: psi * conj(0.25 * (+-1) * psi)
+      if (op == ED_OP_SZSZ || op == ED_OP_SISJ) cr += (a ^ b) ? -0.25 * w : 0.25 * w;
+      if (op != ED_OP_SZSZ) {
+        const double half = (op == ED_OP_SISJ) ? 0.5 : 1.0;
+        if (i == j) {
+          // S+S- = n_i (a = 1), S-S+ = 1 - n_i (a = 0)
+          bool on = (op == ED_OP_SPSM) ? (a == 1u) : (op == ED_OP_SMSP) ? (a == 0u) : true;
+          if (on) cr += half * w;
+        } else {
+          bool on = (op == ED_OP_SPSM) ? (a == 0u && b == 1u) : (op == ED_OP_SMSP) ? (a == 1u && b == 0u) : (a != b);
+          if (on) {
+            const uint32_t c = ed_rank<K>(s ^ ((1u << i) | (1u << j)), stab, rt);
+            const double2 q = __ldg(&psi[c]);
+            // psi_r * conj(psi_c)
+            cr += half * fma(p.x, q.x, p.y * q.y);
+            ci += half * fma(p.y, q.x, -p.x * q.y);
+          }
+        }
+      }
+      acc[2 * g] += cr;
+      acc[2 * g + 1] += ci;
+    }
+  }
+  // block reduction
+  __shared__ double sh[2 * MEAS_G * 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 2 * MEAS_G; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[k * 32 + wid] = v;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    for (int k = 0; k < 2 * MEAS_G; ++k) {
+      double v = lane < nw ? sh[k * 32 + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) partial[(size_t)k * nblk + blockIdx.x] = v;
+    }
+  }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblk, int items, double* __restrict__ out) {
+  const int item = blockIdx.x;
+  if (item >= items) return;
+  __shared__ double sh[256];
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) a += partial[(size_t)item * nblk + b];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[item] = sh[0];
+}
+
+template <int K>
+static int expect_k(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np, double2* out) {
+  ed_ctx* ctx = b->ctx;
+  const int64_t dim = b->dim;
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 2));
+  const int items = 2 * MEAS_G;
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items + 8));
+  size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
+  ED_CUDA(cudaFuncSetAttribute(k_expect<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  double* out_dev = ctx->d_red + (size_t)items * nblk;
+  for (int64_t p0 = 0; p0 < np; p0 += MEAS_G) {
+    PairGroup pg;
+    pg.n = (int)std::min<int64_t>(MEAS_G, np - p0);
+    for (int g = 0; g < MEAS_G; ++g) {
+      pg.i[g] = g < pg.n ? pairs[2 * (p0 + g)] : 0;
+      pg.j[g] = g < pg.n ? pairs[2 * (p0 + g) + 1] : 0;
+    }
+    k_expect<K><<<nblk, 256, smem, ctx->stream>>>(b->d_states, psi, dim, b->rt, op, pg, ctx->d_red, nblk);
+    ED_CHECK_LAUNCH(ctx);
+    k_sum_partials<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, items, out_dev);
+    ED_CHECK_LAUNCH(ctx);
+    ED_CUDA(cudaMemcpyAsync(ctx->h_red, out_dev, sizeof(double) * items, cudaMemcpyDeviceToHost, ctx->stream));
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int g = 0; g < pg.n; ++g) { out[p0 + g].x = ctx->h_red[2 * g]; out[p0 + g].y = ctx->h_red[2 * g + 1]; }
+  }
+  return ED_OK;
+}
+
+int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np,
+                           double2* out) {
+  switch (b->rt.K) {
+    case 1: return expect_k<1>(b, op, psi, pairs, np, out);
+    case 2: return expect_k<2>(b, op, psi, pairs, np, out);
+    case 3: return expect_k<3>(b, op, psi, pairs, np, out);
+    default: return expect_k<4>(b, op, psi, pairs, np, out);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// DSF coefficients.  One launch handles up to MEAS_G sites for one target
+// vector v_n.
+//   Sqz: c_{i,n} = sum_r conj(v_n[r]) * 0.5 * (b_i(s_r) ? 1 : -1) * psi0[r]
+//   Sqp: c_{i,n} = sum_{r: b_i(s_r) = 0} conj(v_n[rank1(s_r | 1<<i)]) * psi0[r]
+// ---------------------------------------------------------------------------
+template <int K1>
+__global__ void __launch_bounds__(256) k_dsf(const uint32_t* __restrict__ states0, const double2* __restrict__ psi0,
+                                             int64_t dim0, const RankTables rt1, int op, int i0, int ni,
+                                             const double2* __restrict__ v, double* __restrict__ partial, int nblk) {
+  extern __shared__ uint32_t stab[];
+  if (op == 1) ed_load_tables(stab, rt1);
+  double acc[2 * MEAS_G];
+#pragma unroll
+  for (int k = 0; k < 2 * MEAS_G; ++k) acc[k] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim0; r += stride) {
+    const uint32_t s = states0[r];
+    const double2 p = psi0[r];
+    if (op == 0) {
+      const double2 q = v[r];
+      // conj(q) * p
+      const double pr = fma(q.x, p.x, q.y * p.y), pi = fma(q.x, p.y, -q.y * p.x);
+#pragma unroll
+      for (int g = 0; g < MEAS_G; ++g) {
+        if (g < ni) {
+          const double sg = ((s >> (i0 + g)) & 1u) ? 0.5 : -0.5;
+          acc[2 * g] = fma(sg, pr, acc[2 * g]);
+          acc[2 * g + 1] = fma(sg, pi, acc[2 * g + 1]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < MEAS_G; ++g) {
+        if (g < ni && !((s >> (i0 + g)) & 1u)) {
+          const uint32_t c = ed_rank<K1>(s | (1u << (i0 + g)), stab, rt1);
+          const double2 q = __ldg(&v[c]);
+          acc[2 * g] += fma(q.x, p.x, q.y * p.y);
+          acc[2 * g + 1] += fma(q.x, p.y, -q.y * p.x);
+        }
+      }
+    }
+  }
+  __shared__ double sh[2 * MEAS_G * 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 2 * MEAS_G; ++k) {
+    double a = acc[k];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) sh[k * 32 + wid] = a;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    for (int k = 0; k < 2 * MEAS_G; ++k) {
+      double a = lane < nw ? sh[k * 32 + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0) partial[(size_t)k * nblk + blockIdx.x] = a;
+    }
+  }
+}
+
+template <int K1>
+static int dsf_k(const ed_basis* b0, const ed_basis* b1, int op, const double2* psi0, const double2* vecs, int nev,
+                 double2* c_host) {
+  ed_ctx* ctx = b0->ctx;
+  const int64_t dim0 = b0->dim, dim1 = b1->dim;
+  const int N = b0->nspins;
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim0 + 255) / 256, (int64_t)ctx->num_sms * 2));
+  const int items = 2 * MEAS_G;
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items + 8));
+  size_t smem = op == 1 ? (size_t)b1->rt.total * sizeof(uint32_t) : 0;
+  ED_CUDA(cudaFuncSetAttribute(k_dsf<K1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  double* out_dev = ctx->d_red + (size_t)items * nblk;
+  for (int n = 0; n < nev; ++n) {
+    const double2* v = vecs + (size_t)n * dim1;
+    for (int i0 = 0; i0 < N; i0 += MEAS_G) {
+      int ni = std::min(MEAS_G, N - i0);
+      k_dsf<K1><<<nblk, 256, smem, ctx->stream>>>(b0->d_states, psi0, dim0, b1->rt, op, i0, ni, v, ctx->d_red, nblk);
+      ED_CHECK_LAUNCH(ctx);
+      k_sum_partials<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, items, out_dev);
+      ED_CHECK_LAUNCH(ctx);
+      ED_CUDA(cudaMemcpyAsync(ctx->h_red, out_dev, sizeof(double) * items, cudaMemcpyDeviceToHost, ctx->stream));
+      ED_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int g = 0; g < ni; ++g) {
+        c_host[(size_t)(i0 + g) * nev + n].x = ctx->h_red[2 * g];
+        c_host[(size_t)(i0 + g) * nev + n].y = ctx->h_red[2 * g + 1];
+      }
+    }
+  }
+  return ED_OK;
+}
+
+int ed_launch_dsf(const ed_basis* b0, const ed_basis* b1, int op, const double2* psi0, const double2* vecs, int nev,
+                  double2* c_host) {
+  switch (b1->rt.K) {
+    case 1: return dsf_k<1>(b0, b1, op, psi0, vecs, nev, c_host);
+    case 2: return dsf_k<2>(b0, b1, op, psi0, vecs, nev, c_host);
+    case 3: return dsf_k<3>(b0, b1, op, psi0, vecs, nev, c_host);
+    default: return dsf_k<4>(b0, b1, op, psi0, vecs, nev, c_host);
+  }
+}

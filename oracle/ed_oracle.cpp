@@ -574,12 +574,16 @@ static void ks_solve(int64_t n, Apply apply, int nev, int ncv, int mpd, double t
       alpha[j] = h[j].real();
       if (nw <= 1e-13 * norig) {
         // invariant subspace: continue with a random vector orthogonal to V
-        start_vector(rseed++, n, w.data());
-        double nw2, no2;
-        std::vector<cplx> h2;
-        orthog(j, h2, nw2, no2);
-        for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = w[r] / nw2;
         beta[j] = 0.0;
+        if (j + 1 < m) {
+          start_vector(rseed++, n, w.data());
+          double nw2, no2;
+          std::vector<cplx> h2;
+          orthog(j, h2, nw2, no2);
+          for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = w[r] / nw2;
+        } else {
+          for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = 0.0;
+        }
       } else {
         for (int64_t r = 0; r < n; ++r) V[(size_t)(j + 1) * n + r] = w[r] / nw;
         beta[j] = nw;
@@ -820,6 +824,29 @@ void orc_vecdot(int64_t n, const double* x, const double* y, double* out) {
     re += t.real(); im += t.imag();
   }
   out[0] = re; out[1] = im;
+}
+
+// One classical Gram-Schmidt pass of the Krylov-Schur restatement: h = V^H w,
+// w -= V h, for nv column vectors of length n (CPU baseline timing).
+void orc_cgs_step(int64_t n, int nv, const double* V, double* w, double* h_out) {
+  const cplx* Vc = (const cplx*)V; cplx* wc = (cplx*)w;
+  std::vector<double> hr(nv, 0.0), hi(nv, 0.0);
+  for (int i = 0; i < nv; ++i) {
+    double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+    for (int64_t r = 0; r < n; ++r) {
+      cplx t = std::conj(Vc[(size_t)i * n + r]) * wc[r];
+      re += t.real(); im += t.imag();
+    }
+    hr[i] = re; hi[i] = im;
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < n; ++r) {
+    cplx acc = wc[r];
+    for (int i = 0; i < nv; ++i) acc -= Vc[(size_t)i * n + r] * cplx(hr[i], hi[i]);
+    wc[r] = acc;
+  }
+  for (int i = 0; i < nv; ++i) { h_out[2 * i] = hr[i]; h_out[2 * i + 1] = hi[i]; }
 }
 
 }  // extern "C"

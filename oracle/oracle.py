@@ -25,7 +25,7 @@ def build(force=False):
     if not force and os.path.exists(_SO) and os.path.getmtime(_SO) >= os.path.getmtime(_SRC):
         return _SO
     tmp = _SO + '.tmp%d' % os.getpid()
-    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared', '-o', tmp, _SRC]
+    cmd = ['g++', '-O2', '-std=c++17', '-ffp-contract=off', '-fopenmp', '-fPIC', '-shared', '-o', tmp, _SRC]
     subprocess.check_call(cmd)
     os.replace(tmp, _SO)
     return _SO
@@ -69,6 +69,7 @@ def lib():
                 'orc_sqz': (None, [vp, i32, vp, vp]),
                 'orc_sqp': (None, [vp, vp, i32, vp, vp]),
                 'orc_vecdot': (None, [i64, vp, vp, vp]),
+                'orc_cgs_step': (None, [i64, i32, vp, vp, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -188,6 +189,13 @@ def vecdot(x, y):
     out = np.zeros(2)
     lib().orc_vecdot(x.size, _p(x), _p(y), _p(out))
     return complex(out[0], out[1])
+
+
+def cgs_step(V, w):
+    """One CGS pass (h = V^H w; w -= V h) on the CPU; V is (nv, n) complex."""
+    h = np.zeros(2 * V.shape[0])
+    lib().orc_cgs_step(V.shape[1], V.shape[0], _p(V), _p(w), _p(h))
+    return h[0::2] + 1j * h[1::2]
 
 
 def set_threads(n):
