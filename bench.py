@@ -30,6 +30,8 @@ WORKLOADS = {
     'c5': ('square2D', 30, 6, 5, 1.0, 1.0, 0.55, 0.55, 0, 4, 16, 1e-9),
     'c2': ('square2D', 20, 4, 5, 1.0, 1.0, 0.5, 0.5, 0, 10, 0, 1e-9),
     'c1': ('chain1D', 16, 1, 16, 1.0, 1.0, 0.0, 0.0, 0, 1, 0, 1e-9),
+    # same family, sized for profiler captures (vectors 0.64 GB, above L2)
+    'p28': ('square2D', 28, 4, 7, 1.0, 1.0, 0.55, 0.55, 0, 4, 16, 1e-9),
 }
 # H.v applications the Krylov-Schur run needs on each workload (seed 0), as
 # measured by the device run; the CPU restatement runs the same algorithm from
@@ -221,6 +223,53 @@ def workload_config(wl):
             'l2': 'inputs larger than L2 (each vector %.2f GB)' % (16 * math.comb(N, mag + N // 2) / 1e9)}
 
 
+def run_hv_only(args):
+    """Time the matrix-free H.v alone (K launches after W warm-up launches,
+    CUDA events on the launching stream) for the workload's Hamiltonian."""
+    import numpy as np
+    import torch
+    from lsquantumed_gb300.build import build
+    build()
+    import lsquantumed_gb300 as ed
+    wl = args.workload
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    env = ed.Environment(nspins=N)
+    b = ed.Basis(env, mag)
+    lat = ed.square2D(env, lx, ly) if ltype == 'square2D' else ed.chain1D(env)
+    H = ed.Hamiltonian(env, b, lat, J1, D1, J2, D2)
+    H.build_diag(env)
+    H.build_off_diag(env)
+    H.set_accumulation(args.acc)
+    dim = b.size
+    x = torch.empty(dim, dtype=torch.complex128, device='cuda')
+    x.real.uniform_(-1, 1)
+    x.imag.uniform_(-1, 1)
+    x /= torch.linalg.vector_norm(x)
+    y = torch.empty_like(x)
+    for _ in range(args.warmup):
+        H.apply(x, out=y)
+    torch.cuda.synchronize()
+    env.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+    e0.record(stream)
+    for _ in range(args.steps):
+        H.apply(x, out=y)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    n_hv, ms_hv = env.profile_read()
+    env.profile(False)
+    pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
+    bytes_row = 16 + 16 * kbar(N, b.nspins_up, pairs) + 16 + 4 + 8
+    ms = ms_hv / max(n_hv, 1)
+    peak, _ = measured_peaks()
+    gbs = dim * bytes_row / (ms * 1e-3) / 1e9
+    print(json.dumps({'mode': 'hv-only', 'workload': wl, 'acc': args.acc, 'dim': dim, 'launches': n_hv,
+                      'ms_per_hv': ms, 'ms_per_step_events': e0.elapsed_time(e1) / args.steps,
+                      'algorithmic_gbs': gbs, 'frac_of_measured_hbm': gbs / peak, 'bytes_per_row': bytes_row}))
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -365,7 +414,8 @@ def run_ours(args):
                      'bytes_per_row': bytes_row, 'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
                      'launches_timed': n_hv},
         'hv_gbs': achieved,
-        'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'eigenvalues': evals,
+        'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'ortho_passes': st['ortho_passes'],
+                   'eigenvalues': evals,
                    'rel_residuals': errs},
         'clocks': clocks, 'cpu_baseline': cpu,
     }
@@ -402,11 +452,15 @@ def main():
     ap.add_argument('--workload', default='c5', choices=sorted(WORKLOADS))
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
+    ap.add_argument('--acc', default='exact', choices=['exact', 'fixed64', 'fp64'], help='H.v accumulation')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == 'reference':
         return run_reference(args)
+    if args.hv_only:
+        return run_hv_only(args)
     return run_ours(args)
 
 

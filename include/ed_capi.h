@@ -40,7 +40,7 @@ enum {
 enum { ED_CHAIN1D = 0, ED_SQUARE2D = 1, ED_HONEYCOMB2D = 2 };  /* lattice_type, include/lattice.hpp */
 enum { ED_OP_SZSZ = 0, ED_OP_SPSM = 1, ED_OP_SMSP = 2, ED_OP_SISJ = 3 };  /* spinOperators/correlation.hpp */
 enum { ED_HAM_MATRIX_FREE = 0, ED_HAM_CSR = 1 };
-enum { ED_ACC_FP64 = 0, ED_ACC_EXACT = 1 };
+enum { ED_ACC_FP64 = 0, ED_ACC_EXACT = 1, ED_ACC_FIXED64 = 2 };
 
 typedef struct { double re, im; } ed_cplx;
 typedef struct ed_ctx ed_ctx;
@@ -129,11 +129,16 @@ int ed_ham_set_mode(ed_ham* h, int mode);
 /* Export the assembled matrix (rows sorted by column, duplicates summed in
  * the reference's order) — the parity view of Hamiltonian::hamilt. */
 int ed_ham_export_csr_host(ed_ham* h, int64_t* rowptr_host, int64_t* cols_host, double* vals_host, int64_t cap);
-/* Matrix-free H.v accumulation: ED_ACC_EXACT (default) sums the gathered
- * entries exactly in 128-bit integers (block floating point input, 2^-61
- * relative to each 32-state block's largest entry) and rounds once to FP64;
- * ED_ACC_FP64 adds them in FP64.  Per-bond Hamiltonians always use FP64.
- * (No counterpart in the reference: PETSc MatMult adds in FP64.) */
+/* Matrix-free H.v accumulation (no counterpart in the reference, whose PETSc
+ * MatMult adds in FP64):
+ *   ED_ACC_EXACT (default): the input is kept as block floating point (62-bit
+ *     mantissas, one exponent per 32 states) and the gathered entries are
+ *     summed exactly in 128-bit integers, then rounded once to FP64;
+ *   ED_ACC_FIXED64: the input is quantised to 64-bit fixed point against its
+ *     largest entry (error <= 2^-57 of max|x| per entry), sums exact in
+ *     int64, rounded once to FP64;
+ *   ED_ACC_FP64: gathered entries added in FP64.
+ * Per-bond Hamiltonians always use FP64. */
 int ed_ham_set_accumulation(ed_ham* h, int kind);
 /* Diagonal of the assembled matrix (MatGetDiagonal). */
 int ed_ham_diag_host(ed_ham* h, double* out_host);
@@ -158,8 +163,9 @@ int ed_eps_solve(ed_eps* e, int* nconv);
  * (optionally) the eigenvector into a device or host buffer. */
 int ed_eps_get_eigenpair(ed_eps* e, int i, double* eig, double* rel_err, ed_cplx* vec_dev);
 int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host);
-/* Iterations (restarts), H.v applications, eigenvalues reported. */
-int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported);
+/* Iterations (restarts), H.v applications, eigenvalues reported, and
+ * Gram-Schmidt update passes (one per step, two when refinement was needed). */
+int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported, int64_t* ortho_passes);
 int ed_eps_destroy(ed_eps* e);  /* Solver::SolverClean */
 
 /* ---- measurements: replace SiSj/SzSz/SpSm/SmSp::ExpectVal

@@ -14,7 +14,7 @@ ED_OK, ED_EINVAL, ED_ECUDA, ED_ENOMEM, ED_ESTATE, ED_ENOTCONV, ED_ENOTSUP = rang
 ED_CHAIN1D, ED_SQUARE2D, ED_HONEYCOMB2D = 0, 1, 2
 ED_OP_SZSZ, ED_OP_SPSM, ED_OP_SMSP, ED_OP_SISJ = 0, 1, 2, 3
 ED_HAM_MATRIX_FREE, ED_HAM_CSR = 0, 1
-ED_ACC_FP64, ED_ACC_EXACT = 0, 1
+ED_ACC_FP64, ED_ACC_EXACT, ED_ACC_FIXED64 = 0, 1, 2
 
 _ERRNAMES = {1: 'EINVAL', 2: 'ECUDA', 3: 'ENOMEM', 4: 'ESTATE', 5: 'ENOTCONV', 6: 'ENOTSUP'}
 
@@ -80,7 +80,7 @@ SIGNATURES = {
     'ed_eps_solve': [vp, P(i32)],
     'ed_eps_get_eigenpair': [vp, i32, P(dbl), P(dbl), vp],
     'ed_eps_get_eigenvector_host': [vp, i32, vp],
-    'ed_eps_get_stats': [vp, P(i32), P(i64), P(i32)],
+    'ed_eps_get_stats': [vp, P(i32), P(i64), P(i32), P(i64)],
     'ed_eps_destroy': [vp],
     'ed_expect_pairs': [vp, i32, vp, vp, i64, vp],
     'ed_expect_all_pairs': [vp, i32, vp, vp],

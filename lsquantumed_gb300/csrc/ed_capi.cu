@@ -498,7 +498,8 @@ int ed_ham_diag_host(ed_ham* h, double* out_host) {
 
 int ed_ham_set_accumulation(ed_ham* h, int kind) {
   if (!h) return ed_fail(ED_EINVAL, "null Hamiltonian");
-  if (kind != ED_ACC_FP64 && kind != ED_ACC_EXACT) return ed_fail(ED_EINVAL, "unknown accumulation kind");
+  if (kind != ED_ACC_FP64 && kind != ED_ACC_EXACT && kind != ED_ACC_FIXED64)
+    return ed_fail(ED_EINVAL, "unknown accumulation kind");
   h->hv_kernel = kind;
   return ED_OK;
 }

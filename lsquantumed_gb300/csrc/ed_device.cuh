@@ -25,6 +25,55 @@ __device__ __forceinline__ uint32_t ed_rank(uint32_t s, const uint32_t* __restri
   return r;
 }
 
+// Per-row rank state for incremental ranks of bond-flipped states: chunk
+// values, set bits below each chunk, and each chunk's table entry.
+template <int K>
+struct RowRank {
+  uint32_t cv[K];
+  int pc[K];
+  uint32_t tv[K];
+};
+
+template <int K>
+__device__ __forceinline__ uint32_t ed_tab_index(const RankTables& rt, int k, int p, uint32_t c) {
+  if (k == 0) return c;
+  if (k == K - 1) return (uint32_t)rt.base[k] + c;
+  return (uint32_t)rt.base[k] + ((uint32_t)p << rt.w[k]) + c;
+}
+
+template <int K>
+__device__ __forceinline__ void ed_row_rank(uint32_t s, const uint32_t* __restrict__ tab, const RankTables& rt,
+                                            RowRank<K>& R) {
+  int c = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    R.cv[k] = (s >> rt.off[k]) & ((1u << rt.w[k]) - 1u);
+    R.pc[k] = c;
+    R.tv[k] = tab[ed_tab_index<K>(rt, k, c, R.cv[k])];
+    c += __popc(R.cv[k]);
+  }
+}
+
+// Rank of the state with bond b flipped, from the unflipped state's rank r:
+// only chunks ci..cj change (the bond is antiparallel: exactly one of its
+// bits is set, so the set-bit count above chunk cj is unchanged).
+template <int K>
+__device__ __forceinline__ uint32_t ed_rank_flip(uint32_t r, uint32_t s, const uint32_t* __restrict__ tab,
+                                                 const RankTables& rt, const RowRank<K>& R, const BondSet& bs, int b) {
+  const int ci = bs.ci[b], cj = bs.cj[b];
+  const int d = ((s >> bs.lo[b]) & 1u) ? -1 : 1;
+  uint32_t rr = r;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (k >= ci && k <= cj) {
+      const uint32_t c = R.cv[k] ^ (uint32_t)bs.xm[b][k];
+      const int p = R.pc[k] + (k > ci ? d : 0);
+      rr += tab[ed_tab_index<K>(rt, k, p, c)] - R.tv[k];
+    }
+  }
+  return rr;
+}
+
 // Counter-based splitmix64 (deterministic, identical on host and device).
 __device__ __forceinline__ uint64_t ed_splitmix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ull;

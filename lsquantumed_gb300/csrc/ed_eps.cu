@@ -26,6 +26,7 @@ struct ed_eps {
   bool solved = false;
   int nconv = 0, its = 0, nrep = 0;
   int64_t nhv = 0;
+  int64_t ortho_passes = 0;
   std::vector<double> evals, errs;
   double2* pool = nullptr;            // column storage
   int pool_cols = 0;
@@ -93,7 +94,48 @@ static void eps_free(ed_eps* e) {
   e->pool_cols = 0;
 }
 
-// CGS with one conditional refinement.  h receives the j+1 coefficients.
+// Orthogonalise w = H v_j against V[0..j].  First the local Lanczos
+// projection (alpha = v_j^H w, and beta_{j-1} v_{j-1} when v_{j-1} is the
+// previous Lanczos vector, i.e. j > k), fused with the dot products of one
+// classical Gram-Schmidt pass against all of V[0..j]; then the CGS update,
+// and a second CGS pass only if the norm fell below eta = 1/sqrt(2) of its
+// value after the local projection (the DGKS criterion SLEPc applies by
+// default).  In exact arithmetic this is the same projection as plain CGS;
+// the local step removes the two large Lanczos components before the
+// refinement test, so the second pass is needed only when real cancellation
+// occurs.  h receives the total j+1 coefficients; norig = ||H v_j||.
+static int orthogonalize_lanczos(ed_eps* e, int j, int k, double beta_prev, std::vector<double2>& h, double* nw,
+                                 double* norig) {
+  ed_ctx* ctx = e->h->ctx;
+  const int64_t n = e->h->basis->dim;
+  std::vector<const double2*> cols(e->col.begin(), e->col.begin() + j + 1);
+  h.assign(j + 1, make_double2(0.0, 0.0));
+  double2 a;
+  double y2 = 0.0, w2 = 0.0, n2 = 0.0;
+  ED_TRY(ed_multidot(ctx, &cols[j], 1, e->w, n, &a, &y2));
+  *norig = std::sqrt(y2);
+  const bool three_term = j > k && j > 0;
+  std::vector<double2> c(j + 1);
+  ED_TRY(ed_local_multidot(ctx, cols.data(), j + 1, e->w, n, e->col[j], a, three_term ? e->col[j - 1] : nullptr,
+                           beta_prev, c.data(), &w2));
+  double n0 = std::sqrt(w2);
+  h[j].x += a.x;
+  h[j].y += a.y;
+  if (three_term) h[j - 1].x += beta_prev;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) ED_TRY(ed_multidot(ctx, cols.data(), j + 1, e->w, n, c.data(), nullptr));
+    ED_TRY(ed_update(ctx, cols.data(), j + 1, c.data(), e->w, n, &n2));
+    for (int i = 0; i <= j; ++i) { h[i].x += c[i].x; h[i].y += c[i].y; }
+    *nw = std::sqrt(n2);
+    e->ortho_passes++;
+    if (*nw >= 0.7071067811865476 * n0) break;
+    n0 = *nw;
+  }
+  return ED_OK;
+}
+
+// Plain CGS with one conditional refinement (used for the random vector
+// after an invariant subspace is found).
 static int orthogonalize(ed_eps* e, int j, std::vector<double2>& h, double* nw, double* norig) {
   ed_ctx* ctx = e->h->ctx;
   const int64_t n = e->h->basis->dim;
@@ -153,6 +195,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   }
   uint64_t rseed = e->seed + 0x51ED2701ull;
   e->nhv = 0;
+  e->ortho_passes = 0;
   int k = 0, nconv = 0, its = 0;
   std::vector<double> theta, Y;
   std::vector<double2> h;
@@ -163,7 +206,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
       ED_TRY(ed_launch_hv(H, e->col[j], e->w));
       e->nhv++;
       double nw, norig;
-      ED_TRY(orthogonalize(e, j, h, &nw, &norig));
+      ED_TRY(orthogonalize_lanczos(e, j, k, j > 0 ? beta[j - 1] : 0.0, h, &nw, &norig));
       alpha[j] = h[j].x;
       if (nw <= 1e-13 * norig) {
         // invariant subspace: continue with a random vector orthogonal to V
@@ -324,8 +367,9 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host) {
   return ED_OK;
 }
 
-int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported) {
+int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported, int64_t* ortho_passes) {
   if (!e) return ed_fail(ED_EINVAL, "null solver");
+  if (ortho_passes) *ortho_passes = e->ortho_passes;
   if (its) *its = e->its;
   if (n_hv) *n_hv = e->nhv;
   if (n_reported) *n_reported = e->nrep;

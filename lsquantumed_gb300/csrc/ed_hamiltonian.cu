@@ -130,16 +130,33 @@ int ed_launch_build_diag(ed_ham* h) {
 // ---------------------------------------------------------------------------
 // Off-diagonal bond set for H.v.
 // ---------------------------------------------------------------------------
+static void bond_chunks(const RankTables& rt, BondSet& bs, int b, int i, int j) {
+  const int lo = i < j ? i : j, hi = i < j ? j : i;
+  int ci = 0, cj = 0;
+  for (int k = 0; k < rt.K; ++k) {
+    if (lo >= rt.off[k] && lo < rt.off[k] + rt.w[k]) ci = k;
+    if (hi >= rt.off[k] && hi < rt.off[k] + rt.w[k]) cj = k;
+  }
+  bs.ci[b] = (uint8_t)ci;
+  bs.cj[b] = (uint8_t)cj;
+  bs.lo[b] = (uint8_t)lo;
+  const uint32_t m = (1u << i) | (1u << j);
+  for (int k = 0; k < ED_RANK_MAX_CHUNKS; ++k)
+    bs.xm[b][k] = k < rt.K ? (uint16_t)((m >> rt.off[k]) & ((1u << rt.w[k]) - 1u)) : 0;
+}
+
 void ed_ham_make_bondset(ed_ham* h) {
   BondSet& bs = h->bs;
   memset(&bs, 0, sizeof(bs));
   if (!h->offdiag_built) return;
+  const RankTables& rt = h->basis->rt;
   if (h->per_bond) {
     bs.per_bond = 1;
     for (size_t b = 0; b < h->bi.size(); ++b) {
       bs.mask[bs.nb] = (1u << h->bi[b]) | (1u << h->bj[b]);
       bs.type[bs.nb] = (uint8_t)bs.nb;
       bs.chalf[bs.nb] = h->bJ[b] * 0.5;
+      bond_chunks(rt, bs, bs.nb, h->bi[b], h->bj[b]);
       ++bs.nb;
     }
     bs.ntypes = bs.nb;
@@ -154,8 +171,26 @@ void ed_ham_make_bondset(ed_ham* h) {
     if (std::fabs(J) < 1e-14) continue;  // pass skipped (tmpl_func.hpp:246, 280)
     bs.mask[bs.nb] = (1u << h->bi[b]) | (1u << h->bj[b]);
     bs.type[bs.nb] = (uint8_t)t;
+    bond_chunks(rt, bs, bs.nb, h->bi[b], h->bj[b]);
     ++bs.nb;
   }
+  // segments for the fixed-point kernel (order within a row is irrelevant
+  // there: integer sums are exact)
+  BondSegments& sg = h->segs;
+  memset(&sg, 0, sizeof(sg));
+  int n = 0, cls = 0;
+  for (int ci = 0; ci < ED_RANK_MAX_CHUNKS; ++ci)
+    for (int cj = ci; cj < ED_RANK_MAX_CHUNKS; ++cj, ++cls)
+      for (int t = 0; t < 2; ++t) {
+        sg.seg[cls * 2 + t] = n;
+        for (int b = 0; b < bs.nb; ++b) {
+          if (bs.ci[b] != ci || bs.cj[b] != cj || bs.type[b] != t) continue;
+          if (__builtin_popcount(bs.mask[b]) != 2) continue;  // i == j never couples
+          sg.word[n++] = (unsigned long long)bs.mask[b] | ((unsigned long long)bs.xm[b][ci] << 32) |
+                         ((unsigned long long)bs.xm[b][cj] << 48);
+        }
+      }
+  sg.seg[2 * ED_NCLASS] = n;
 }
 
 void ed_ham_unique_masks(const ed_ham* h, std::vector<uint32_t>& masks, std::vector<double>& vals) {
@@ -187,13 +222,15 @@ __global__ void __launch_bounds__(256) k_hv_gather(const uint32_t* __restrict__ 
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const uint32_t s = states[r];
+    RowRank<K> R;
+    ed_row_rank<K>(s, stab, rt, R);
     double a0r = 0.0, a0i = 0.0, a1r = 0.0, a1i = 0.0;
 #pragma unroll 4
     for (int b = 0; b < bs.nb; ++b) {
       const uint32_t m = bs.mask[b];
       const uint32_t t = s & m;
       if (t != 0u && t != m) {
-        const uint32_t c = ed_rank<K>(s ^ m, stab, rt);
+        const uint32_t c = ed_rank_flip<K>((uint32_t)r, s, stab, rt, R, bs, b);
         const double2 v = __ldg(&x[c]);
         if (PERBOND) {
           const double ch = bs.chalf[b];
@@ -341,6 +378,8 @@ __global__ void __launch_bounds__(256) k_hv_fixed(const uint32_t* __restrict__ s
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const uint32_t s = states[r];
+    RowRank<K> R;
+    ed_row_rank<K>(s, stab, rt, R);
     Acc128 a0r = {0, 0}, a0i = {0, 0}, a1r = {0, 0}, a1i = {0, 0};
     bool bad = false;
 #pragma unroll 4
@@ -348,7 +387,7 @@ __global__ void __launch_bounds__(256) k_hv_fixed(const uint32_t* __restrict__ s
       const uint32_t m = bs.mask[b];
       const uint32_t t = s & m;
       if (t != 0u && t != m) {
-        const uint32_t c = ed_rank<K>(s ^ m, stab, rt);
+        const uint32_t c = ed_rank_flip<K>((uint32_t)r, s, stab, rt, R, bs, b);
         const longlong2 q = __ldg(&xq[c]);
         const int eb = (int)__ldg(&xe[c >> 5]);
         bad |= (q.x == (long long)0x8000000000000000ull) | (q.y == (long long)0x8000000000000000ull);
@@ -373,12 +412,170 @@ __global__ void __launch_bounds__(256) k_hv_fixed(const uint32_t* __restrict__ s
   }
 }
 
+// ---------------------------------------------------------------------------
+// 64-bit fixed point: x is quantised once per H.v against its largest entry,
+// q = round(v * 2^(S - (Emax - 1022))) with |q| <= 2^S, where 2^(Emax-1022)
+// bounds every |v| and S = 62 - ceil(log2(max bonds per coupling type + 1)),
+// so a row's sum of one coupling type cannot overflow int64.  Each gathered
+// term is then one 64-bit add; the sums are exact and rounded once to FP64.
+// Quantisation error per entry <= 2^-(S+1) of the largest |v|.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_max_exponent(const double2* __restrict__ x, int64_t dim,
+                                                      int* __restrict__ gmax, int* __restrict__ nonfinite) {
+  int m = 0, nf = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const double2 v = x[r];
+    const int er = (int)(((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7FF);
+    const int ei = (int)(((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7FF);
+    nf |= (er == 0x7FF) | (ei == 0x7FF);
+    m = max(m, max(er == 0x7FF ? 0 : er, ei == 0x7FF ? 0 : ei));
+  }
+  m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+  nf = (int)__reduce_or_sync(0xffffffffu, (unsigned)nf);
+  if ((threadIdx.x & 31) == 0) {
+    if (m > 0) atomicMax(gmax, m);
+    if (nf) atomicOr(nonfinite, 1);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_quantize64(const double2* __restrict__ x, int64_t dim, const int* __restrict__ gmax_p,
+                                                    int sbits, longlong2* __restrict__ xq) {
+  const int emax = *gmax_p;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const double2 v = x[r];
+    const unsigned long long bits[2] = {(unsigned long long)__double_as_longlong(v.x),
+                                        (unsigned long long)__double_as_longlong(v.y)};
+    long long q[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int e = (int)((bits[k] >> 52) & 0x7FF);
+      long long m = 0;
+      if (e == 0x7FF) {
+        m = (long long)0x8000000000000000ull;  // non-finite sentinel
+      } else if (e != 0) {
+        const unsigned long long mant = (bits[k] & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+        const int sh = e - emax + sbits - 53;  // q = mant * 2^sh, sh <= sbits - 53
+        unsigned long long a;
+        if (sh >= 0) a = mant << sh;
+        else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);  // round half up in magnitude
+        else a = 0;
+        m = (long long)a;
+        if (bits[k] >> 63) m = -m;
+      }
+      q[k] = m;
+    }
+    xq[r] = make_longlong2(q[0], q[1]);
+  }
+}
+
+// One (chunk class, type) segment of the fixed-point kernel: rank of the
+// flipped state from the row's rank (only chunks CI..CJ change), predicated
+// gathers four bonds at a time so several loads are in flight per thread.
+template <int K, int CI, int CJ>
+__device__ __forceinline__ void fx64_segment(const BondSegments& sg, int b0, int b1, uint32_t s, uint32_t r,
+                                             const uint32_t* __restrict__ stab, const RankTables& rt,
+                                             const RowRank<K>& R, const longlong2* __restrict__ xq, long long& ar,
+                                             long long& ai, bool& bad) {
+  constexpr int U = 4;
+  const long long kNaN = (long long)0x8000000000000000ull;
+  for (int b = b0; b < b1; b += U) {
+    uint32_t c[U];
+    bool on[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool inb = b + u < b1;
+      const unsigned long long w = inb ? sg.word[b + u] : 0ull;
+      const uint32_t m = (uint32_t)w;
+      const uint32_t t = s & m;
+      on[u] = inb && t != 0u && t != m;
+      uint32_t rr = r;
+      if (CI == CJ) {
+        const uint32_t cc = R.cv[CI] ^ (uint32_t)((w >> 32) & 0xFFFFu);
+        rr += stab[ed_tab_index<K>(rt, CI, R.pc[CI], cc)] - R.tv[CI];
+      } else {
+        const int d = (s & m & (0u - m)) ? -1 : 1;  // lowest bond bit set -> one fewer below
+#pragma unroll
+        for (int k = CI; k <= CJ; ++k) {
+          uint32_t cc = R.cv[k];
+          if (k == CI) cc ^= (uint32_t)((w >> 32) & 0xFFFFu);
+          if (k == CJ) cc ^= (uint32_t)(w >> 48);
+          const int p = R.pc[k] + (k > CI ? d : 0);
+          rr += stab[ed_tab_index<K>(rt, k, p, cc)] - R.tv[k];
+        }
+      }
+      c[u] = on[u] ? rr : r;
+    }
+    longlong2 q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[c[u]]) : make_longlong2(0, 0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
+      ar += q[u].x;
+      ai += q[u].y;
+    }
+  }
+}
+
+template <int K, int CI, int CJ>
+__device__ __forceinline__ void fx64_class(const BondSegments& sg, uint32_t s, uint32_t r, const uint32_t* stab,
+                                           const RankTables& rt, const RowRank<K>& R, const longlong2* xq,
+                                           long long (&a)[4], bool& bad) {
+  if (CJ >= K) return;
+  constexpr int cls = CI * (2 * ED_RANK_MAX_CHUNKS - CI + 1) / 2 + (CJ - CI);
+  fx64_segment<K, CI, CJ>(sg, sg.seg[2 * cls], sg.seg[2 * cls + 1], s, r, stab, rt, R, xq, a[0], a[1], bad);
+  fx64_segment<K, CI, CJ>(sg, sg.seg[2 * cls + 1], sg.seg[2 * cls + 2], s, r, stab, rt, R, xq, a[2], a[3], bad);
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) k_hv_fx64(const uint32_t* __restrict__ states, const double* __restrict__ diag,
+                                                 const double2* __restrict__ x, const longlong2* __restrict__ xq,
+                                                 const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
+                                                 int64_t dim, const RankTables rt, const BondSegments sg,
+                                                 double c0, double c1) {
+  extern __shared__ uint32_t stab[];
+  ed_load_tables(stab, rt);
+  // one unit = 2^(emax - 1022 - sbits), applied as two normal factors
+  const int e_unit = *gmax_p - 1022 - sbits;
+  const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
+  const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const uint32_t s = states[r];
+    RowRank<K> R;
+    ed_row_rank<K>(s, stab, rt, R);
+    long long a[4] = {0, 0, 0, 0};  // nn re, nn im, nnn re, nnn im
+    bool bad = false;
+    const uint32_t rr = (uint32_t)r;
+    fx64_class<K, 0, 0>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 1, 1>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 2, 2>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 3, 3>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 0, 1>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 1, 2>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 2, 3>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 0, 2>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 1, 3>(sg, s, rr, stab, rt, R, xq, a, bad);
+    fx64_class<K, 0, 3>(sg, s, rr, stab, rt, R, xq, a, bad);
+    const double d = diag[r];
+    const double2 xv = x[r];
+    const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
+    const double s1r = (double)a[2] * s1 * s2, s1i = (double)a[3] * s1 * s2;
+    double yr = fma(d, xv.x, fma(c0, s0r, c1 * s1r));
+    double yi = fma(d, xv.y, fma(c0, s0i, c1 * s1i));
+    if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
+    y[r] = make_double2(yr, yi);
+  }
+}
+
 static int ensure_fixed_buffers(ed_ham* h) {
   const int64_t dim = h->basis->dim;
   if (!h->d_xq) {
     if (cudaMalloc(&h->d_xq, sizeof(longlong2) * (size_t)dim) != cudaSuccess ||
         cudaMalloc(&h->d_xe, sizeof(uint16_t) * (size_t)((dim + 31) / 32)) != cudaSuccess ||
-        cudaMalloc(&h->d_gmax, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&h->d_gmax, 2 * sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
       return ed_fail(ED_ENOMEM, "H.v scratch does not fit in device memory");
     }
@@ -409,9 +606,54 @@ static int launch_hv_fixed_k(ed_ham* h, const double2* x, double2* y) {
   return ED_OK;
 }
 
+// Largest number of bonds of one coupling type, for the fixed-point headroom.
+static int max_type_count(const BondSet& bs) {
+  int c[2] = {0, 0};
+  for (int b = 0; b < bs.nb; ++b) c[bs.type[b] & 1]++;
+  return c[0] > c[1] ? c[0] : c[1];
+}
+
+template <int K>
+static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  ED_TRY(ensure_fixed_buffers(h));
+  int head = 0;
+  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
+  const int sbits = 62 - head;
+  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 2 * sizeof(int), ctx->stream));
+  const int g = grid_cap(ctx, b->dim, 256, 8);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
+  ED_CHECK_LAUNCH(ctx);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, sbits, h->d_xq);
+  ED_CHECK_LAUNCH(ctx);
+  size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
+  static bool attr_set[5] = {false};
+  if (!attr_set[K]) {
+    ED_CUDA(cudaFuncSetAttribute(k_hv_fx64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+    attr_set[K] = true;
+  }
+  int per_sm = 0;
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_fx64<K>, 256, smem));
+  if (per_sm < 1) per_sm = 1;
+  k_hv_fx64<K><<<grid_cap(ctx, b->dim, 256, per_sm), 256, smem, ctx->stream>>>(
+      b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, b->rt, h->segs, h->bs.chalf[0],
+      h->bs.chalf[1]);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
 static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
   if (h->mode == ED_HAM_CSR && h->d_rowptr) return ed_launch_csr_spmv(h, x, y);
   const bool pb = h->bs.per_bond != 0;
+  if (!pb && h->hv_kernel == 2) {
+    switch (h->basis->rt.K) {
+      case 1: return launch_hv_fx64_k<1>(h, x, y);
+      case 2: return launch_hv_fx64_k<2>(h, x, y);
+      case 3: return launch_hv_fx64_k<3>(h, x, y);
+      default: return launch_hv_fx64_k<4>(h, x, y);
+    }
+  }
   if (!pb && h->hv_kernel == 1) {
     switch (h->basis->rt.K) {
       case 1: return launch_hv_fixed_k<1>(h, x, y);

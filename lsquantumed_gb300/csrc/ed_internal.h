@@ -56,13 +56,29 @@ struct RankTables {
 
 // Bonds in the order the reference visits them, with coupling types.
 // mask = (1 << i) | (1 << j); type indexes the per-type coefficients.
+// For the incremental rank: a bond (i, j), i < j, lies in chunks ci <= cj
+// of the rank tables; flipping it changes only the table entries of chunks
+// ci..cj (the chunk values of ci and cj, and the set-bit count below every
+// chunk in (ci, cj]).  xm[b][k] is the bond's mask restricted to chunk k.
 struct BondSet {
   int nb;
   int ntypes;
   int per_bond;                   // 1: one type per bond (J_b, D_b)
   uint32_t mask[ED_MAX_BONDS];
   uint8_t type[ED_MAX_BONDS];
+  uint8_t ci[ED_MAX_BONDS], cj[ED_MAX_BONDS], lo[ED_MAX_BONDS];
+  uint16_t xm[ED_MAX_BONDS][ED_RANK_MAX_CHUNKS];
   double chalf[ED_MAX_TYPES];     // J_t * 0.5 (off-diagonal element per bond)
+};
+
+// Bonds regrouped for the fixed-point H.v kernel: segments by (chunk class
+// (ci, cj), coupling type); each bond packed as
+// mask | xm[ci] << 32 | xm[cj] << 48.  Segment s = (class * 2 + type) spans
+// word[seg[s] .. seg[s+1]).  Classes enumerate (ci, cj), ci <= cj, row-major.
+#define ED_NCLASS 10
+struct BondSegments {
+  int seg[2 * ED_NCLASS + 1];
+  unsigned long long word[ED_MAX_BONDS];
 };
 
 struct ed_ctx {
@@ -118,7 +134,8 @@ struct ed_ham {
   longlong2* d_xq = nullptr;      // 62-bit mantissas, (re, im) per state
   uint16_t* d_xe = nullptr;       // biased exponent per 32-state block
   int* d_gmax = nullptr;          // largest block exponent
-  int hv_kernel = 1;              // 0: FP64 accumulation, 1: exact integer accumulation
+  int hv_kernel = 2;              // 0: FP64, 1: exact 128-bit, 2: 64-bit fixed point
+  BondSegments segs{};
 };
 
 // ---------------------------------------------------------------------------
@@ -145,6 +162,8 @@ int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* 
                 double2* h_host, double* wnorm2_host);
 int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_host, double2* w, int64_t n,
               double* wnorm2_host);
+int ed_local_multidot(ed_ctx* ctx, const double2* const* cols, int nv, double2* w, int64_t n, const double2* vj,
+                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host);
 int ed_scale_copy(ed_ctx* ctx, const double2* src, double2* dst, double s, int64_t n);
 int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const double* Y, int ldY, int l,
                        double2* const* out, int64_t n);

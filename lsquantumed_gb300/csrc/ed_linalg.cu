@@ -140,6 +140,78 @@ int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* 
   return ED_OK;
 }
 
+// Local Lanczos projection fused with the first group of the full CGS dot
+// products: w <- w - a v_j - b v_{j-1} (written back when `local` is set),
+// then partial[i] = V_{v0+i}^H w and ||w||^2.
+template <int G>
+__global__ void __launch_bounds__(ED_RED_THREADS) k_local_multidot(const ColPtrs cp, int v0, int ng,
+                                                                   double2* __restrict__ w, int64_t n, int local,
+                                                                   const double2* __restrict__ vj, double2 a,
+                                                                   const double2* __restrict__ vjm1, double b,
+                                                                   int with_norm, double* __restrict__ partial, int nblk) {
+  double acc[2 * G + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * G + 1; ++k) acc[k] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    double2 wv = w[r];
+    if (local) {
+      const double2 p = vj[r];
+      wv.x = fma(-a.x, p.x, fma(a.y, p.y, wv.x));
+      wv.y = fma(-a.x, p.y, fma(-a.y, p.x, wv.y));
+      if (vjm1) {
+        const double2 q = vjm1[r];
+        wv.x = fma(-b, q.x, wv.x);
+        wv.y = fma(-b, q.y, wv.y);
+      }
+      w[r] = wv;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g < ng) {
+        const double2 v = cp.p[v0 + g][r];
+        acc[2 * g] = fma(v.x, wv.x, fma(v.y, wv.y, acc[2 * g]));
+        acc[2 * g + 1] = fma(v.x, wv.y, fma(-v.y, wv.x, acc[2 * g + 1]));
+      }
+    }
+    if (with_norm) acc[2 * G] = fma(wv.x, wv.x, fma(wv.y, wv.y, acc[2 * G]));
+  }
+  __shared__ double sh[(2 * G + 1) * 32];
+  block_reduce<2 * G + 1>(acc, sh);
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < ng; ++g) {
+      partial[(size_t)(2 * (v0 + g)) * nblk + blockIdx.x] = acc[2 * g];
+      partial[(size_t)(2 * (v0 + g) + 1) * nblk + blockIdx.x] = acc[2 * g + 1];
+    }
+    if (with_norm) partial[(size_t)(2 * (v0 + ng)) * nblk + blockIdx.x] = acc[2 * G];
+  }
+}
+
+int ed_local_multidot(ed_ctx* ctx, const double2* const* cols, int nv, double2* w, int64_t n, const double2* vj,
+                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host) {
+  if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  const int nblk = red_blocks(ctx, n);
+  const int items = 2 * nv + 1;
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items));
+  ColPtrs cp = make_cols(cols, nv);
+  // the norm item must be computed after the local update: it is produced by
+  // the last group, which runs after the first (local) one on the stream
+  const int ngroups = (nv + ED_GROUP - 1) / ED_GROUP;
+  for (int gidx = 0; gidx < ngroups; ++gidx) {
+    const int v0 = gidx * ED_GROUP;
+    const int ng = std::min(ED_GROUP, nv - v0);
+    const int last = gidx == ngroups - 1;
+    k_local_multidot<ED_GROUP><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, gidx == 0, vj, a, vjm1, b,
+                                                                         last, ctx->d_red, nblk);
+    ED_CHECK_LAUNCH(ctx);
+  }
+  std::vector<double> out(items);
+  ED_TRY(finish_reduce(ctx, items, nblk, out.data()));
+  for (int i = 0; i < nv; ++i) { h_host[i].x = out[2 * i]; h_host[i].y = out[2 * i + 1]; }
+  if (wnorm2_host) *wnorm2_host = out[2 * nv];
+  return ED_OK;
+}
+
 // w <- w - sum_i V_i h_i ; partial ||w||^2
 __global__ void __launch_bounds__(ED_RED_THREADS) k_update(const ColPtrs cp, int nv, const double2* __restrict__ h,
                                                            double2* __restrict__ w, int64_t n, double* __restrict__ partial,

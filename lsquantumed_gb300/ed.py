@@ -325,8 +325,11 @@ class Hamiltonian:
              capi.ED_HAM_MATRIX_FREE)
 
     def set_accumulation(self, kind):
-        """'exact' (128-bit integer sums, default) or 'fp64' for the matrix-free H.v."""
-        call('ed_ham_set_accumulation', self._h, capi.ED_ACC_EXACT if kind == 'exact' else capi.ED_ACC_FP64)
+        """Matrix-free H.v accumulation: 'exact' (128-bit integer sums of block
+        floating point input, default), 'fixed64' (64-bit fixed point input) or
+        'fp64'."""
+        k = {'exact': capi.ED_ACC_EXACT, 'fixed64': capi.ED_ACC_FIXED64, 'fp64': capi.ED_ACC_FP64}[kind]
+        call('ed_ham_set_accumulation', self._h, k)
 
     def export_csr(self):
         """(rowptr, cols, vals) of the assembled matrix, rows sorted by column."""
@@ -389,9 +392,9 @@ class EPS:
             call('ed_eps_set_initial_vector', self._h, _p(v), 1 if v.is_cuda else 0)
 
     def stats(self):
-        its, nhv, nrep = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int()
-        call('ed_eps_get_stats', self._h, ctypes.byref(its), ctypes.byref(nhv), ctypes.byref(nrep))
-        return {'its': its.value, 'nhv': nhv.value, 'nreported': nrep.value}
+        its, nhv, nrep, op = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
+        call('ed_eps_get_stats', self._h, ctypes.byref(its), ctypes.byref(nhv), ctypes.byref(nrep), ctypes.byref(op))
+        return {'its': its.value, 'nhv': nhv.value, 'nreported': nrep.value, 'ortho_passes': op.value}
 
     def destroy(self):
         if getattr(self, '_h', None):

@@ -203,7 +203,7 @@ def test_per_bond_bit_exact(ed, envs):
 def test_hv_matches_oracle(ed, envs, case):
     ltype, N, lx, ly, mag, J1, D1, J2, D2 = case
     env, b, h, M = make_pair(ed, envs, ltype, N, lx, ly, mag, J1, D1, J2, D2)
-    for acc in ('exact', 'fp64'):
+    for acc in ('exact', 'fixed64', 'fp64'):
         h.set_accumulation(acc)
         for seed in (1, 2):
             x = oracle.start_vector(seed, b.size)
@@ -216,7 +216,7 @@ def test_hv_matches_oracle(ed, envs, case):
     x = oracle.start_vector(3, b.size) * np.exp(np.linspace(-30, 5, b.size))
     x[::7] = 0.0
     y_ref = M.apply(x)
-    for acc in ('exact', 'fp64'):
+    for acc in ('exact', 'fixed64', 'fp64'):
         h.set_accumulation(acc)
         assert np.abs(h.apply(x).cpu().numpy() - y_ref).max() <= 1e-14 * np.linalg.norm(x), acc
     h.set_mode('csr')
@@ -249,7 +249,7 @@ def test_hv_nonfinite_input(ed, envs):
     env, b, h, M = make_pair(ed, envs, 0, 12, 1, 12, 0, 1.0, 1.0, 0.0, 0.0)
     x = oracle.start_vector(1, b.size)
     x[100] = np.nan
-    for acc in ('exact', 'fp64'):
+    for acc in ('exact', 'fixed64', 'fp64'):
         h.set_accumulation(acc)
         y = h.apply(x).cpu().numpy()
         assert np.isnan(y[100])
