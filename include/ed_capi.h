@@ -122,6 +122,21 @@ int ed_ham_build_disorder(ed_ham* h, const double* hi_host);
 int ed_ham_apply(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev);
 /* Same with host buffers (copies in and out on the context's stream). */
 int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host);
+/* y = H x (device vectors) without allocating any device memory: for
+ * callers that cannot let a library call cudaMalloc, e.g. code running under
+ * a framework that owns the whole device memory pool, or a loop that cannot
+ * afford the synchronisation an allocation may bring.  No counterpart in the
+ * reference.  Same fixed-point H.v as ed_ham_apply (ED_ACC_FIXED64), with its
+ * scratch in one static device array reserved when the library's module is
+ * loaded, so every GPU that loads the library holds ED_NOALLOC_MAX_STATES *
+ * 16 + 256 bytes (64 MiB) until the process exits.  Limits: at most
+ * ED_NOALLOC_MAX_STATES basis states (ED_EINVAL beyond), uniform J1/J2
+ * Hamiltonians only (ED_ENOTSUP for per-bond ones).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race on it, so order them. */
+#define ED_NOALLOC_MAX_STATES (1 << 22)
+int ed_ham_apply_noalloc(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev);
 /* Explicit CSR on the device (when it fits); then ed_ham_set_mode(ED_HAM_CSR)
  * makes ed_ham_apply / the solver use the CSR SpMV. */
 int ed_ham_build_csr(ed_ham* h, int64_t* nnz);

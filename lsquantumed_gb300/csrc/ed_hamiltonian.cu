@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <mutex>
 
 struct DiagParams {
   int nb;
@@ -863,4 +864,91 @@ int ed_launch_csr_spmv(ed_ham* h, const double2* x, double2* y) {
   k_csr_spmv<<<grid_cap(ctx, dim * 8, 256, 8), 256, 0, ctx->stream>>>(h->d_rowptr, h->d_cols, h->d_vals, x, y, dim);
   ED_CHECK_LAUNCH(ctx);
   return ED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// H.v without any device allocation.
+//
+// ed_ham_apply keeps its quantised copy of x in buffers it allocates on first
+// use.  Some callers cannot let a library call cudaMalloc: code that runs
+// under a host framework which owns the whole device memory pool, or a
+// latency-critical loop that cannot afford the implicit device
+// synchronisation an allocation may bring.  ed_ham_apply_noalloc runs the
+// same fixed-point H.v (quantise, then gather with exact int64 sums) but keeps
+// its scratch in the file-scope array below, which the CUDA module reserves
+// when it is loaded, so the call itself allocates nothing.  It is limited to
+// ED_NOALLOC_MAX_STATES basis states.
+//
+// Layout of the scratch array: the first 256 bytes hold the largest exponent
+// and the non-finite flag (cleared at every call); the quantised input
+// (16 bytes per state) follows.  Every call shares this one array, so calls
+// that overlap on the GPU (different streams, or different host threads)
+// race on it; the caller must order them.
+// ---------------------------------------------------------------------------
+#define ED_NOALLOC_HEADER_BYTES 256
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ED_NOALLOC_HEADER_BYTES +
+                                                                  (size_t)ED_NOALLOC_MAX_STATES * sizeof(longlong2)];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is not a device address).
+static int noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= 64) return ed_fail(ED_ENOTSUP, "device index above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return ed_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    g_noalloc_ptr[device] = p;
+  }
+  *out = (unsigned char*)g_noalloc_ptr[device];
+  return ED_OK;
+}
+
+template <int K>
+static int launch_hv_noalloc_k(ed_ham* h, const double2* x, double2* y, unsigned char* scratch) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  int* gmax = (int*)scratch;
+  longlong2* xq = (longlong2*)(scratch + ED_NOALLOC_HEADER_BYTES);
+  int head = 0;
+  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
+  const int sbits = 62 - head;
+  ED_CUDA(cudaMemsetAsync(gmax, 0, 2 * sizeof(int), ctx->stream));
+  const int g = grid_cap(ctx, b->dim, 256, 8);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, gmax + 1);
+  ED_CHECK_LAUNCH(ctx);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, sbits, xq);
+  ED_CHECK_LAUNCH(ctx);
+  size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
+  ED_CUDA(cudaFuncSetAttribute(k_hv_fx64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  int per_sm = 0;
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_fx64<K>, 256, smem));
+  if (per_sm < 1) per_sm = 1;
+  k_hv_fx64<K><<<grid_cap(ctx, b->dim, 256, per_sm), 256, smem, ctx->stream>>>(
+      b->d_states, h->d_diag, x, xq, gmax, sbits, y, b->dim, b->rt, h->segs, h->bs.chalf[0], h->bs.chalf[1]);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+extern "C" int ed_ham_apply_noalloc(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev) {
+  if (!h || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
+  if ((const void*)x_dev == (const void*)y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
+  if (h->per_bond) return ed_fail(ED_ENOTSUP, "ed_ham_apply_noalloc supports uniform J1/J2 couplings only");
+  if (h->basis->dim > (int64_t)ED_NOALLOC_MAX_STATES)
+    return ed_fail(ED_EINVAL, "ed_ham_apply_noalloc handles at most " + std::to_string((long long)ED_NOALLOC_MAX_STATES) +
+                                  " basis states; this basis has " + std::to_string((long long)h->basis->dim));
+  ED_CUDA(cudaSetDevice(h->ctx->device));
+  unsigned char* scratch = nullptr;
+  ED_TRY(noalloc_scratch(h->ctx->device, &scratch));
+  const double2* x = (const double2*)x_dev;
+  double2* y = (double2*)y_dev;
+  switch (h->basis->rt.K) {
+    case 1: return launch_hv_noalloc_k<1>(h, x, y, scratch);
+    case 2: return launch_hv_noalloc_k<2>(h, x, y, scratch);
+    case 3: return launch_hv_noalloc_k<3>(h, x, y, scratch);
+    default: return launch_hv_noalloc_k<4>(h, x, y, scratch);
+  }
 }
