@@ -223,6 +223,86 @@ def workload_config(wl):
             'l2': 'inputs larger than L2 (each vector %.2f GB)' % (16 * math.comb(N, mag + N // 2) / 1e9)}
 
 
+def run_disorder(args):
+    """C3: disorder sweep, chain N=20 (J1=1, J2=0.2, Delta=1), h_i ~ U[-2, 2]
+    from mt19937_64(seed) for seed = 0..511 (RandomDisorder::hi_init with
+    srand_seq[k] = seed), Sz = 0, 1, 2: 1536 solves (lowest 2 pairs,
+    eps_tol 1e-9).  Batched: one lockstep batch per sector.  Plain: the same
+    solves issued one at a time (a bounded subset, timed per solve)."""
+    import numpy as np
+    import torch
+    from lsquantumed_gb300.build import build
+    build()
+    import lsquantumed_gb300 as ed
+    N, J1, J2, W, nev, tol = 20, 1.0, 0.2, 2.0, 2, 1e-9
+    nseeds = args.seeds
+    env = ed.Environment(nspins=N)
+    fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in range(nseeds)])
+    sectors = (0, 1, 2)
+    hams = {}
+    for mag in sectors:
+        b = ed.Basis(env, mag)
+        h = ed.Hamiltonian(env, b, ed.chain1D(env), J1, 1.0, J2, J2)
+        h.build_diag(env)
+        h.build_off_diag(env)
+        hams[mag] = (b, h)
+    # batched
+    for _ in range(1 if args.warmup else 0):  # warm-up on a small batch
+        bt = ed.DisorderBatch(hams[0][1], fields[:8])
+        bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
+        del bt
+    torch.cuda.synchronize()
+    k0 = env.kernel_count()
+    t0 = time.perf_counter()
+    max_err, its, bad = 0.0, [], 0
+    batch_evals = {}
+    for mag in sectors:
+        bt = ed.DisorderBatch(hams[mag][1], fields)
+        r = bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
+        max_err = max(max_err, float(r['errs'].max()))
+        bad += int((r['nconv'] < nev).sum())
+        its.append(r['its'])
+        batch_evals[mag] = r['evals']
+        del bt
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    launches = env.kernel_count() - k0
+    nsolve = nseeds * len(sectors)
+    # plain: one solve at a time on a subset
+    nplain = min(args.plain_sample, nseeds)
+    t0 = time.perf_counter()
+    agree = True
+    for mag in sectors:
+        b, _ = hams[mag]
+        for sd in range(nplain):
+            h = ed.Hamiltonian(env, b, ed.chain1D(env), J1, 1.0, J2, J2)
+            h.build_diag(env)
+            h.build_off_diag(env)
+            h.build_disorder(env, fields[sd])
+            eps = ed.Solver.SolverInit(h, nev, 16)
+            ed.Solver.EPSSetTolerances(eps, tol)
+            ed.Solver.solve(env, eps)
+            for i in range(nev):
+                e, _ = ed.Solver.eigenvalue(eps, i)
+                agree &= abs(e - batch_evals[mag][sd][i]) <= 1e-8 * abs(e)
+            ed.Solver.SolverClean(eps)
+    torch.cuda.synchronize()
+    t_plain = (time.perf_counter() - t0) / (nplain * len(sectors))
+    line = {'metric': METRIC, 'workload': 'c3', 'value': nsolve / t_batch, 'unit': 'samples/s',
+            'higher_is_better': True, 'n_gpus': 1, 'steps': 1, 'warmup': args.warmup,
+            'batched': {'samples_per_s': nsolve / t_batch, 'seconds': t_batch, 'solves': nsolve,
+                        'restarts_per_sector': its, 'max_rel_residual': max_err, 'unconverged': bad,
+                        'gpu_launches': launches},
+            'plain': {'samples_per_s': 1.0 / t_plain, 'seconds_per_solve': t_plain,
+                      'sample': '%d seeds x %d sectors, one solve at a time' % (nplain, len(sectors))},
+            'batched_over_plain': (nsolve / t_batch) * t_plain,
+            'eigenvalues_agree_1e-8': bool(agree), 'dtype': 'c128', 'data': 'synthetic',
+            'config': {'workload': 'c3 chain1D N=20 J1=1 J2=0.2 Delta=1, h_i~U[-2,2] seeds 0..%d, Sz=0,1,2, '
+                                   'nev=2, ncv=16, eps_tol=1e-9' % (nseeds - 1), 'dims': [b.size for b, _ in hams.values()]}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_hv_only(args):
     """Time the matrix-free H.v alone (K launches after W warm-up launches,
     CUDA events on the launching stream) for the workload's Hamiltonian."""
@@ -344,13 +424,14 @@ def run_ours(args):
     hv_ms = ms_hv / max(n_hv, 1)
     achieved = dim * bytes_row / (hv_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = None
+    traffic, traffic_note = None, None
     tp = os.path.join(ROOT, 'profiles', 'hv_traffic.json')
     if os.path.exists(tp):
         try:
-            tj = json.load(open(tp))
-            if tj.get('workload') == wl:
+            tj = json.load(open(tp)).get(wl)
+            if tj:
                 traffic = tj.get('dram_bytes_per_launch')
+                traffic_note = tj.get('note')
         except Exception:
             traffic = None
 
@@ -410,7 +491,10 @@ def run_ours(args):
         'vs_baseline': None, 'dtype': 'c128', 'data': 'synthetic', 'config': workload_config(wl),
         'e2e': e2e, 'gpu_launches': launches,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-                     'traffic': traffic, 'kernel': 'k_hv_gather (matrix-free H.v)', 'peak_kind': peak_kind,
+                     'traffic': traffic,
+                     'kernel': 'matrix-free H.v: k_hv_lin (two-table rank) + k_quantize64 + k_max_exponent',
+                     'hv_variant': {'plain': H.hv_variant(False), 'fused_dot': H.hv_variant(True)},
+                     'traffic_note': traffic_note, 'peak_kind': peak_kind,
                      'bytes_per_row': bytes_row, 'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
                      'launches_timed': n_hv},
         'hv_gbs': achieved,
@@ -424,8 +508,9 @@ def run_ours(args):
 
 
 def start_vector_host(n, seed=0):
-    """The solver's seeded start vector (re, im ~ U[-1,1) from splitmix64),
-    generated on the host for the end-to-end run."""
+    """The solver's seeded start vector, generated on the host for the
+    end-to-end run: re ~ U[-1,1) from splitmix64, imaginary parts zero (the
+    solver starts from a real vector)."""
     import numpy as np
     i = np.arange(n, dtype=np.uint64)
     base = np.uint64((seed * 0xD1B54A32D192ED03) & 0xFFFFFFFFFFFFFFFF)
@@ -437,10 +522,8 @@ def start_vector_host(n, seed=0):
         return z ^ (z >> np.uint64(31))
     with np.errstate(over='ignore'):
         h1 = sm(base + np.uint64(2) * i)
-        h2 = sm(base + np.uint64(2) * i + np.uint64(1))
     u1 = (h1 >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
-    u2 = (h2 >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
-    return (2.0 * u1 - 1.0) + 1j * (2.0 * u2 - 1.0)
+    return (2.0 * u1 - 1.0).astype(np.complex128)
 
 
 def main():
@@ -449,10 +532,12 @@ def main():
     ap.add_argument('--steps', type=int, default=2)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--workload', default='c5', choices=sorted(WORKLOADS))
+    ap.add_argument('--workload', default='c5', choices=sorted(WORKLOADS) + ['c3'])
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
+    ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
+    ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')
     ap.add_argument('--acc', default='exact', choices=['exact', 'fixed64', 'fp64'], help='H.v accumulation')
     args = ap.parse_args()
     if args.warmup < 3:
@@ -461,6 +546,8 @@ def main():
         return run_reference(args)
     if args.hv_only:
         return run_hv_only(args)
+    if args.workload == 'c3':
+        return run_disorder(args)
     return run_ours(args)
 
 

@@ -158,6 +158,11 @@ int ed_ham_set_accumulation(ed_ham* h, int kind);
 /* Diagonal of the assembled matrix (MatGetDiagonal). */
 int ed_ham_diag_host(ed_ham* h, double* out_host);
 int ed_ham_size(const ed_ham* h, int64_t* size);
+/* Name of the matrix-free H.v launch variant the autotuner chose (dot = 0:
+ * plain H.v, 1: H.v fused with x^H y), "" before the first H.v or when the
+ * operator does not use the two-table kernel.  No counterpart in the
+ * reference; for reports. */
+int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len);
 
 /* ---- eigensolver: replaces Solver:: (src/solver.cpp:7-68) ----------------- */
 /* SolverInit(eps, H, nev, ncv, mpd): Hermitian, Krylov-Schur, smallest real.
@@ -183,6 +188,27 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host);
 int ed_eps_get_stats(ed_eps* e, int* its, int64_t* n_hv, int* n_reported, int64_t* ortho_passes);
 int ed_eps_destroy(ed_eps* e);  /* Solver::SolverClean */
 
+/* ---- batched disorder sweep: replaces the one-realisation-at-a-time loop
+ *      of examples/main_disorder.cpp:82-120 -------------------------------- */
+typedef struct ed_batch ed_batch;
+/* B realisations of h (uniform J1/J2, build_off_diag done) with fields
+ * hi_host[b*N + i]; each realisation's diagonal is build_disorder's
+ * (hamiltonian.tmpl_func.hpp:97-125), bit for bit.  Vectors of the batch are
+ * [dim][B] complex128 (realisation index fastest). */
+int ed_batch_create(ed_ham* h, int B, const double* hi_host, ed_batch** out);
+int ed_batch_destroy(ed_batch* bt);
+/* Y[:, b] = H_b X[:, b] for every realisation. */
+int ed_batch_apply(ed_batch* bt, const ed_cplx* x_dev, ed_cplx* y_dev);
+/* The [dim][B] diagonal (MatGetDiagonal per realisation). */
+int ed_batch_diag_host(ed_batch* bt, double* out_host);
+/* Lowest nev eigenpairs of every realisation by lockstep Krylov-Schur (same
+ * method and start vector as ed_eps_solve); evals/errs [B][nev], nconv [B]. */
+int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed, double* evals_host,
+                   double* errs_host, int* nconv_host);
+/* Eigenvector i of realisation b into a contiguous device vector. */
+int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev);
+int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv);
+
 /* ---- measurements: replace SiSj/SzSz/SpSm/SmSp::ExpectVal
  *      (src/spinOperators/correlation.cpp:38-299) --------------------------- */
 /* out[p] = ExpectVal(op, i_p, j_p, psi) for npairs pairs in one fused pass
@@ -200,6 +226,16 @@ int ed_expect_all_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, ed_cp
  * op 1 = Sqp (S+ into sector m+1, spinOPft.tmpl_func.hpp:77-143). */
 int ed_dsf_coefficients(const ed_basis* b0, const ed_basis* b1, int op, const ed_cplx* psi0_dev,
                         const ed_cplx* vecs_dev, int nev, ed_cplx* c_host);
+/* S(q, w) from DSF coefficients, replacing the post-processing notebook
+ * (postprocessing/dynamicStep0_preprocess.ipynb cells 11-15):
+ * S_dev[iq*nw + k] += sum_n F[iq][n] * (1/pi) eps^2 / (eps^2 + (w_k - dE[n])^2),
+ * F[iq][n] = |sum_i exp(i q.r_i) c[i*nev + n]|^2 / nspins, w_k = w_min + k (w_max - w_min)/(nw - 1),
+ * q_host[2*iq..] = (q_x, q_y), r_host[2*i..] = site position.  S_dev (device,
+ * nq x nw doubles) accumulates, so disorder realisations sum in place; the
+ * notebook's average is then 2 pi / rep times the sum (cell 17). */
+int ed_dsf_spectrum(ed_ctx* ctx, int nspins, int nev, const ed_cplx* c_host, const double* dE_host, int nq,
+                    const double* q_host, const double* r_host, int nw, double w_min, double w_max, double eps,
+                    double* S_dev);
 
 /* ---- disorder: replaces Tools::RandomDisorder
  *      (src/tools/random_disorder.cpp:33-59), host only --------------------- */
@@ -211,6 +247,26 @@ int ed_random_fields(int64_t seed, int nspins, double min, double max, double* h
 /* n draws of std::normal_distribution(0, 1) from mt19937_64(seed) (per-bond
  * coupling disorder; no counterpart in the reference). */
 int ed_random_normal(int64_t seed, int64_t n, double* out_host);
+
+/* ---- adjoint gradients: no counterpart in the reference (uniform couplings,
+ *      no derivatives).  H = sum_b [J_b XY_b + D_b ZZ_b] + sum_i h_i Z_i with
+ *      XY_b = (S+_i S-_j + S-_i S+_j)/2, ZZ_b = S^z_i S^z_j, Z_i = S^z_i. ---- */
+enum { ED_TERM_XY = 0, ED_TERM_ZZ = 1, ED_TERM_Z = 2, ED_TERM_SISJ = 3 };
+/* out[t] = <lam| O_t |psi> for terms (kind[t], ij[2t], ij[2t+1]); Z ignores j;
+ * XY and SISJ with i == j give the identity/2 and S.S = 3/4 respectively. */
+int ed_expect_mixed(const ed_basis* b, const int* kinds_host, const int32_t* ij_host, int64_t nterms,
+                    const ed_cplx* lam_dev, const ed_cplx* psi_dev, ed_cplx* out_host);
+/* out = O psi for one term (no aliasing). */
+int ed_apply_term(const ed_basis* b, int kind, int i, int j, const ed_cplx* psi_dev, ed_cplx* out_dev);
+/* Hellmann-Feynman gradient of E = <psi|H|psi>/<psi|psi> for an eigenvector
+ * psi: dJ[q] = <XY_q>, dD[q] = <ZZ_q> for bond q = (pairs[2q], pairs[2q+1]),
+ * dh[i] = <S^z_i>.  Any output may be NULL. */
+int ed_grad_energy(const ed_basis* b, const int32_t* pairs_host, int64_t nbonds, const ed_cplx* psi_dev,
+                   double* dJ_host, double* dD_host, double* dh_host);
+/* MINRES for (H - shift) x = rhs, projected onto the complement of the unit
+ * vector q_dev (NULL: no projection).  Stops at ||r|| <= tol ||rhs||. */
+int ed_minres(ed_ham* h, double shift, const ed_cplx* rhs_dev, const ed_cplx* q_dev, double tol, int max_it,
+              ed_cplx* x_dev, int* its_out, double* relres_out);
 
 #ifdef __cplusplus
 }

@@ -6,9 +6,9 @@ LSQuantumED interfaces (Basis, Hamiltonian, Solver, SiSj, Phys, ...).
 """
 from . import capi  # noqa: F401
 from .capi import EDError, InvalidArgument  # noqa: F401
-from .ed import (AF, DSF_data, EPS, PETSC_DECIDE, PETSC_DEFAULT, Basis, Environment, Hamiltonian,  # noqa: F401
+from .ed import (AF, Adjoint, DSF_data, EPS, DisorderBatch, PETSC_DECIDE, PETSC_DEFAULT, Basis, Environment, Hamiltonian,  # noqa: F401
                  Phys, RandomDisorder, SiSj, SmSp, Solver, SpSm, Striped, SzSz, chain1D, honeycomb2D,
-                 random_fields, random_normal, square2D)
+                 ground_state_energy, random_fields, random_normal, square2D)
 
 
 def build(force=False):

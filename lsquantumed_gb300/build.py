@@ -18,7 +18,9 @@ BUILD = os.path.join(ROOT, '_build', 'edgb300')
 LIBDIR = os.path.join(HERE, '_lib')
 LIB = os.path.join(LIBDIR, 'libedgb300.so')
 
-SOURCES = ['ed_capi.cu', 'ed_basis.cu', 'ed_hamiltonian.cu', 'ed_linalg.cu', 'ed_eps.cu', 'ed_measure.cu']
+SOURCES = ['ed_capi.cu', 'ed_basis.cu', 'ed_hamiltonian.cu', 'ed_linalg.cu', 'ed_eps.cu', 'ed_measure.cu',
+           'ed_batch.cu', 'ed_adjoint.cu', 'ed_hv_lin.cu',
+           'ed_spectrum.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
          '--expt-relaxed-constexpr', '-I' + os.path.join(ROOT, 'include')]

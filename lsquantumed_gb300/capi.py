@@ -15,6 +15,7 @@ ED_CHAIN1D, ED_SQUARE2D, ED_HONEYCOMB2D = 0, 1, 2
 ED_OP_SZSZ, ED_OP_SPSM, ED_OP_SMSP, ED_OP_SISJ = 0, 1, 2, 3
 ED_HAM_MATRIX_FREE, ED_HAM_CSR = 0, 1
 ED_ACC_FP64, ED_ACC_EXACT, ED_ACC_FIXED64 = 0, 1, 2
+ED_TERM_XY, ED_TERM_ZZ, ED_TERM_Z, ED_TERM_SISJ = 0, 1, 2, 3
 
 _ERRNAMES = {1: 'EINVAL', 2: 'ECUDA', 3: 'ENOMEM', 4: 'ESTATE', 5: 'ENOTCONV', 6: 'ENOTSUP'}
 
@@ -73,6 +74,7 @@ SIGNATURES = {
     'ed_ham_set_accumulation': [vp, i32],
     'ed_ham_diag_host': [vp, vp],
     'ed_ham_size': [vp, P(i64)],
+    'ed_ham_hv_variant': [vp, i32, vp, ctypes.c_size_t],
     'ed_eps_create': [vp, i32, i32, i32, P(vp)],
     'ed_eps_set_dimensions': [vp, i32, i32, i32],
     'ed_eps_set_tolerances': [vp, dbl, i32],
@@ -83,12 +85,24 @@ SIGNATURES = {
     'ed_eps_get_eigenvector_host': [vp, i32, vp],
     'ed_eps_get_stats': [vp, P(i32), P(i64), P(i32), P(i64)],
     'ed_eps_destroy': [vp],
+    'ed_batch_create': [vp, i32, vp, P(vp)],
+    'ed_batch_destroy': [vp],
+    'ed_batch_apply': [vp, vp, vp],
+    'ed_batch_diag_host': [vp, vp],
+    'ed_batch_solve': [vp, i32, i32, dbl, i32, u64, vp, vp, vp],
+    'ed_batch_get_eigenvector': [vp, i32, i32, vp],
+    'ed_batch_stats': [vp, P(i32), P(i64)],
     'ed_expect_pairs': [vp, i32, vp, vp, i64, vp],
     'ed_expect_all_pairs': [vp, i32, vp, vp],
     'ed_dsf_coefficients': [vp, vp, i32, vp, vp, i32, vp],
     'ed_random_seeds': [i32, i64, vp],
     'ed_random_fields': [i64, i32, dbl, dbl, vp],
     'ed_random_normal': [i64, i64, vp],
+    'ed_expect_mixed': [vp, vp, vp, i64, vp, vp, vp],
+    'ed_apply_term': [vp, i32, i32, i32, vp, vp],
+    'ed_grad_energy': [vp, vp, i64, vp, vp, vp, vp],
+    'ed_minres': [vp, dbl, vp, vp, dbl, i32, vp, P(i32), P(dbl)],
+    'ed_dsf_spectrum': [vp, i32, i32, vp, vp, i32, vp, vp, i32, dbl, dbl, dbl, vp],
 }
 
 _lib = None

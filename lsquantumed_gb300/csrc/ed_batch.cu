@@ -1,0 +1,756 @@
+// Batched disorder sweep: B realisations of the same Hamiltonian that differ
+// only in the random fields h_i (main_disorder.cpp:82-120 runs them one after
+// another; build_disorder, hamiltonian.tmpl_func.hpp:97-125, rewrites only
+// the diagonal).  All realisations share the off-diagonal pattern, so the
+// batch is held as one [dim][B] array (realisation index fastest): a row's
+// rank lookups serve all B columns and every gather reads B contiguous
+// complex128 values.  B Krylov-Schur solves run in lockstep (same expansion
+// and restart schedule), each with its own projected matrix and convergence;
+// a realisation whose nev pairs have converged has its Ritz vectors saved and
+// is frozen.
+#include "ed_internal.h"
+#include "ed_device.cuh"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+struct ed_batch {
+  ed_ham* h = nullptr;
+  int B = 0;
+  int64_t dim = 0;
+  double* d_diag = nullptr;        // [dim][B], build_disorder semantics per realisation
+  longlong2* d_xq = nullptr;       // fixed-point copy of the SpMM input
+  int* d_gmax = nullptr;
+  // solver results
+  int nev = 0, nrep = 0, its = 0;
+  int64_t nhv = 0;
+  std::vector<double> evals, errs;  // [B][nrep]
+  std::vector<int> nconv;           // [B]
+  double2* d_vecs = nullptr;        // [nrep][dim][B] saved Ritz vectors
+  double* d_red = nullptr;
+  size_t red_cap = 0;
+  double* h_red = nullptr;
+};
+
+// Per-realisation diagonal, exactly as build_disorder computes it:
+// D1*0.25*E_nn + D2*0.25*E_nnn + 0.5*sum_i(+-h_i), separately rounded.
+struct BatchDiagParams {
+  int nb, N, B;
+  uint32_t mask[ED_MAX_BONDS];
+  uint8_t type[ED_MAX_BONDS];
+  double D1, D2;
+};
+
+__global__ void k_batch_diag(const uint32_t* __restrict__ states, int64_t dim, const BatchDiagParams p,
+                             const double* __restrict__ hi /* [B][N] */, double* __restrict__ diag) {
+  const int64_t total = dim * p.B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
+    const int64_t r = k / p.B;
+    const int b = (int)(k - r * p.B);
+    const uint32_t s = states[r];
+    int n1 = 0, a1 = 0, n2 = 0, a2 = 0;
+    for (int q = 0; q < p.nb; ++q) {
+      const uint32_t t = s & p.mask[q];
+      const int anti = (t != 0u && t != p.mask[q]) ? 1 : 0;
+      if (p.type[q] == 0) { ++n1; a1 += anti; } else { ++n2; a2 += anti; }
+    }
+    double dis = 0.0;
+    const double* h = hi + (size_t)b * p.N;
+    for (int i = 0; i < p.N; ++i) dis = ((s >> i) & 1u) ? __dadd_rn(dis, h[i]) : __dsub_rn(dis, h[i]);
+    const double x = __dmul_rn(__dmul_rn(p.D1, 0.25), (double)(n1 - 2 * a1));
+    const double y = __dmul_rn(__dmul_rn(p.D2, 0.25), (double)(n2 - 2 * a2));
+    diag[k] = __dadd_rn(__dadd_rn(x, y), __dmul_rn(0.5, dis));
+  }
+}
+
+// Largest finite exponent over the batch array, for the fixed-point copy.
+__global__ void k_batch_maxexp(const double2* __restrict__ x, int64_t n, int* __restrict__ gmax) {
+  int m = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const double2 v = x[r];
+    const int er = (int)(((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7FF);
+    const int ei = (int)(((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7FF);
+    m = max(m, max(er == 0x7FF ? 0 : er, ei == 0x7FF ? 0 : ei));
+  }
+  m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(gmax, m);
+}
+
+__global__ void k_batch_quantize(const double2* __restrict__ x, int64_t n, const int* __restrict__ gmax_p, int sbits,
+                                 longlong2* __restrict__ xq) {
+  const int emax = *gmax_p;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const double2 v = x[r];
+    const unsigned long long bits[2] = {(unsigned long long)__double_as_longlong(v.x),
+                                        (unsigned long long)__double_as_longlong(v.y)};
+    long long q[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int e = (int)((bits[k] >> 52) & 0x7FF);
+      long long m = 0;
+      if (e == 0x7FF) {
+        m = (long long)0x8000000000000000ull;
+      } else if (e != 0) {
+        const unsigned long long mant = (bits[k] & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+        const int sh = e - emax + sbits - 53;
+        unsigned long long a;
+        if (sh >= 0) a = mant << sh;
+        else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);
+        else a = 0;
+        m = (long long)a;
+        if (bits[k] >> 63) m = -m;
+      }
+      q[k] = m;
+    }
+    xq[r] = make_longlong2(q[0], q[1]);
+  }
+}
+
+// Batched H.v: one CTA per row at a time; every thread of the CTA sees the
+// same basis state, so the antiparallel test and the rank of the flipped
+// state are uniform across the CTA (shared-memory broadcasts), and the
+// gathers of the B columns of the target row are contiguous.  Exact int64
+// sums of the fixed-point input, rounded once to FP64.
+template <int K>
+__global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ states, const double* __restrict__ diag,
+                                                  const double2* __restrict__ x, const longlong2* __restrict__ xq,
+                                                  const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
+                                                  int64_t dim, int B, const RankTables rt, const BondSet bs) {
+  extern __shared__ uint32_t stab[];
+  ed_load_tables(stab, rt);
+  const int e_unit = *gmax_p - 1022 - sbits;
+  const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
+  const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
+  const long long kNaN = (long long)0x8000000000000000ull;
+  const double c0 = bs.chalf[0], c1 = bs.chalf[1];
+  for (int64_t r = blockIdx.x; r < dim; r += gridDim.x) {
+    const uint32_t s = states[r];
+    RowRank<K> R;
+    ed_row_rank<K>(s, stab, rt, R);
+    for (int b0 = 0; b0 < B; b0 += blockDim.x) {
+      const int b = b0 + threadIdx.x;
+      const bool act = b < B;
+      long long a0r = 0, a0i = 0, a1r = 0, a1i = 0;
+      bool bad = false;
+      for (int q = 0; q < bs.nb; ++q) {
+        const uint32_t m = bs.mask[q];
+        const uint32_t t = s & m;
+        if (t == 0u || t == m) continue;  // uniform across the CTA
+        const uint32_t c = ed_rank_flip<K>((uint32_t)r, s, stab, rt, R, bs, q);
+        if (act) {
+          const longlong2 v = __ldg(&xq[(size_t)c * B + b]);
+          bad |= (v.x == kNaN) | (v.y == kNaN);
+          if (bs.type[q] == 0) { a0r += v.x; a0i += v.y; } else { a1r += v.x; a1i += v.y; }
+        }
+      }
+      if (act) {
+        const size_t k = (size_t)r * B + b;
+        const double d = diag[k];
+        const double2 xv = x[k];
+        const double s0r = (double)a0r * s1 * s2, s0i = (double)a0i * s1 * s2;
+        const double t1r = (double)a1r * s1 * s2, t1i = (double)a1i * s1 * s2;
+        double yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
+        double yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
+        if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
+        y[k] = make_double2(yr, yi);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column-wise (per realisation) linear algebra on [dim][B] arrays.
+// ---------------------------------------------------------------------------
+struct BCols {
+  const double2* p[64];
+};
+
+// partial[(item * B + b) * nblk + blk]; items: nv dots (real or complex) + norm
+template <bool REAL>
+__global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const double2* __restrict__ w, int64_t dim,
+                                                    int B, int with_norm, double* __restrict__ partial, int nblk) {
+  // each block: rows [r0, r1), one thread per column b (loop over b chunks)
+  const int64_t rows_per = (dim + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per, r1 = min(dim, r0 + rows_per);
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    double acc_re[16], acc_im[16];
+    double nrm = 0.0;
+    for (int i0 = 0; i0 < max(nv, 1); i0 += 16) {
+      const int ni = max(0, min(16, nv - i0));
+#pragma unroll
+      for (int i = 0; i < 16; ++i) { acc_re[i] = 0.0; acc_im[i] = 0.0; }
+      for (int64_t r = r0; r < r1; ++r) {
+        const double2 wv = w[(size_t)r * B + b];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          if (i < ni) {
+            const double2 v = V.p[i0 + i][(size_t)r * B + b];
+            if (REAL) {
+              acc_re[i] = fma(v.x, wv.x, acc_re[i]);
+            } else {
+              acc_re[i] = fma(v.x, wv.x, fma(v.y, wv.y, acc_re[i]));
+              acc_im[i] = fma(v.x, wv.y, fma(-v.y, wv.x, acc_im[i]));
+            }
+          }
+        }
+        if (with_norm && i0 == 0) nrm = REAL ? fma(wv.x, wv.x, nrm) : fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        if (i < ni) {
+          partial[((size_t)(2 * (i0 + i)) * B + b) * nblk + blockIdx.x] = acc_re[i];
+          partial[((size_t)(2 * (i0 + i) + 1) * B + b) * nblk + blockIdx.x] = REAL ? 0.0 : acc_im[i];
+        }
+      }
+    }
+    if (with_norm) partial[((size_t)(2 * nv) * B + b) * nblk + blockIdx.x] = nrm;
+  }
+}
+
+__global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int64_t items, double* __restrict__ out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += stride) {
+    double a = 0.0;
+    for (int k = 0; k < nblk; ++k) a += partial[(size_t)it * nblk + k];
+    out[it] = a;
+  }
+}
+
+// w[:, b] <- w[:, b] - sum_i V_i[:, b] h[i][b] (h real when REAL); also the
+// local Lanczos terms a[b] v_j + bet[b] v_jm1 (applied first when given).
+template <bool REAL>
+__global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, const double2* __restrict__ h /* [nv][B] */,
+                                                      double2* __restrict__ w, int64_t dim, int B) {
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const int b = (int)(k % B);
+    double2 wv = w[k];
+    for (int i = 0; i < nv; ++i) {
+      const double2 v = V.p[i][k];
+      const double2 c = h[(size_t)i * B + b];
+      if (REAL) {
+        wv.x = fma(-v.x, c.x, wv.x);
+      } else {
+        wv.x = fma(-v.x, c.x, fma(v.y, c.y, wv.x));
+        wv.y = fma(-v.x, c.y, fma(-v.y, c.x, wv.y));
+      }
+    }
+    w[k] = wv;
+  }
+}
+
+// dst[:, b] = src[:, b] * s[b]
+__global__ void k_batch_scale(const double2* __restrict__ src, double2* __restrict__ dst, const double* __restrict__ s,
+                              int64_t dim, int B) {
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const double f = s[k % B];
+    const double2 v = src[k];
+    dst[k] = make_double2(v.x * f, v.y * f);
+  }
+}
+
+// out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation).
+// The batched solve keeps its basis exactly real (real start vectors, real H),
+// so only the real parts are formed.
+__global__ void __launch_bounds__(256) k_batch_restart(const BCols V, int m, const double* __restrict__ Y, int l,
+                                                       BCols out, int c0, int nc, int64_t dim, int B) {
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const int b = (int)(k % B);
+    const double* Yb = Y + (size_t)b * m * l;
+    double ar[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) ar[c] = 0.0;
+    for (int i = 0; i < m; ++i) {
+      const double vx = V.p[i][k].x;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        if (c < nc) {
+          const double y = Yb[(size_t)i * l + c0 + c];
+          ar[c] = fma(vx, y, ar[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < nc) ((double2*)out.p[c0 + c])[k] = make_double2(ar[c], 0.0);
+  }
+}
+
+// start vectors: every realisation starts from the plain solver's seeded
+// real start vector (imaginary parts zero, so the basis stays exactly real
+// and the real-coefficient kernels are exact)
+__global__ void k_batch_start(uint64_t seed, int64_t dim, int B, double2* __restrict__ v) {
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const uint64_t base = seed * 0xD1B54A32D192ED03ull;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const uint64_t i = (uint64_t)(k / B);
+    const uint64_t h1 = ed_splitmix64(base + 2 * i);
+    const double u1 = (double)(h1 >> 11) * (1.0 / 9007199254740992.0);
+    v[k] = make_double2(2.0 * u1 - 1.0, 0.0);
+  }
+}
+
+// copy realisation b's column of a [dim][B] array into a contiguous vector
+__global__ void k_batch_extract(const double2* __restrict__ src, int64_t dim, int B, int b, double2* __restrict__ dst) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) dst[r] = src[(size_t)r * B + b];
+}
+
+// copy column b of src into column b of dst (both [dim][B])
+__global__ void k_batch_copy_col(const double2* __restrict__ src, double2* __restrict__ dst, int64_t dim, int B,
+                                 const int* __restrict__ cols, int ncols) {
+  const int64_t n = dim * ncols;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const int64_t r = k / ncols;
+    const int b = cols[k % ncols];
+    dst[(size_t)r * B + b] = src[(size_t)r * B + b];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int grid_n(ed_ctx* ctx, int64_t n, int per_sm = 8) {
+  int64_t g = (n + 255) / 256;
+  int64_t cap = (int64_t)ctx->num_sms * per_sm;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+static int batch_reduce_buf(ed_batch* bt, size_t doubles) {
+  if (doubles <= bt->red_cap) return ED_OK;
+  if (bt->d_red) cudaFree(bt->d_red);
+  if (bt->h_red) cudaFreeHost(bt->h_red);
+  bt->d_red = nullptr;
+  bt->h_red = nullptr;
+  ED_CUDA(cudaMalloc(&bt->d_red, doubles * sizeof(double)));
+  ED_CUDA(cudaMallocHost(&bt->h_red, doubles * sizeof(double)));
+  bt->red_cap = doubles;
+  return ED_OK;
+}
+
+// dots of nv vectors against w, per realisation; out (host) [item][B]: item
+// 2i = Re, 2i+1 = Im of V_i^H w, item 2nv = ||w||^2.
+static int batch_dots(ed_batch* bt, const std::vector<const double2*>& V, const double2* w, bool real, bool norm,
+                      std::vector<double>& out) {
+  ed_ctx* ctx = bt->h->ctx;
+  const int B = bt->B, nv = (int)V.size();
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 2));
+  const int64_t items = (int64_t)(2 * nv + 1) * B;
+  ED_TRY(batch_reduce_buf(bt, (size_t)items * nblk + (size_t)items));
+  BCols vc;
+  memset(&vc, 0, sizeof(vc));
+  for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
+  const int threads = std::min(256, ((B + 31) / 32) * 32);
+  if (real)
+    k_batch_dots<true><<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
+  else
+    k_batch_dots<false><<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
+  ED_CHECK_LAUNCH(ctx);
+  double* res = bt->d_red + (size_t)items * nblk;
+  k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
+  ED_CHECK_LAUNCH(ctx);
+  ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
+  ED_CUDA(cudaStreamSynchronize(ctx->stream));
+  out.assign(bt->h_red, bt->h_red + items);
+  return ED_OK;
+}
+
+template <int K>
+static int batch_hv_k(ed_batch* bt, const double2* x, double2* y) {
+  ed_ham* h = bt->h;
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  const int64_t n = bt->dim * bt->B;
+  int cnt[2] = {0, 0};
+  for (int q = 0; q < h->bs.nb; ++q) cnt[h->bs.type[q] & 1]++;
+  int head = 0;
+  while ((1 << head) < std::max(cnt[0], cnt[1]) + 1) ++head;
+  const int sbits = 62 - head;
+  ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
+  k_batch_maxexp<<<grid_n(ctx, n), 256, 0, ctx->stream>>>(x, n, bt->d_gmax);
+  ED_CHECK_LAUNCH(ctx);
+  k_batch_quantize<<<grid_n(ctx, n), 256, 0, ctx->stream>>>(x, n, bt->d_gmax, sbits, bt->d_xq);
+  ED_CHECK_LAUNCH(ctx);
+  const size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
+  ED_CUDA(cudaFuncSetAttribute(k_batch_hv<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  int per_sm = 0;
+  const int threads = std::min(256, ((bt->B + 31) / 32) * 32);
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<K>, threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int grid = (int)std::min<int64_t>(bt->dim, (int64_t)ctx->num_sms * per_sm);
+  k_batch_hv<K><<<grid, threads, smem, ctx->stream>>>(b->d_states, bt->d_diag, x, bt->d_xq, bt->d_gmax, sbits, y,
+                                                      bt->dim, bt->B, b->rt, h->bs);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+static int batch_hv(ed_batch* bt, const double2* x, double2* y) {
+  switch (bt->h->basis->rt.K) {
+    case 1: return batch_hv_k<1>(bt, x, y);
+    case 2: return batch_hv_k<2>(bt, x, y);
+    case 3: return batch_hv_k<3>(bt, x, y);
+    default: return batch_hv_k<4>(bt, x, y);
+  }
+}
+
+extern "C" {
+
+int ed_batch_create(ed_ham* h, int B, const double* hi_host, ed_batch** out) {
+  if (!h || !hi_host || !out) return ed_fail(ED_EINVAL, "null argument");
+  if (B < 1) return ed_fail(ED_EINVAL, "batch size must be >= 1");
+  if (h->per_bond) return ed_fail(ED_ENOTSUP, "batched sweeps need uniform J1/J2 couplings");
+  if (!h->offdiag_built) return ed_fail(ED_ESTATE, "build_off_diag before creating a batch");
+  ed_ctx* ctx = h->ctx;
+  const int N = h->basis->nspins;
+  ed_batch* bt = new ed_batch();
+  bt->h = h;
+  bt->B = B;
+  bt->dim = h->basis->dim;
+  const size_t n = (size_t)bt->dim * B;
+  double* dhi = nullptr;
+  if (cudaMalloc(&bt->d_diag, sizeof(double) * n) != cudaSuccess || cudaMalloc(&bt->d_xq, sizeof(longlong2) * n) != cudaSuccess ||
+      cudaMalloc(&bt->d_gmax, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&dhi, sizeof(double) * (size_t)B * N) != cudaSuccess) {
+    cudaGetLastError();
+    if (dhi) cudaFree(dhi);
+    ed_batch_destroy(bt);
+    return ed_fail(ED_ENOMEM, "batch does not fit in device memory");
+  }
+  cudaMemcpyAsync(dhi, hi_host, sizeof(double) * (size_t)B * N, cudaMemcpyHostToDevice, ctx->stream);
+  BatchDiagParams p;
+  memset(&p, 0, sizeof(p));
+  p.nb = (int)h->bi.size();
+  p.N = N;
+  p.B = B;
+  p.D1 = h->D1;
+  p.D2 = h->D2;
+  for (int q = 0; q < p.nb; ++q) {
+    p.mask[q] = (1u << h->bi[q]) | (1u << h->bj[q]);
+    p.type[q] = (uint8_t)h->btype[q];
+  }
+  k_batch_diag<<<grid_n(ctx, (int64_t)n), 256, 0, ctx->stream>>>(h->basis->d_states, bt->dim, p, dhi, bt->d_diag);
+  cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(dhi);
+  if (e != cudaSuccess) {
+    ed_batch_destroy(bt);
+    return ed_cuda_fail(e, "k_batch_diag", __FILE__, __LINE__);
+  }
+  ctx->kernels++;
+  *out = bt;
+  return ED_OK;
+}
+
+int ed_batch_destroy(ed_batch* bt) {
+  if (!bt) return ED_OK;
+  if (bt->d_diag) cudaFree(bt->d_diag);
+  if (bt->d_xq) cudaFree(bt->d_xq);
+  if (bt->d_gmax) cudaFree(bt->d_gmax);
+  if (bt->d_vecs) cudaFree(bt->d_vecs);
+  if (bt->d_red) cudaFree(bt->d_red);
+  if (bt->h_red) cudaFreeHost(bt->h_red);
+  delete bt;
+  return ED_OK;
+}
+
+int ed_batch_apply(ed_batch* bt, const ed_cplx* x_dev, ed_cplx* y_dev) {
+  if (!bt || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
+  if ((const void*)x_dev == (const void*)y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
+  return batch_hv(bt, (const double2*)x_dev, (double2*)y_dev);
+}
+
+int ed_batch_diag_host(ed_batch* bt, double* out_host) {
+  if (!bt || !out_host) return ed_fail(ED_EINVAL, "null argument");
+  ED_CUDA(cudaMemcpyAsync(out_host, bt->d_diag, sizeof(double) * (size_t)bt->dim * bt->B, cudaMemcpyDeviceToHost,
+                          bt->h->ctx->stream));
+  ED_CUDA(cudaStreamSynchronize(bt->h->ctx->stream));
+  return ED_OK;
+}
+
+// Lockstep Krylov-Schur over the batch (same method as ed_eps_solve: local
+// Lanczos projection + one CGS pass with the DGKS refinement test, real
+// coefficients, thick restart), all realisations restarted together keeping
+// l = max(nev + 2, ncv / 2) vectors.
+int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed, double* evals_host,
+                   double* errs_host, int* nconv_host) {
+  if (!bt || !evals_host || !errs_host || !nconv_host) return ed_fail(ED_EINVAL, "null argument");
+  ed_ctx* ctx = bt->h->ctx;
+  const int64_t dim = bt->dim;
+  const int B = bt->B;
+  if (nev < 1) return ed_fail(ED_EINVAL, "nev must be >= 1");
+  int m = ncv > 0 ? ncv : std::max(2 * nev, nev + 15);
+  if (m > dim) m = (int)dim;
+  if (nev > m) nev = m;
+  if (m > 62) return ed_fail(ED_ENOTSUP, "batched ncv above 62 is not supported");
+  if (m < nev + 2 && m < dim) m = std::min<int>((int)dim, nev + 2);
+  if (tol <= 0) tol = 1e-8;
+  if (max_it <= 0) max_it = (int)std::max<int64_t>(100, 2 * dim / std::max(m, 1));
+  const int l_keep = std::min(m - 1, std::max(nev + 2, m / 2));
+  const size_t colsz = (size_t)dim * B;
+  // storage: 2m+1 columns of [dim][B] + w
+  double2* pool = nullptr;
+  double2* w = nullptr;
+  const int pool_cols = 2 * m + 1;
+  if (cudaMalloc(&pool, sizeof(double2) * colsz * pool_cols) != cudaSuccess ||
+      cudaMalloc(&w, sizeof(double2) * colsz) != cudaSuccess) {
+    cudaGetLastError();
+    if (pool) cudaFree(pool);
+    return ed_fail(ED_ENOMEM, "batched Krylov basis does not fit in device memory");
+  }
+  if (bt->d_vecs) cudaFree(bt->d_vecs);
+  bt->d_vecs = nullptr;
+  if (cudaMalloc(&bt->d_vecs, sizeof(double2) * colsz * nev) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(pool);
+    cudaFree(w);
+    return ed_fail(ED_ENOMEM, "batched eigenvectors do not fit in device memory");
+  }
+  std::vector<double2*> col(m + 1), freel;
+  for (int i = 0; i < pool_cols; ++i) {
+    double2* p = pool + (size_t)i * colsz;
+    if (i <= m) col[i] = p; else freel.push_back(p);
+  }
+  double* d_coef = nullptr;  // [64][B] double2 coefficients / scale factors
+  ED_CUDA(cudaMalloc(&d_coef, sizeof(double2) * 64 * (size_t)B));
+  int rc = ED_OK;
+  std::vector<double> out;
+  std::vector<double> alpha((size_t)B * (m + 1)), beta((size_t)B * (m + 1)), arrow((size_t)B * (m + 1));
+  std::vector<int> done(B, 0), nconv(B, 0);
+  bt->evals.assign((size_t)B * nev, 0.0);
+  bt->errs.assign((size_t)B * nev, 0.0);
+  std::vector<double> theta, Y, T;
+  std::vector<double> Yall((size_t)B * m * l_keep);
+  int k = 0, its = 0, remaining = B;
+  bt->nhv = 0;
+  auto fail = [&](int code) { rc = code; };
+  // start vectors, normalised per realisation
+  k_batch_start<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(seed, dim, B, col[0]);
+  ctx->kernels++;
+  {
+    std::vector<const double2*> none;
+    if ((rc = batch_dots(bt, none, col[0], true, true, out)) != ED_OK) goto cleanup;
+    std::vector<double> sc(B);
+    for (int b = 0; b < B; ++b) sc[b] = 1.0 / std::sqrt(out[b]);
+    cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * B, cudaMemcpyHostToDevice, ctx->stream);
+    k_batch_scale<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(col[0], col[0], d_coef, dim, B);
+    ctx->kernels++;
+  }
+  while (remaining > 0 && its < max_it) {
+    ++its;
+    for (int j = k; j < m; ++j) {
+      if ((rc = batch_hv(bt, col[j], w)) != ED_OK) goto cleanup;
+      bt->nhv++;
+      // local projection coefficients: a_b = v_j^H w (real), beta_{j-1}
+      std::vector<const double2*> vj(1, col[j]);
+      if ((rc = batch_dots(bt, vj, w, true, true, out)) != ED_OK) goto cleanup;
+      std::vector<double> yn(B), a(B);
+      for (int b = 0; b < B; ++b) { a[b] = out[(size_t)0 * B + b]; yn[b] = std::sqrt(out[(size_t)2 * B + b]); }
+      // w -= a v_j + beta v_{j-1}
+      {
+        std::vector<double2> hc((size_t)2 * B);
+        const bool three = j > k && j > 0;
+        for (int b = 0; b < B; ++b) {
+          hc[b] = make_double2(a[b], 0.0);
+          hc[(size_t)B + b] = make_double2(three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0, 0.0);
+        }
+        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * 2 * B, cudaMemcpyHostToDevice, ctx->stream);
+        BCols vc;
+        memset(&vc, 0, sizeof(vc));
+        vc.p[0] = col[j];
+        vc.p[1] = three ? col[j - 1] : col[j];
+        k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, three ? 2 : 1,
+                                                                                   (const double2*)d_coef, w, dim, B);
+        ctx->kernels++;
+        for (int b = 0; b < B; ++b) {
+          alpha[(size_t)b * (m + 1) + j] = a[b];
+        }
+      }
+      // full CGS pass (+ DGKS refinement when any realisation needs it)
+      std::vector<const double2*> vs(col.begin(), col.begin() + j + 1);
+      std::vector<double> prevn(B, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        if ((rc = batch_dots(bt, vs, w, true, true, out)) != ED_OK) goto cleanup;
+        std::vector<double2> hc((size_t)(j + 1) * B);
+        for (int i = 0; i <= j; ++i)
+          for (int b = 0; b < B; ++b) hc[(size_t)i * B + b] = make_double2(out[((size_t)2 * i) * B + b], 0.0);
+        for (int b = 0; b < B; ++b) prevn[b] = std::sqrt(out[((size_t)2 * (j + 1)) * B + b]);
+        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
+        BCols vc;
+        memset(&vc, 0, sizeof(vc));
+        for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
+        k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, j + 1, (const double2*)d_coef, w,
+                                                                                   dim, B);
+        ctx->kernels++;
+        for (int b = 0; b < B; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * B + b].x;
+        // norms after the update
+        std::vector<const double2*> none;
+        if ((rc = batch_dots(bt, none, w, true, true, out)) != ED_OK) goto cleanup;
+        bool again = false;
+        for (int b = 0; b < B; ++b) {
+          const double nw = std::sqrt(out[b]);
+          beta[(size_t)b * (m + 1) + j] = nw;
+          if (!done[b] && nw < 0.7071067811865476 * prevn[b]) again = true;
+        }
+        if (!again) break;
+      }
+      // normalise into col[j+1]
+      std::vector<double> sc(B);
+      for (int b = 0; b < B; ++b) {
+        const double nb = beta[(size_t)b * (m + 1) + j];
+        sc[b] = nb > 1e-300 ? 1.0 / nb : 0.0;
+      }
+      cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * B, cudaMemcpyHostToDevice, ctx->stream);
+      k_batch_scale<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, B);
+      ctx->kernels++;
+    }
+    // projected problems, convergence and restart, per realisation
+    std::vector<int> newly;
+    for (int b = 0; b < B; ++b) {
+      T.assign((size_t)m * m, 0.0);
+      const double* al = &alpha[(size_t)b * (m + 1)];
+      const double* be = &beta[(size_t)b * (m + 1)];
+      const double* ar = &arrow[(size_t)b * (m + 1)];
+      for (int i = 0; i < k; ++i) {
+        T[(size_t)i * m + i] = al[i];
+        T[(size_t)i * m + k] = T[(size_t)k * m + i] = ar[i];
+      }
+      for (int jj = k; jj < m; ++jj) {
+        T[(size_t)jj * m + jj] = al[jj];
+        if (jj + 1 < m) T[(size_t)jj * m + jj + 1] = T[(size_t)(jj + 1) * m + jj] = be[jj];
+      }
+      ed_jacobi_eig(m, T, theta, Y);
+      const double bm = be[m - 1];
+      int nc = 0;
+      for (int i = 0; i < m; ++i) {
+        const double res = std::fabs(bm * Y[(size_t)(m - 1) * m + i]);
+        if (res / std::max(std::fabs(theta[i]), 1e-300) < tol) ++nc; else break;
+      }
+      for (int i = 0; i < l_keep; ++i)
+        for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = 0.0;
+      for (int i = 0; i < m; ++i)
+        for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = Y[(size_t)i * m + c];
+      if (!done[b]) {
+        nconv[b] = nc;
+        for (int i = 0; i < nev; ++i) bt->evals[(size_t)b * nev + i] = theta[i];
+        if (nc >= nev || its >= max_it) { newly.push_back(b); }
+      }
+      // kept Ritz values and arrow couplings for the next cycle
+      for (int i = 0; i < l_keep; ++i) {
+        alpha[(size_t)b * (m + 1) + i] = theta[i];
+        arrow[(size_t)b * (m + 1) + i] = bm * Y[(size_t)(m - 1) * m + i];
+      }
+    }
+    // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
+    {
+      double* dY = nullptr;
+      ED_CUDA(cudaMalloc(&dY, sizeof(double) * Yall.size()));
+      cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream);
+      BCols vin, vout;
+      memset(&vin, 0, sizeof(vin));
+      memset(&vout, 0, sizeof(vout));
+      for (int i = 0; i < m; ++i) vin.p[i] = col[i];
+      std::vector<double2*> outc(freel.begin(), freel.begin() + l_keep);
+      for (int c = 0; c < l_keep; ++c) vout.p[c] = outc[c];
+      for (int c0 = 0; c0 < l_keep; c0 += 8) {
+        k_batch_restart<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vin, m, dY, l_keep, vout, c0,
+                                                                              std::min(8, l_keep - c0), dim, B);
+        ctx->kernels++;
+      }
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(dY);
+      // save converged realisations' Ritz vectors
+      if (!newly.empty()) {
+        int* dcols = nullptr;
+        ED_CUDA(cudaMalloc(&dcols, sizeof(int) * newly.size()));
+        cudaMemcpyAsync(dcols, newly.data(), sizeof(int) * newly.size(), cudaMemcpyHostToDevice, ctx->stream);
+        for (int i = 0; i < nev; ++i) {
+          k_batch_copy_col<<<grid_n(ctx, dim * (int64_t)newly.size()), 256, 0, ctx->stream>>>(
+              outc[i], bt->d_vecs + (size_t)i * colsz, dim, B, dcols, (int)newly.size());
+          ctx->kernels++;
+        }
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(dcols);
+        for (int b : newly) { done[b] = 1; --remaining; }
+      }
+      std::vector<double2*> newcol(m + 1, nullptr);
+      for (int c = 0; c < l_keep; ++c) newcol[c] = outc[c];
+      newcol[l_keep] = col[m];
+      std::vector<double2*> nf(freel.begin() + l_keep, freel.end());
+      for (int c = 0; c < m; ++c) nf.push_back(col[c]);
+      for (int c = l_keep + 1; c <= m; ++c) { newcol[c] = nf.back(); nf.pop_back(); }
+      col.swap(newcol);
+      freel.swap(nf);
+    }
+    k = l_keep;
+  }
+  // true relative residuals ||H x - theta x|| / |theta| of the saved vectors
+  for (int i = 0; i < nev; ++i) {
+    double2* xv = bt->d_vecs + (size_t)i * colsz;
+    if ((rc = batch_hv(bt, xv, w)) != ED_OK) goto cleanup;
+    std::vector<double> th(B);
+    for (int b = 0; b < B; ++b) th[b] = bt->evals[(size_t)b * nev + i];
+    // w -= theta x  (per realisation), then ||w||, ||x||
+    std::vector<double2> hc(B);
+    for (int b = 0; b < B; ++b) hc[b] = make_double2(th[b], 0.0);
+    cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * B, cudaMemcpyHostToDevice, ctx->stream);
+    BCols vc;
+    memset(&vc, 0, sizeof(vc));
+    vc.p[0] = xv;
+    k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, 1, (const double2*)d_coef, w, dim, B);
+    ctx->kernels++;
+    std::vector<const double2*> none;
+    if ((rc = batch_dots(bt, none, w, true, true, out)) != ED_OK) goto cleanup;
+    std::vector<double> r2(out.begin(), out.begin() + B);
+    if ((rc = batch_dots(bt, none, xv, true, true, out)) != ED_OK) goto cleanup;
+    for (int b = 0; b < B; ++b)
+      bt->errs[(size_t)b * nev + i] = std::sqrt(r2[b]) / std::max(std::fabs(th[b]) * std::sqrt(out[b]), 1e-300);
+  }
+  bt->nev = nev;
+  bt->nrep = nev;
+  bt->its = its;
+  bt->nconv = nconv;
+  for (int b = 0; b < B; ++b) {
+    nconv_host[b] = nconv[b];
+    for (int i = 0; i < nev; ++i) {
+      evals_host[(size_t)b * nev + i] = bt->evals[(size_t)b * nev + i];
+      errs_host[(size_t)b * nev + i] = bt->errs[(size_t)b * nev + i];
+    }
+  }
+cleanup:
+  (void)fail;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(pool);
+  cudaFree(w);
+  cudaFree(d_coef);
+  return rc;
+}
+
+int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev) {
+  if (!bt || !vec_dev) return ed_fail(ED_EINVAL, "null argument");
+  if (!bt->d_vecs || i < 0 || i >= bt->nrep || b < 0 || b >= bt->B) return ed_fail(ED_EINVAL, "index out of range");
+  ed_ctx* ctx = bt->h->ctx;
+  k_batch_extract<<<grid_n(ctx, bt->dim), 256, 0, ctx->stream>>>(bt->d_vecs + (size_t)i * bt->dim * bt->B, bt->dim,
+                                                                bt->B, b, (double2*)vec_dev);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv) {
+  if (!bt) return ed_fail(ED_EINVAL, "null batch");
+  if (its) *its = bt->its;
+  if (n_hv) *n_hv = bt->nhv;
+  return ED_OK;
+}
+
+}  // extern "C"

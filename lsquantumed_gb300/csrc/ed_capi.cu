@@ -408,6 +408,7 @@ int ed_ham_destroy(ed_ham* h) {
   if (h->d_xq) cudaFree(h->d_xq);
   if (h->d_xe) cudaFree(h->d_xe);
   if (h->d_gmax) cudaFree(h->d_gmax);
+  ed_lin_free(h->lin);
   ham_free_csr(h);
   delete h;
   return ED_OK;
@@ -507,6 +508,16 @@ int ed_ham_set_accumulation(ed_ham* h, int kind) {
 int ed_ham_size(const ed_ham* h, int64_t* size) {
   if (!h || !size) return ed_fail(ED_EINVAL, "null argument");
   *size = h->basis->dim;
+  return ED_OK;
+}
+
+int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len) {
+  if (!h || !buf || len == 0) return ed_fail(ED_EINVAL, "null argument");
+  const char* name = ed_lin_variant_name(h, dot);
+  size_t n = strlen(name);
+  if (n >= len) n = len - 1;
+  memcpy(buf, name, n);
+  buf[n] = 0;
   return ED_OK;
 }
 

@@ -82,6 +82,30 @@ __device__ __forceinline__ uint64_t ed_splitmix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
+// Block reduction of NV doubles (fixed tree order); thread 0 ends with the
+// block sums in v[].  sh holds NV * 32 doubles.
+template <int NV>
+__device__ __forceinline__ void ed_block_reduce(double (&v)[NV], double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double a = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) sh[k * 32 + wid] = a;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double a = lane < nw ? sh[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      v[k] = a;
+    }
+  }
+}
+
 // Load the rank tables into shared memory (block-cooperative).
 __device__ __forceinline__ void ed_load_tables(uint32_t* stab, const RankTables& rt) {
   for (int i = threadIdx.x; i < rt.total; i += blockDim.x) stab[i] = rt.tab[i];

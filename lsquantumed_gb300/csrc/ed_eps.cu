@@ -27,6 +27,7 @@ struct ed_eps {
   int nconv = 0, its = 0, nrep = 0;
   int64_t nhv = 0;
   int64_t ortho_passes = 0;
+  bool real_coeffs = true;            // see orthogonalize_lanczos
   std::vector<double> evals, errs;
   double2* pool = nullptr;            // column storage
   int pool_cols = 0;
@@ -104,27 +105,47 @@ static void eps_free(ed_eps* e) {
 // the local step removes the two large Lanczos components before the
 // refinement test, so the second pass is needed only when real cancellation
 // occurs.  h receives the total j+1 coefficients; norig = ||H v_j||.
+//
+// Real mode: H is real symmetric, so when the start vector is real (all
+// imaginary parts exactly zero) every H.v, projection, normalisation and
+// restart keeps the basis exactly real in complex128 arithmetic, and every
+// coefficient v_i^H w has an exactly zero imaginary part.  The kernels then
+// skip the products whose factors are those zeros (half the FP64 work) and
+// give the same values as the full complex form.  A complex start vector
+// (EPSSetInitialSpace) runs the full complex form.  (Keeping only Re(v_i^H w)
+// for a complex start vector would be wrong in floating point: rounding
+// seeds components along i*y for converged Ritz vectors y, which real
+// coefficients never remove, and Lanczos then grows them into ghost copies.)
 static int orthogonalize_lanczos(ed_eps* e, int j, int k, double beta_prev, std::vector<double2>& h, double* nw,
-                                 double* norig) {
+                                 double* norig, const double2* pre_a, double pre_y2) {
   ed_ctx* ctx = e->h->ctx;
   const int64_t n = e->h->basis->dim;
   std::vector<const double2*> cols(e->col.begin(), e->col.begin() + j + 1);
   h.assign(j + 1, make_double2(0.0, 0.0));
   double2 a;
   double y2 = 0.0, w2 = 0.0, n2 = 0.0;
-  ED_TRY(ed_multidot(ctx, &cols[j], 1, e->w, n, &a, &y2));
+  if (pre_a) {  // alpha = v_j^H w and ||w||^2 came with the H.v
+    a = *pre_a;
+    y2 = pre_y2;
+  } else {
+    ED_TRY(ed_multidot(ctx, &cols[j], 1, e->w, n, &a, &y2, e->real_coeffs));
+  }
   *norig = std::sqrt(y2);
+  const bool real = e->real_coeffs;
+  if (real) a.y = 0.0;
   const bool three_term = j > k && j > 0;
   std::vector<double2> c(j + 1);
   ED_TRY(ed_local_multidot(ctx, cols.data(), j + 1, e->w, n, e->col[j], a, three_term ? e->col[j - 1] : nullptr,
-                           beta_prev, c.data(), &w2));
+                           beta_prev, c.data(), &w2, real));
   double n0 = std::sqrt(w2);
   h[j].x += a.x;
   h[j].y += a.y;
   if (three_term) h[j - 1].x += beta_prev;
   for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1) ED_TRY(ed_multidot(ctx, cols.data(), j + 1, e->w, n, c.data(), nullptr));
-    ED_TRY(ed_update(ctx, cols.data(), j + 1, c.data(), e->w, n, &n2));
+    if (pass == 1) {
+      ED_TRY(ed_multidot(ctx, cols.data(), j + 1, e->w, n, c.data(), nullptr, real));
+    }
+    ED_TRY(ed_update(ctx, cols.data(), j + 1, c.data(), e->w, n, &n2, real));
     for (int i = 0; i <= j; ++i) { h[i].x += c[i].x; h[i].y += c[i].y; }
     *nw = std::sqrt(n2);
     e->ortho_passes++;
@@ -185,8 +206,13 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   }
   std::vector<double> alpha(m + 1, 0.0), beta(m + 1, 0.0), arrow(m + 1, 0.0);
   // start vector: the user's (EPSSetInitialSpace) or the seeded one
-  if (e->v0) ED_TRY(ed_copy(ctx, e->v0, e->col[0], n));
-  else ED_TRY(ed_start_vector(ctx, e->seed, n, e->col[0]));
+  bool real_start = true;
+  if (e->v0) {
+    ED_TRY(ed_copy(ctx, e->v0, e->col[0], n));
+    ED_TRY(ed_is_real(ctx, e->v0, n, &real_start));
+  } else {
+    ED_TRY(ed_start_vector(ctx, e->seed, n, e->col[0], true));
+  }
   {
     std::vector<double2> none;
     double v2 = 0.0;
@@ -196,6 +222,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   uint64_t rseed = e->seed + 0x51ED2701ull;
   e->nhv = 0;
   e->ortho_passes = 0;
+  e->real_coeffs = real_start;
   int k = 0, nconv = 0, its = 0;
   std::vector<double> theta, Y;
   std::vector<double2> h;
@@ -203,16 +230,25 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   while (!done) {
     ++its;
     for (int j = k; j < m; ++j) {
-      ED_TRY(ed_launch_hv(H, e->col[j], e->w));
+      double2 pre_a = make_double2(0.0, 0.0);
+      double pre_y2 = 0.0;
+      bool fused = false;
+      if (ed_lin_supported(H)) {
+        ED_TRY(ed_launch_hv_dot(H, e->col[j], e->w, &pre_a, &pre_y2));
+        fused = true;
+      } else {
+        ED_TRY(ed_launch_hv(H, e->col[j], e->w));
+      }
       e->nhv++;
       double nw, norig;
-      ED_TRY(orthogonalize_lanczos(e, j, k, j > 0 ? beta[j - 1] : 0.0, h, &nw, &norig));
+      ED_TRY(orthogonalize_lanczos(e, j, k, j > 0 ? beta[j - 1] : 0.0, h, &nw, &norig, fused ? &pre_a : nullptr,
+                                   pre_y2));
       alpha[j] = h[j].x;
       if (nw <= 1e-13 * norig) {
         // invariant subspace: continue with a random vector orthogonal to V
         beta[j] = 0.0;
         if (j + 1 < m) {
-          ED_TRY(ed_start_vector(ctx, rseed++, n, e->w));
+          ED_TRY(ed_start_vector(ctx, rseed++, n, e->w, e->real_coeffs));
           std::vector<double2> h2;
           double nw2, no2;
           ED_TRY(orthogonalize(e, j, h2, &nw2, &no2));
@@ -252,7 +288,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
     // new columns 0..l-1 = V Y[:, 0..l-1] into free columns
     std::vector<double2*> outc(freelist.begin(), freelist.begin() + l);
     std::vector<const double2*> inc(e->col.begin(), e->col.begin() + m);
-    ED_TRY(ed_restart_combine(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n));
+    ED_TRY(ed_restart_combine(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n, e->real_coeffs));
     std::vector<double2*> newcol(m + 1, nullptr);
     for (int c = 0; c < l; ++c) newcol[c] = outc[c];
     newcol[l] = e->col[m];

@@ -149,6 +149,7 @@ static void bond_chunks(const RankTables& rt, BondSet& bs, int b, int i, int j) 
 void ed_ham_make_bondset(ed_ham* h) {
   BondSet& bs = h->bs;
   memset(&bs, 0, sizeof(bs));
+  ed_lin_invalidate(h->lin);
   if (!h->offdiag_built) return;
   const RankTables& rt = h->basis->rt;
   if (h->per_bond) {
@@ -614,6 +615,22 @@ static int max_type_count(const BondSet& bs) {
   return c[0] > c[1] ? c[0] : c[1];
 }
 
+int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  ED_TRY(ensure_fixed_buffers(h));
+  int head = 0;
+  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
+  *sbits = 62 - head;
+  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 2 * sizeof(int), ctx->stream));
+  const int g = grid_cap(ctx, b->dim, 256, 8);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
+  ED_CHECK_LAUNCH(ctx);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, *sbits, h->d_xq);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
 template <int K>
 static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
   ed_ctx* ctx = h->ctx;
@@ -647,6 +664,7 @@ static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
 static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
   if (h->mode == ED_HAM_CSR && h->d_rowptr) return ed_launch_csr_spmv(h, x, y);
   const bool pb = h->bs.per_bond != 0;
+  if (ed_lin_supported(h)) return ed_launch_hv_lin(h, x, y, false, nullptr);
   if (!pb && h->hv_kernel == 2) {
     switch (h->basis->rt.K) {
       case 1: return launch_hv_fx64_k<1>(h, x, y);
@@ -683,6 +701,30 @@ int ed_launch_hv(ed_ham* h, const double2* x, double2* y) {
   ctx->prof_events.push_back(e0);
   ctx->prof_events.push_back(e1);
   return rc;
+}
+
+int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, double* y2) {
+  ed_ctx* ctx = h->ctx;
+  if (!ed_lin_supported(h)) return ED_ENOTSUP;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ctx->profiling) {
+    ED_CUDA(cudaEventCreate(&e0));
+    ED_CUDA(cudaEventCreate(&e1));
+    ED_CUDA(cudaEventRecord(e0, ctx->stream));
+  }
+  int nblk = 0;
+  ED_TRY(ed_launch_hv_lin(h, x, y, true, &nblk));
+  if (ctx->profiling) {
+    ED_CUDA(cudaEventRecord(e1, ctx->stream));
+    ctx->prof_events.push_back(e0);
+    ctx->prof_events.push_back(e1);
+  }
+  double out[3];
+  ED_TRY(ed_finish_reduce(ctx, 3, nblk, out));
+  dot->x = out[0];
+  dot->y = out[1];
+  if (y2) *y2 = out[2];
+  return ED_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,347 @@
+// Fixed-point matrix-free H.v with a two-table (low/high half) combinadic rank.
+//
+// The basis state s splits into c0 = the low w0 bits and c1 = the high
+// w1 = N - w0 bits.  With p_i the position of the i-th set bit (ascending),
+// the rank of s in the fixed-Sz basis (ascending integers, the order of
+// Basis::generate_int_basis, basis.cpp:192-215) is sum_i C(p_i, i), which
+// splits into T0[c0] + T1[c1]: the set-bit count below the high half is
+// nup - popc(c1), so the high half's share depends on c1 alone.  T0 (< 2^16
+// per entry for w0 <= 14) sits in shared memory as uint16, T1 in global
+// memory behind the read-only cache (consecutive rows share c1).
+//
+// A bond flip then costs one table entry: bonds inside the low half change
+// only T0 (target rank r - T0[c0] + T0[c0 ^ m0]), bonds inside the high half
+// only T1 (target r - T1[c1] + T1[c1 ^ m1], the same low offset in another
+// block: consecutive rows gather consecutive entries), and bonds across the
+// halves both.  The gathered terms are int64 fixed-point copies of x (see
+// k_quantize64) summed exactly per coupling type, so the result is
+// bit-identical to every other fixed-point kernel of this library.
+#include "ed_internal.h"
+#include "ed_device.cuh"
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#define LIN_MAX_W0 14
+
+// Bond words by class (0 = low half, 1 = high half, 2 = across) and coupling
+// type: lo 32 bits = mask within the low half, hi 32 = mask within the high
+// half (shifted down by w0).
+struct LinSegs {
+  int w0;
+  int seg[7];
+  unsigned long long word[ED_MAX_BONDS];
+};
+
+struct ed_lin {
+  int w0 = 0, w1 = 0;
+  uint16_t* d_t0 = nullptr;
+  uint32_t* d_t1 = nullptr;
+  LinSegs segs{};
+  int built_nb = -1;
+  int variant[2] = {-1, -1};  // launch variants (plain, with dot) chosen by lin_autotune; -1: not yet
+};
+
+static uint64_t binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  uint64_t r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (uint64_t)(n - k + i) / (uint64_t)i;
+  return r;
+}
+
+void ed_lin_free(ed_lin* L) {
+  if (!L) return;
+  if (L->d_t0) cudaFree(L->d_t0);
+  if (L->d_t1) cudaFree(L->d_t1);
+  delete L;
+}
+
+// Tables and bond words for h (once per Hamiltonian; the bond set is fixed
+// after build_off_diag).
+static int lin_prepare(ed_ham* h) {
+  const ed_basis* b = h->basis;
+  const int N = b->nspins, nup = b->nup;
+  if (!h->lin) {
+    ed_lin* L = new ed_lin();
+    L->w0 = std::min(LIN_MAX_W0, (N + 1) / 2);
+    L->w1 = N - L->w0;
+    std::vector<uint16_t> t0((size_t)1 << L->w0);
+    std::vector<uint32_t> t1((size_t)1 << L->w1);
+    for (uint32_t c = 0; c < t0.size(); ++c) {
+      uint64_t v = 0;
+      int k = 0;
+      for (int p = 0; p < L->w0; ++p)
+        if ((c >> p) & 1u) v += binom(p, ++k);
+      t0[c] = (uint16_t)v;
+    }
+    for (uint32_t c = 0; c < t1.size(); ++c) {
+      const int k0 = nup - __builtin_popcount(c);
+      uint64_t v = 0;
+      if (k0 >= 0 && k0 <= L->w0) {
+        int k = k0;
+        for (int q = 0; q < L->w1; ++q)
+          if ((c >> q) & 1u) v += binom(L->w0 + q, ++k);
+      }
+      t1[c] = (uint32_t)v;
+    }
+    if (cudaMalloc(&L->d_t0, t0.size() * sizeof(uint16_t)) != cudaSuccess ||
+        cudaMalloc(&L->d_t1, t1.size() * sizeof(uint32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      ed_lin_free(L);
+      return ed_fail(ED_ENOMEM, "rank tables do not fit in device memory");
+    }
+    cudaError_t e1 = cudaMemcpy(L->d_t0, t0.data(), t0.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+    cudaError_t e2 = cudaMemcpy(L->d_t1, t1.data(), t1.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      ed_lin_free(L);
+      return ed_cuda_fail(e1 != cudaSuccess ? e1 : e2, "rank table upload", __FILE__, __LINE__);
+    }
+    h->lin = L;
+  }
+  ed_lin* L = h->lin;
+  if (L->built_nb != h->bs.nb) {
+    LinSegs& sg = L->segs;
+    memset(&sg, 0, sizeof(sg));
+    sg.w0 = L->w0;
+    const uint32_t low = (1u << L->w0) - 1u;
+    int n = 0;
+    for (int cls = 0; cls < 3; ++cls)
+      for (int t = 0; t < 2; ++t) {
+        sg.seg[cls * 2 + t] = n;
+        for (int q = 0; q < h->bs.nb; ++q) {
+          const uint32_t m = h->bs.mask[q];
+          if (h->bs.type[q] != t || __builtin_popcount(m) != 2) continue;  // i == j never couples
+          const uint32_t m0 = m & low, m1 = m >> L->w0;
+          const int c = m1 == 0 ? 0 : (m0 == 0 ? 1 : 2);
+          if (c != cls) continue;
+          sg.word[n++] = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
+        }
+      }
+    sg.seg[6] = n;
+    L->built_nb = h->bs.nb;
+  }
+  return ED_OK;
+}
+
+// Bonds inside one half: the flipped state's rank is rb + T[c ^ m].
+template <bool CHECK, bool HIGH, int U>
+__device__ __forceinline__ void lin_half(const LinSegs& sg, int b0, int b1, uint32_t c, uint32_t rb,
+                                         const uint16_t* __restrict__ t0s, const uint32_t* __restrict__ t1,
+                                         const longlong2* __restrict__ xq, long long& ar, long long& ai, bool& bad) {
+  const long long kNaN = (long long)0x8000000000000000ull;
+  for (int b = b0; b < b1; b += U) {
+    uint32_t tgt[U];
+    bool on[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool inb = b + u < b1;
+      const unsigned long long w = inb ? sg.word[b + u] : 0ull;
+      const uint32_t m = HIGH ? (uint32_t)(w >> 32) : (uint32_t)w;
+      const uint32_t t = c & m;
+      on[u] = t != 0u && t != m;  // m == 0 (past the end) is never on
+      tgt[u] = rb + (HIGH ? __ldg(&t1[c ^ m]) : (uint32_t)t0s[c ^ m]);
+    }
+    longlong2 q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
+      ar += q[u].x;
+      ai += q[u].y;
+    }
+  }
+}
+
+// Bonds across the halves: one site in each, the rank is T0[c0 ^ m0] + T1[c1 ^ m1].
+template <bool CHECK, int U>
+__device__ __forceinline__ void lin_cross(const LinSegs& sg, int b0, int b1, uint32_t c0, uint32_t c1,
+                                          const uint16_t* __restrict__ t0s, const uint32_t* __restrict__ t1,
+                                          const longlong2* __restrict__ xq, long long& ar, long long& ai, bool& bad) {
+  const long long kNaN = (long long)0x8000000000000000ull;
+  for (int b = b0; b < b1; b += U) {
+    uint32_t tgt[U];
+    bool on[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool inb = b + u < b1;
+      const unsigned long long w = inb ? sg.word[b + u] : 0ull;
+      const uint32_t m0 = (uint32_t)w, m1 = (uint32_t)(w >> 32);
+      on[u] = inb && (((c0 & m0) != 0u) != ((c1 & m1) != 0u));
+      tgt[u] = (uint32_t)t0s[c0 ^ m0] + __ldg(&t1[c1 ^ m1]);
+    }
+    longlong2 q[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
+      ar += q[u].x;
+      ai += q[u].y;
+    }
+  }
+}
+
+template <bool CHECK, bool DOT, int U>
+__device__ __forceinline__ void lin_rows(const uint32_t* __restrict__ states, const double* __restrict__ diag,
+                                         const double2* __restrict__ x, const longlong2* __restrict__ xq,
+                                         double2* __restrict__ y, int64_t dim, const uint16_t* __restrict__ t0s,
+                                         const uint32_t* __restrict__ t1, const LinSegs& sg, double c0c, double c1c,
+                                         double s1, double s2, double (&dacc)[3]) {
+  const uint32_t low = (1u << sg.w0) - 1u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const uint32_t s = states[r];
+    const uint32_t c0 = s & low, c1 = s >> sg.w0;
+    const uint32_t rr = (uint32_t)r;
+    const uint32_t rb0 = rr - (uint32_t)t0s[c0];
+    const uint32_t rb1 = rr - __ldg(&t1[c1]);
+    long long a[4] = {0, 0, 0, 0};  // nn re, nn im, nnn re, nnn im
+    bool bad = false;
+    lin_half<CHECK, false, U>(sg, sg.seg[0], sg.seg[1], c0, rb0, t0s, t1, xq, a[0], a[1], bad);
+    lin_half<CHECK, false, U>(sg, sg.seg[1], sg.seg[2], c0, rb0, t0s, t1, xq, a[2], a[3], bad);
+    lin_half<CHECK, true, U>(sg, sg.seg[2], sg.seg[3], c1, rb1, t0s, t1, xq, a[0], a[1], bad);
+    lin_half<CHECK, true, U>(sg, sg.seg[3], sg.seg[4], c1, rb1, t0s, t1, xq, a[2], a[3], bad);
+    lin_cross<CHECK, U>(sg, sg.seg[4], sg.seg[5], c0, c1, t0s, t1, xq, a[0], a[1], bad);
+    lin_cross<CHECK, U>(sg, sg.seg[5], sg.seg[6], c0, c1, t0s, t1, xq, a[2], a[3], bad);
+    const double d = diag[r];
+    const double2 xv = x[r];
+    const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
+    const double s1r = (double)a[2] * s1 * s2, s1i = (double)a[3] * s1 * s2;
+    double yr = fma(d, xv.x, fma(c0c, s0r, c1c * s1r));
+    double yi = fma(d, xv.y, fma(c0c, s0i, c1c * s1i));
+    if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
+    y[r] = make_double2(yr, yi);
+    if (DOT) {
+      dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
+      dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
+      dacc[2] = fma(yr, yr, fma(yi, yi, dacc[2]));
+    }
+  }
+}
+
+// DOT: partial[item * gridDim.x + block] for item 0/1 = Re/Im x^H y, 2 = ||y||^2.
+// U: bonds per unrolled batch (gathers in flight per thread); MINB: blocks
+// per SM the register allocation must allow.
+template <bool DOT, int U, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_hv_lin(const uint32_t* __restrict__ states, const double* __restrict__ diag,
+                                                const double2* __restrict__ x, const longlong2* __restrict__ xq,
+                                                const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
+                                                int64_t dim, const uint16_t* __restrict__ t0,
+                                                const uint32_t* __restrict__ t1, const LinSegs sg, double c0c,
+                                                double c1c, double* __restrict__ partial) {
+  extern __shared__ uint16_t t0s[];
+  const int n0 = 1 << sg.w0;
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) t0s[i] = t0[i];
+  __syncthreads();
+  const int e_unit = gmax_p[0] - 1022 - sbits;
+  const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
+  const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
+  double dacc[3] = {0.0, 0.0, 0.0};
+  if (gmax_p[1])  // some input entry is not finite: track the rows that gather it
+    lin_rows<true, DOT, U>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+  else
+    lin_rows<false, DOT, U>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+  if (DOT) {
+    __shared__ double sh[3 * 32];
+    ed_block_reduce<3>(dacc, sh);
+    if (threadIdx.x == 0) {
+      partial[blockIdx.x] = dacc[0];
+      partial[gridDim.x + blockIdx.x] = dacc[1];
+      partial[2 * gridDim.x + blockIdx.x] = dacc[2];
+    }
+  }
+}
+
+bool ed_lin_supported(const ed_ham* h) {
+  return !h->bs.per_bond && h->mode != ED_HAM_CSR && h->hv_kernel == 2 && h->basis->nspins >= 2;
+}
+
+// Launch variants (same results: the integer sums are exact, so the unroll
+// depth and register budget change only the speed).
+typedef void (*LinKernel)(const uint32_t*, const double*, const double2*, const longlong2*, const int*, int, double2*,
+                          int64_t, const uint16_t*, const uint32_t*, const LinSegs, double, double, double*);
+struct LinVariant {
+  LinKernel plain, dot;
+  const char* name;
+};
+static const LinVariant kLinVariants[] = {
+    {k_hv_lin<false, 4, 6>, k_hv_lin<true, 4, 5>, "u4-b6"},
+    {k_hv_lin<false, 4, 8>, k_hv_lin<true, 4, 6>, "u4-b8"},
+    {k_hv_lin<false, 8, 4>, k_hv_lin<true, 8, 4>, "u8-b4"},
+    {k_hv_lin<false, 8, 1>, k_hv_lin<true, 8, 1>, "u8-b1"},
+};
+static const int kNumLinVariants = (int)(sizeof(kLinVariants) / sizeof(kLinVariants[0]));
+
+static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, int sbits, int* nblk_out) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  const ed_lin* L = h->lin;
+  const size_t smem = sizeof(uint16_t) * ((size_t)1 << L->w0);
+  LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
+  int per_sm = 0;
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+  if (per_sm < 1) per_sm = 1;
+  int64_t g = (b->dim + 255) / 256;
+  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * per_sm));
+  const int nblk = (int)g;
+  if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
+  k<<<nblk, 256, smem, ctx->stream>>>(b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, L->d_t0, L->d_t1,
+                                      L->segs, h->bs.chalf[0], h->bs.chalf[1], dot ? ctx->d_red : nullptr);
+  ED_CHECK_LAUNCH(ctx);
+  if (nblk_out) *nblk_out = nblk;
+  return ED_OK;
+}
+
+// First H.v (and first fused H.v + dot) of a large operator: time each
+// variant (two launches after one warm-up, CUDA events on the context's
+// stream) and keep the fastest.  The timing synchronises the stream once.
+static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool dot) {
+  ed_lin* L = h->lin;
+  ed_ctx* ctx = h->ctx;
+  int& chosen = L->variant[dot ? 1 : 0];
+  chosen = 0;
+  if (h->basis->dim < (int64_t)1 << 20) return ED_OK;
+  cudaEvent_t e0, e1;
+  ED_CUDA(cudaEventCreate(&e0));
+  ED_CUDA(cudaEventCreate(&e1));
+  float best = 0.0f;
+  int rc = ED_OK;
+  for (int v = 0; v < kNumLinVariants && rc == ED_OK; ++v) {
+    rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
+    if (rc == ED_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
+    for (int it = 0; it < 2 && rc == ED_OK; ++it) rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
+    if (rc == ED_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
+    float ms = 0.0f;
+    if (rc == ED_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      rc = ed_fail(ED_ECUDA, "event timing");
+    if (rc == ED_OK && (v == 0 || ms < best)) {
+      best = ms;
+      chosen = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+// y = H x through the two-table kernel.  With dot set, the kernel also leaves
+// per-block partials of Re/Im x^H y and ||y||^2 in ctx->d_red (3 items of
+// *nblk_out blocks each, for ed_finish_reduce).
+int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out) {
+  ED_TRY(lin_prepare(h));
+  int sbits = 0;
+  ED_TRY(ed_fx64_quantize(h, x, &sbits));
+  const int which = dot ? 1 : 0;
+  if (h->lin->variant[which] < 0) ED_TRY(lin_autotune(h, x, y, sbits, dot));
+  return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out);
+}
+
+const char* ed_lin_variant_name(const ed_ham* h, int dot) {
+  const int which = dot ? 1 : 0;
+  return (h->lin && h->lin->variant[which] >= 0) ? kLinVariants[h->lin->variant[which]].name : "";
+}
+
+void ed_lin_invalidate(ed_lin* L) {
+  if (L) L->built_nb = -1;
+}

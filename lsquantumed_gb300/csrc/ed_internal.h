@@ -107,6 +107,8 @@ struct ed_basis {
   std::vector<uint32_t> h_tab;    // host copy of the rank tables
 };
 
+struct ed_lin;  // two-table fixed-point H.v state (ed_hv_lin.cu)
+
 struct ed_ham {
   ed_ctx* ctx = nullptr;
   const ed_basis* basis = nullptr;
@@ -136,6 +138,7 @@ struct ed_ham {
   int* d_gmax = nullptr;          // largest block exponent
   int hv_kernel = 2;              // 0: FP64, 1: exact 128-bit, 2: 64-bit fixed point
   BondSegments segs{};
+  ed_lin* lin = nullptr;          // tables and bond words of the two-table kernel
 };
 
 // ---------------------------------------------------------------------------
@@ -148,6 +151,17 @@ int ed_launch_unrank(ed_ctx* ctx, const ed_basis* b, const int64_t* ranks_dev, i
 
 int ed_launch_build_diag(ed_ham* h);
 int ed_launch_hv(ed_ham* h, const double2* x, double2* y);
+// y = H x and, in the same pass over the rows, dot = x^H y and *y2 = ||y||^2.
+// Returns ED_ENOTSUP (nothing launched) where the operator has no fused form.
+int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, double* y2);
+// Fixed-point copy of x into h->d_xq (largest exponent and non-finite flag in
+// h->d_gmax[0..1]); *sbits = the fixed-point scale used.
+int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
+bool ed_lin_supported(const ed_ham* h);
+int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out);
+void ed_lin_invalidate(ed_lin* L);
+const char* ed_lin_variant_name(const ed_ham* h, int dot);
+void ed_lin_free(ed_lin* L);
 int ed_launch_csr_build(ed_ham* h);
 int ed_launch_csr_spmv(ed_ham* h, const double2* x, double2* y);
 void ed_ham_make_bondset(ed_ham* h);
@@ -157,16 +171,25 @@ void ed_ham_unique_masks(const ed_ham* h, std::vector<uint32_t>& masks, std::vec
 
 // linear algebra on device vectors (complex128)
 int ed_ensure_reduce(ed_ctx* ctx, size_t doubles);
-int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v);
+// Sum `items` rows of nblk per-block partials in ctx->d_red (fixed order),
+// copy to host_out and synchronise the stream.
+int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out);
+int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v, bool real_only = false);
+// *real = every imaginary part of v is zero.
+int ed_is_real(ed_ctx* ctx, const double2* v, int64_t n, bool* real);
+// real = true: V and w are real (imaginary parts exactly zero); only the
+// real parts are formed (imaginary parts of the results returned as 0).
 int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* w, int64_t n,
-                double2* h_host, double* wnorm2_host);
+                double2* h_host, double* wnorm2_host, bool real = false);
+// real = true: all vectors and coefficients are real (imaginary parts exactly
+// zero: H real symmetric and a real start vector); only real parts are formed.
 int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_host, double2* w, int64_t n,
-              double* wnorm2_host);
+              double* wnorm2_host, bool real = false);
 int ed_local_multidot(ed_ctx* ctx, const double2* const* cols, int nv, double2* w, int64_t n, const double2* vj,
-                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host);
+                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host, bool real = false);
 int ed_scale_copy(ed_ctx* ctx, const double2* src, double2* dst, double s, int64_t n);
 int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const double* Y, int ldY, int l,
-                       double2* const* out, int64_t n);
+                       double2* const* out, int64_t n, bool real = false);
 int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double theta, int64_t n, double* r2_host,
                       double* x2_host);
 int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);

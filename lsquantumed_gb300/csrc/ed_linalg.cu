@@ -14,7 +14,7 @@ struct ColPtrs {
 
 static int red_blocks(ed_ctx* ctx, int64_t n) {
   int64_t b = (n + ED_RED_THREADS - 1) / ED_RED_THREADS;
-  int64_t cap = (int64_t)ctx->num_sms * 2;
+  int64_t cap = (int64_t)ctx->num_sms * 4;
   return (int)std::max<int64_t>(1, std::min(b, cap));
 }
 
@@ -31,31 +31,8 @@ int ed_ensure_reduce(ed_ctx* ctx, size_t doubles) {
   return ED_OK;
 }
 
-// Block reduction of NV doubles; thread 0 of the block ends with the sums in out[].
-template <int NV>
-__device__ __forceinline__ void block_reduce(double (&v)[NV], double* sh /* [NV][32] */) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double a = v[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-    if (lane == 0) sh[k * 32 + wid] = a;
-  }
-  __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double a = lane < nw ? sh[k * 32 + lane] : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-      v[k] = a;
-    }
-  }
-}
-
 // partial[item * nblk + blk]
-template <int G>
+template <int G, bool REAL>
 __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot(const ColPtrs cp, int v0, int ng, const double2* __restrict__ w,
                                                              int64_t n, int with_norm, double* __restrict__ partial,
                                                              int nblk) {
@@ -69,18 +46,26 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot(const ColPtrs cp, i
     for (int g = 0; g < G; ++g) {
       if (g < ng) {
         const double2 v = cp.p[v0 + g][r];
-        acc[2 * g] = fma(v.x, wv.x, fma(v.y, wv.y, acc[2 * g]));
-        acc[2 * g + 1] = fma(v.x, wv.y, fma(-v.y, wv.x, acc[2 * g + 1]));
+        if (REAL) {
+          acc[2 * g] = fma(v.x, wv.x, acc[2 * g]);
+        } else {
+          acc[2 * g] = fma(v.x, wv.x, fma(v.y, wv.y, acc[2 * g]));
+          acc[2 * g + 1] = fma(v.x, wv.y, fma(-v.y, wv.x, acc[2 * g + 1]));
+        }
       }
     }
-    if (with_norm) acc[2 * G] = fma(wv.x, wv.x, fma(wv.y, wv.y, acc[2 * G]));
+    if (with_norm) acc[2 * G] = REAL ? fma(wv.x, wv.x, acc[2 * G]) : fma(wv.x, wv.x, fma(wv.y, wv.y, acc[2 * G]));
   }
   __shared__ double sh[(2 * G + 1) * 32];
-  block_reduce<2 * G + 1>(acc, sh);
+  ed_block_reduce<2 * G + 1>(acc, sh);
   if (threadIdx.x == 0) {
-    for (int g = 0; g < ng; ++g) {
-      partial[(size_t)(2 * (v0 + g)) * nblk + blockIdx.x] = acc[2 * g];
-      partial[(size_t)(2 * (v0 + g) + 1) * nblk + blockIdx.x] = acc[2 * g + 1];
+    // compile-time indices only: a runtime-indexed acc[] would live in local memory
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g < ng) {
+        partial[(size_t)(2 * (v0 + g)) * nblk + blockIdx.x] = acc[2 * g];
+        partial[(size_t)(2 * (v0 + g) + 1) * nblk + blockIdx.x] = REAL ? 0.0 : acc[2 * g + 1];
+      }
     }
     if (with_norm) partial[(size_t)(2 * (v0 + ng)) * nblk + blockIdx.x] = acc[2 * G];
   }
@@ -101,7 +86,7 @@ __global__ void k_reduce_items(const double* __restrict__ partial, int nblk, dou
   if (threadIdx.x == 0) out[item] = sh[0];
 }
 
-static int finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out) {
+int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out) {
   double* out_dev = ctx->d_red + (size_t)items * nblk;
   k_reduce_items<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, out_dev);
   ED_CHECK_LAUNCH(ctx);
@@ -119,7 +104,7 @@ static ColPtrs make_cols(const double2* const* cols, int nv) {
 }
 
 int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* w, int64_t n, double2* h_host,
-                double* wnorm2_host) {
+                double* wnorm2_host, bool real) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
   const int items = 2 * nv + 1;
@@ -129,12 +114,15 @@ int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* 
   for (int v0 = 0; v0 < nv || !with_norm_done; v0 += ED_GROUP) {
     int ng = std::max(0, std::min(ED_GROUP, nv - v0));
     int last = (v0 + ED_GROUP >= nv);
-    k_multidot<ED_GROUP><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, last, ctx->d_red, nblk);
+    if (real)
+      k_multidot<ED_GROUP, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, last, ctx->d_red, nblk);
+    else
+      k_multidot<ED_GROUP, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, last, ctx->d_red, nblk);
     ED_CHECK_LAUNCH(ctx);
     if (last) with_norm_done = 1;
   }
   std::vector<double> out(items);
-  ED_TRY(finish_reduce(ctx, items, nblk, out.data()));
+  ED_TRY(ed_finish_reduce(ctx, items, nblk, out.data()));
   for (int i = 0; i < nv; ++i) { h_host[i].x = out[2 * i]; h_host[i].y = out[2 * i + 1]; }
   if (wnorm2_host) *wnorm2_host = out[2 * nv];
   return ED_OK;
@@ -143,7 +131,7 @@ int ed_multidot(ed_ctx* ctx, const double2* const* cols, int nv, const double2* 
 // Local Lanczos projection fused with the first group of the full CGS dot
 // products: w <- w - a v_j - b v_{j-1} (written back when `local` is set),
 // then partial[i] = V_{v0+i}^H w and ||w||^2.
-template <int G>
+template <int G, bool REAL>
 __global__ void __launch_bounds__(ED_RED_THREADS) k_local_multidot(const ColPtrs cp, int v0, int ng,
                                                                    double2* __restrict__ w, int64_t n, int local,
                                                                    const double2* __restrict__ vj, double2 a,
@@ -157,12 +145,16 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_local_multidot(const ColPtrs
     double2 wv = w[r];
     if (local) {
       const double2 p = vj[r];
-      wv.x = fma(-a.x, p.x, fma(a.y, p.y, wv.x));
-      wv.y = fma(-a.x, p.y, fma(-a.y, p.x, wv.y));
+      if (REAL) {
+        wv.x = fma(-a.x, p.x, wv.x);
+      } else {
+        wv.x = fma(-a.x, p.x, fma(a.y, p.y, wv.x));
+        wv.y = fma(-a.x, p.y, fma(-a.y, p.x, wv.y));
+      }
       if (vjm1) {
         const double2 q = vjm1[r];
         wv.x = fma(-b, q.x, wv.x);
-        wv.y = fma(-b, q.y, wv.y);
+        if (!REAL) wv.y = fma(-b, q.y, wv.y);
       }
       w[r] = wv;
     }
@@ -170,25 +162,33 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_local_multidot(const ColPtrs
     for (int g = 0; g < G; ++g) {
       if (g < ng) {
         const double2 v = cp.p[v0 + g][r];
-        acc[2 * g] = fma(v.x, wv.x, fma(v.y, wv.y, acc[2 * g]));
-        acc[2 * g + 1] = fma(v.x, wv.y, fma(-v.y, wv.x, acc[2 * g + 1]));
+        if (REAL) {
+          acc[2 * g] = fma(v.x, wv.x, acc[2 * g]);
+        } else {
+          acc[2 * g] = fma(v.x, wv.x, fma(v.y, wv.y, acc[2 * g]));
+          acc[2 * g + 1] = fma(v.x, wv.y, fma(-v.y, wv.x, acc[2 * g + 1]));
+        }
       }
     }
-    if (with_norm) acc[2 * G] = fma(wv.x, wv.x, fma(wv.y, wv.y, acc[2 * G]));
+    if (with_norm) acc[2 * G] = REAL ? fma(wv.x, wv.x, acc[2 * G]) : fma(wv.x, wv.x, fma(wv.y, wv.y, acc[2 * G]));
   }
   __shared__ double sh[(2 * G + 1) * 32];
-  block_reduce<2 * G + 1>(acc, sh);
+  ed_block_reduce<2 * G + 1>(acc, sh);
   if (threadIdx.x == 0) {
-    for (int g = 0; g < ng; ++g) {
-      partial[(size_t)(2 * (v0 + g)) * nblk + blockIdx.x] = acc[2 * g];
-      partial[(size_t)(2 * (v0 + g) + 1) * nblk + blockIdx.x] = acc[2 * g + 1];
+    // compile-time indices only: a runtime-indexed acc[] would live in local memory
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g < ng) {
+        partial[(size_t)(2 * (v0 + g)) * nblk + blockIdx.x] = acc[2 * g];
+        partial[(size_t)(2 * (v0 + g) + 1) * nblk + blockIdx.x] = REAL ? 0.0 : acc[2 * g + 1];
+      }
     }
     if (with_norm) partial[(size_t)(2 * (v0 + ng)) * nblk + blockIdx.x] = acc[2 * G];
   }
 }
 
 int ed_local_multidot(ed_ctx* ctx, const double2* const* cols, int nv, double2* w, int64_t n, const double2* vj,
-                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host) {
+                      double2 a, const double2* vjm1, double b, double2* h_host, double* wnorm2_host, bool real) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
   const int items = 2 * nv + 1;
@@ -201,18 +201,25 @@ int ed_local_multidot(ed_ctx* ctx, const double2* const* cols, int nv, double2* 
     const int v0 = gidx * ED_GROUP;
     const int ng = std::min(ED_GROUP, nv - v0);
     const int last = gidx == ngroups - 1;
-    k_local_multidot<ED_GROUP><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, gidx == 0, vj, a, vjm1, b,
-                                                                         last, ctx->d_red, nblk);
+    if (real)
+      k_local_multidot<ED_GROUP, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, gidx == 0, vj, a,
+                                                                               vjm1, b, last, ctx->d_red, nblk);
+    else
+      k_local_multidot<ED_GROUP, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, gidx == 0, vj, a,
+                                                                                vjm1, b, last, ctx->d_red, nblk);
     ED_CHECK_LAUNCH(ctx);
   }
   std::vector<double> out(items);
-  ED_TRY(finish_reduce(ctx, items, nblk, out.data()));
+  ED_TRY(ed_finish_reduce(ctx, items, nblk, out.data()));
   for (int i = 0; i < nv; ++i) { h_host[i].x = out[2 * i]; h_host[i].y = out[2 * i + 1]; }
   if (wnorm2_host) *wnorm2_host = out[2 * nv];
   return ED_OK;
 }
 
-// w <- w - sum_i V_i h_i ; partial ||w||^2
+// w <- w - sum_i V_i h_i ; partial ||w||^2.  REAL: the vectors and the
+// coefficients are real (all imaginary parts exactly zero), so only the
+// real parts are formed: one FMA per element per vector, same values.
+template <bool REAL>
 __global__ void __launch_bounds__(ED_RED_THREADS) k_update(const ColPtrs cp, int nv, const double2* __restrict__ h,
                                                            double2* __restrict__ w, int64_t n, double* __restrict__ partial,
                                                            int nblk) {
@@ -221,24 +228,42 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update(const ColPtrs cp, int
   __syncthreads();
   double acc[1] = {0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    double2 wv = w[r];
+  // two rows per thread and iteration: twice the loads in flight
+  for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < n; r0 += 2 * stride) {
+    const int64_t r1 = r0 + stride;
+    const bool has1 = r1 < n;
+    double2 w0 = w[r0];
+    double2 w1 = has1 ? w[r1] : make_double2(0.0, 0.0);
+#pragma unroll 4
     for (int i = 0; i < nv; ++i) {
-      const double2 v = cp.p[i][r];
+      const double2* col = cp.p[i];
+      const double2 v0 = col[r0];
+      const double2 v1 = has1 ? col[r1] : make_double2(0.0, 0.0);
       const double2 c = sh_h[i];
-      wv.x = fma(-v.x, c.x, fma(v.y, c.y, wv.x));
-      wv.y = fma(-v.x, c.y, fma(-v.y, c.x, wv.y));
+      if (REAL) {
+        w0.x = fma(-v0.x, c.x, w0.x);
+        w1.x = fma(-v1.x, c.x, w1.x);
+      } else {
+        w0.x = fma(-v0.x, c.x, fma(v0.y, c.y, w0.x));
+        w0.y = fma(-v0.x, c.y, fma(-v0.y, c.x, w0.y));
+        w1.x = fma(-v1.x, c.x, fma(v1.y, c.y, w1.x));
+        w1.y = fma(-v1.x, c.y, fma(-v1.y, c.x, w1.y));
+      }
     }
-    w[r] = wv;
-    acc[0] = fma(wv.x, wv.x, fma(wv.y, wv.y, acc[0]));
+    w[r0] = w0;
+    acc[0] = REAL ? fma(w0.x, w0.x, acc[0]) : fma(w0.x, w0.x, fma(w0.y, w0.y, acc[0]));
+    if (has1) {
+      w[r1] = w1;
+      acc[0] = REAL ? fma(w1.x, w1.x, acc[0]) : fma(w1.x, w1.x, fma(w1.y, w1.y, acc[0]));
+    }
   }
   __shared__ double sh[32];
-  block_reduce<1>(acc, sh);
+  ed_block_reduce<1>(acc, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
 }
 
 int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_host, double2* w, int64_t n,
-              double* wnorm2_host) {
+              double* wnorm2_host, bool real) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
   ED_TRY(ed_ensure_reduce(ctx, (size_t)nblk + 4 + 2 * 128));
@@ -246,10 +271,11 @@ int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_
   double2* h_dev = (double2*)(ctx->d_red + ((nblk + 2 + 1) & ~1));
   ED_CUDA(cudaMemcpyAsync(h_dev, h_host, sizeof(double2) * nv, cudaMemcpyHostToDevice, ctx->stream));
   ColPtrs cp = make_cols(cols, nv);
-  k_update<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, nblk);
+  if (real) k_update<true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, nblk);
+  else k_update<false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
   double out;
-  ED_TRY(finish_reduce(ctx, 1, nblk, &out));
+  ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));
   if (wnorm2_host) *wnorm2_host = out;
   return ED_OK;
 }
@@ -275,6 +301,8 @@ int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n) {
 }
 
 // out_c = sum_i V_i * Y[i*ldY + c], c in [c0, c0+nc), nc <= 8; Y real.
+// REAL: the columns are real (imaginary parts exactly zero): real parts only.
+template <bool REAL>
 __global__ void __launch_bounds__(256) k_restart(const ColPtrs cp, int m, const double* __restrict__ Y, int ldY, int c0,
                                                  int nc, const ColPtrs outp, int64_t n) {
   extern __shared__ double shY[];  // m x 8
@@ -294,7 +322,7 @@ __global__ void __launch_bounds__(256) k_restart(const ColPtrs cp, int m, const 
       for (int c = 0; c < 8; ++c) {
         const double y = shY[i * 8 + c];
         ar[c] = fma(v.x, y, ar[c]);
-        ai[c] = fma(v.y, y, ai[c]);
+        if (!REAL) ai[c] = fma(v.y, y, ai[c]);
       }
     }
 #pragma unroll
@@ -304,7 +332,7 @@ __global__ void __launch_bounds__(256) k_restart(const ColPtrs cp, int m, const 
 }
 
 int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const double* Y, int ldY, int l,
-                       double2* const* out, int64_t n) {
+                       double2* const* out, int64_t n, bool real) {
   if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   ColPtrs cp = make_cols(cols, m);
   ColPtrs op = make_cols((const double2* const*)out, l);
@@ -316,7 +344,8 @@ int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const dou
   size_t smem = sizeof(double) * (size_t)m * 8;
   for (int c0 = 0; c0 < l; c0 += 8) {
     int nc = std::min(8, l - c0);
-    k_restart<<<g, 256, smem, ctx->stream>>>(cp, m, dY, ldY, c0, nc, op, n);
+    if (real) k_restart<true><<<g, 256, smem, ctx->stream>>>(cp, m, dY, ldY, c0, nc, op, n);
+    else k_restart<false><<<g, 256, smem, ctx->stream>>>(cp, m, dY, ldY, c0, nc, op, n);
     ED_CHECK_LAUNCH(ctx);
   }
   return ED_OK;
@@ -335,7 +364,7 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_residual(const double2* __re
     acc[1] = fma(b.x, b.x, fma(b.y, b.y, acc[1]));
   }
   __shared__ double sh[64];
-  block_reduce<2>(acc, sh);
+  ed_block_reduce<2>(acc, sh);
   if (threadIdx.x == 0) { partial[blockIdx.x] = acc[0]; partial[nblk + blockIdx.x] = acc[1]; }
 }
 
@@ -346,15 +375,15 @@ int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double t
   k_residual<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(hx, x, theta, n, ctx->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
   double out[2];
-  ED_TRY(finish_reduce(ctx, 2, nblk, out));
+  ED_TRY(ed_finish_reduce(ctx, 2, nblk, out));
   *r2_host = out[0];
   *x2_host = out[1];
   return ED_OK;
 }
 
 // Deterministic start vector: re, im ~ U[-1, 1) from a counter hash (same
-// bits as the CPU oracle's start vector).
-__global__ void k_start_vector(uint64_t seed, int64_t n, double2* __restrict__ v) {
+// bits as the CPU oracle's start vector); real_only zeroes the imaginary parts.
+__global__ void k_start_vector(uint64_t seed, int64_t n, int real_only, double2* __restrict__ v) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const uint64_t base = seed * 0xD1B54A32D192ED03ull;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -362,13 +391,41 @@ __global__ void k_start_vector(uint64_t seed, int64_t n, double2* __restrict__ v
     const uint64_t h2 = ed_splitmix64(base + 2 * (uint64_t)i + 1);
     const double u1 = (double)(h1 >> 11) * (1.0 / 9007199254740992.0);
     const double u2 = (double)(h2 >> 11) * (1.0 / 9007199254740992.0);
-    v[i] = make_double2(2.0 * u1 - 1.0, 2.0 * u2 - 1.0);
+    v[i] = make_double2(2.0 * u1 - 1.0, real_only ? 0.0 : 2.0 * u2 - 1.0);
   }
 }
 
-int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v) {
+int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v, bool real_only) {
   int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
-  k_start_vector<<<g, 256, 0, ctx->stream>>>(seed, n, v);
+  k_start_vector<<<g, 256, 0, ctx->stream>>>(seed, n, real_only ? 1 : 0, v);
   ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+// *any = 1 if some entry of v has a nonzero imaginary part.
+__global__ void k_imag_any(const double2* __restrict__ v, int64_t n, int* __restrict__ any) {
+  int a = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) a |= v[i].y != 0.0;
+  a = (int)__reduce_or_sync(0xffffffffu, (unsigned)a);
+  if ((threadIdx.x & 31) == 0 && a) atomicOr(any, 1);
+}
+
+int ed_is_real(ed_ctx* ctx, const double2* v, int64_t n, bool* real) {
+  int* d_any = nullptr;
+  ED_CUDA(cudaMalloc(&d_any, sizeof(int)));
+  int h_any = 0;
+  cudaError_t e = cudaMemsetAsync(d_any, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess) {
+    int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
+    k_imag_any<<<g, 256, 0, ctx->stream>>>(v, n, d_any);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) ctx->kernels++;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h_any, d_any, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_any);
+  if (e != cudaSuccess) return ed_cuda_fail(e, "imaginary-part test", __FILE__, __LINE__);
+  *real = h_any == 0;
   return ED_OK;
 }

@@ -331,6 +331,12 @@ class Hamiltonian:
         k = {'exact': capi.ED_ACC_EXACT, 'fixed64': capi.ED_ACC_FIXED64, 'fp64': capi.ED_ACC_FP64}[kind]
         call('ed_ham_set_accumulation', self._h, k)
 
+    def hv_variant(self, dot=False):
+        """Launch variant of the matrix-free H.v chosen by the autotuner."""
+        buf = ctypes.create_string_buffer(64)
+        call('ed_ham_hv_variant', self._h, 1 if dot else 0, buf, 64)
+        return buf.value.decode()
+
     def export_csr(self):
         """(rowptr, cols, vals) of the assembled matrix, rows sorted by column."""
         nnz = self.build_csr()
@@ -466,6 +472,62 @@ class Solver:
     def SolverClean(eps: EPS):
         eps.destroy()
         return 0
+
+
+# ---------------------------------------------------------------------------
+# Batched disorder sweep (the loop of examples/main_disorder.cpp:82-120)
+# ---------------------------------------------------------------------------
+class DisorderBatch:
+    """B field realisations of one Hamiltonian, solved together.
+
+    ``fields`` is (B, N): realisation b uses h_i = fields[b, i] exactly as
+    build_disorder would.  Vectors are (dim, B) CUDA tensors."""
+
+    def __init__(self, hamilt: Hamiltonian, fields):
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        if f.ndim != 2 or f.shape[1] != hamilt.basis.nspins:
+            raise InvalidArgument(capi.ED_EINVAL, 'fields must be (B, nspins)')
+        self.hamilt = hamilt
+        self.B = f.shape[0]
+        h = ctypes.c_void_p()
+        call('ed_batch_create', hamilt.handle, self.B, _p(f), ctypes.byref(h))
+        self._h = h
+
+    def apply(self, X, out=None):
+        torch = _torch()
+        X = X.to(device='cuda', dtype=torch.complex128).contiguous()
+        Y = torch.empty_like(X) if out is None else out
+        call('ed_batch_apply', self._h, _p(X), _p(Y))
+        return Y
+
+    def diagonal(self):
+        out = np.zeros((self.hamilt.size, self.B), dtype=np.float64)
+        call('ed_batch_diag_host', self._h, _p(out))
+        return out
+
+    def solve(self, nev=1, ncv=0, tol=1e-8, max_it=0, seed=0):
+        ev = np.zeros((self.B, nev))
+        er = np.zeros((self.B, nev))
+        nc = np.zeros(self.B, dtype=np.int32)
+        call('ed_batch_solve', self._h, int(nev), int(ncv), float(tol), int(max_it), int(seed), _p(ev), _p(er),
+             _p(nc))
+        its, nhv = ctypes.c_int(), ctypes.c_int64()
+        call('ed_batch_stats', self._h, ctypes.byref(its), ctypes.byref(nhv))
+        return {'evals': ev, 'errs': er, 'nconv': nc, 'its': its.value, 'nhv': nhv.value}
+
+    def eigenvector(self, b, i):
+        torch = _torch()
+        v = torch.empty(self.hamilt.size, dtype=torch.complex128, device='cuda')
+        call('ed_batch_get_eigenvector', self._h, int(b), int(i), _p(v))
+        return v
+
+    def __del__(self):
+        if getattr(self, '_h', None):
+            try:
+                capi.lib().ed_batch_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
 
 
 # ---------------------------------------------------------------------------
@@ -693,9 +755,199 @@ class Phys:
         return np.array([(i // ly, i % ly) for i in range(n)], dtype=np.float64)
 
     @staticmethod
+    def q_grid(lattice: Lattice):
+        """The notebooks' wave vectors (dynamicStep0_preprocess.ipynb cell 4):
+        q_i = ((i // ly) 2 pi / lx, (i % ly) 2 pi / ly), i < N."""
+        n, lx, ly = lattice.nspins, lattice.nspins_x, lattice.nspins_y
+        return np.array([((i // ly) * 2 * np.pi / lx, (i % ly) * 2 * np.pi / ly) for i in range(n)])
+
+    @staticmethod
+    def dsf_spectrum(env, c, dE, positions, qs, nw=5001, w_min=0.0, w_max=5.0, eps=None, out=None):
+        """S(q, w) on the device from DSF coefficients c (N x nev) and level
+        energies dE (nev): Lorentzian-broadened weights as in the
+        post-processing notebook (dynamicStep0_preprocess.ipynb cells 11-15),
+        eps = 1/N by default.  Accumulates into `out` (a (nq, nw) float64
+        CUDA tensor) when given, so realisations sum; returns the tensor."""
+        torch = _torch()
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        nspins, nev = c.shape
+        dE = np.ascontiguousarray(dE, dtype=np.float64)
+        qs = np.ascontiguousarray(np.asarray(qs, dtype=np.float64).reshape(-1, 2))
+        r = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).reshape(-1, 2))
+        if dE.size != nev or r.shape[0] != nspins:
+            raise InvalidArgument(capi.ED_EINVAL, 'c must be (N, nev), dE (nev), positions (N, 2)')
+        if eps is None:
+            eps = 1.0 / nspins
+        S = out if out is not None else torch.zeros((len(qs), nw), dtype=torch.float64, device='cuda')
+        call('ed_dsf_spectrum', env.handle, nspins, nev, _p(c), _p(dE), len(qs), _p(qs), _p(r), int(nw),
+             float(w_min), float(w_max), float(eps), _p(S))
+        return S
+
+    @staticmethod
+    def dsf_sum_rule(S, w_min=0.0, w_max=5.0):
+        """sum_{q,w} S dw / (2 pi) of a disorder-averaged S(q, w) (already
+        scaled by 2 pi / rep), the notebooks' check against 1/4
+        (dynamicStep2_plotSw.ipynb cell 12)."""
+        S = S.cpu().numpy() if hasattr(S, 'cpu') else np.asarray(S)
+        dw = (w_max - w_min) / (S.shape[-1] - 1)
+        return float(S.sum() * dw / (2 * np.pi))
+
+    @staticmethod
     def dsf_weights(c, positions, q):
         """|sum_i e^{i q.r_i} c_{i,n}|^2 / N for each level n (the weight the
         post-processing notebooks form from the dsf files)."""
         ph = np.exp(1j * (positions @ np.asarray(q, dtype=np.float64)))
         amp = ph @ c
         return np.abs(amp) ** 2 / c.shape[0]
+
+
+# ---------------------------------------------------------------------------
+# Adjoint gradients (no counterpart in the reference: its couplings are
+# uniform and it forms no derivatives).
+#   H = sum_b [J_b XY_b + D_b ZZ_b] + sum_i h_i S^z_i,
+#   XY_b = (S+_i S-_j + S-_i S+_j)/2,  ZZ_b = S^z_i S^z_j.
+# ---------------------------------------------------------------------------
+class Adjoint:
+    """Hellmann-Feynman energy gradients and adjoint (MINRES) gradients of
+    ground-state expectation values with respect to J_b, D_b and h_i."""
+    XY, ZZ, Z, SISJ = capi.ED_TERM_XY, capi.ED_TERM_ZZ, capi.ED_TERM_Z, capi.ED_TERM_SISJ
+
+    @staticmethod
+    def _terms(terms):
+        t = np.asarray(terms, dtype=np.int64).reshape(-1, 3)
+        kinds = np.ascontiguousarray(t[:, 0], dtype=np.int32)
+        ij = np.ascontiguousarray(t[:, 1:], dtype=np.int32)
+        return kinds, ij
+
+    @staticmethod
+    def expect_mixed(basis: Basis, terms, lam, psi):
+        """<lam| O_t |psi> for terms (kind, i, j); complex array."""
+        lam = as_device_vector(lam, basis.size)
+        psi = as_device_vector(psi, basis.size)
+        kinds, ij = Adjoint._terms(terms)
+        out = np.zeros(len(kinds), dtype=np.complex128)
+        call('ed_expect_mixed', basis.handle, _p(kinds), _p(ij), len(kinds), _p(lam), _p(psi), _p(out))
+        return out
+
+    @staticmethod
+    def apply_term(basis: Basis, kind, i, j, psi, out=None):
+        torch = _torch()
+        psi = as_device_vector(psi, basis.size)
+        y = torch.empty_like(psi) if out is None else out
+        call('ed_apply_term', basis.handle, int(kind), int(i), int(j), _p(psi), _p(y))
+        return y
+
+    @staticmethod
+    def energy_gradient(basis: Basis, pairs, psi):
+        """(dE/dJ_b, dE/dD_b, dE/dh_i) at the eigenvector psi (Hellmann-Feynman;
+        valid for a non-degenerate level)."""
+        psi = as_device_vector(psi, basis.size)
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        dJ = np.zeros(len(pr))
+        dD = np.zeros(len(pr))
+        dh = np.zeros(basis.nspins)
+        call('ed_grad_energy', basis.handle, _p(pr), len(pr), _p(psi), _p(dJ), _p(dD), _p(dh))
+        return dJ, dD, dh
+
+    @staticmethod
+    def eigenvalue_sum_gradient(eps, pairs, k):
+        """Gradient of E_0 + ... + E_{k-1} (the lowest k levels of a solved
+        EPS) with respect to (J_b, D_b, h_i): the sum of the levels'
+        Hellmann-Feynman expectations.  Valid when level k-1 is not part of a
+        multiplet that continues past k (a trace over whole multiplets does
+        not depend on the basis chosen inside them)."""
+        basis = eps.hamilt.basis
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        gJ = np.zeros(len(pr))
+        gD = np.zeros(len(pr))
+        gh = np.zeros(basis.nspins)
+        for n in range(int(k)):
+            _, v, _ = Solver.solution(eps, n)
+            dJ, dD, dh = Adjoint.energy_gradient(basis, pr, v)
+            gJ += dJ
+            gD += dD
+            gh += dh
+        return gJ, gD, gh
+
+    @staticmethod
+    def minres(hamilt: Hamiltonian, shift, rhs, q=None, tol=1e-12, max_it=0):
+        """x with (H - shift) x = rhs on the complement of the unit vector q."""
+        torch = _torch()
+        b = as_device_vector(rhs, hamilt.size)
+        qd = None if q is None else as_device_vector(q, hamilt.size)
+        x = torch.empty_like(b)
+        its, rel = ctypes.c_int(), ctypes.c_double()
+        call('ed_minres', hamilt.handle, float(shift), _p(b), None if qd is None else _p(qd), float(tol),
+             int(max_it), _p(x), ctypes.byref(its), ctypes.byref(rel))
+        return x, its.value, rel.value
+
+    @staticmethod
+    def apply_observable(basis: Basis, observable, psi):
+        """O psi for O = sum_t c_t O_t, observable = [(c, kind, i, j), ...]."""
+        torch = _torch()
+        psi = as_device_vector(psi, basis.size)
+        acc = torch.zeros_like(psi)
+        tmp = torch.empty_like(psi)
+        for c, kind, i, j in observable:
+            Adjoint.apply_term(basis, kind, i, j, psi, out=tmp)
+            acc.add_(tmp, alpha=complex(c))
+        return acc
+
+    @staticmethod
+    def expectation_gradient(hamilt: Hamiltonian, pairs, e0, psi0, observable, tol=1e-12, max_it=0):
+        """Gradient of <psi0|O|psi0> (psi0 the normalised, non-degenerate ground
+        state, e0 its energy) with respect to (J_b, D_b, h_i):
+        (H - e0) lam = P (O psi0), P = 1 - psi0 psi0^H, then
+        d<O>/dtheta = -2 Re <lam| dH/dtheta |psi0>.
+        Returns (value, dJ, dD, dh, info)."""
+        basis = hamilt.basis
+        psi = as_device_vector(psi0, basis.size)
+        nrm = float(np.sqrt(np.real(psi.conj().dot(psi).item())))
+        psi = psi / nrm
+        opsi = Adjoint.apply_observable(basis, observable, psi)
+        val = psi.conj().dot(opsi).item()
+        rhs = opsi - val * psi
+        lam, its, rel = Adjoint.minres(hamilt, e0, rhs, q=psi, tol=tol, max_it=max_it)
+        pr = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        terms = [(Adjoint.XY, i, j) for i, j in pr] + [(Adjoint.ZZ, i, j) for i, j in pr] + \
+                [(Adjoint.Z, i, i) for i in range(basis.nspins)]
+        g = -2.0 * np.real(Adjoint.expect_mixed(basis, terms, lam, psi))
+        nb = len(pr)
+        return float(np.real(val)), g[:nb], g[nb:2 * nb], g[2 * nb:], {'its': its, 'relres': rel}
+
+
+def ground_state_energy(env, basis: Basis, pairs, J, D, h=None, nev=1, ncv=0, tol=1e-12):
+    """E0(J, D, h) as a differentiable torch function of per-bond couplings
+    (J, D: float64 tensors of len(pairs)) and site fields h (len nspins, or
+    None).  The backward pass is the Hellmann-Feynman gradient."""
+    torch = _torch()
+    pairs_np = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+
+    class _E0(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, J, D, hf):
+            ham = Hamiltonian.from_bonds(env, basis, pairs_np, J.detach().cpu().numpy(), D.detach().cpu().numpy())
+            ham.build_diag(env)
+            ham.build_off_diag(env)
+            if hf is not None and hf.numel():
+                ham.build_disorder(env, hf.detach().cpu().numpy())
+            eps = Solver.SolverInit(ham, nev, ncv if ncv else PETSC_DEFAULT)
+            Solver.EPSSetTolerances(eps, tol)
+            Solver.solve(env, eps)
+            e0, _ = Solver.eigenvalue(eps, 0)
+            v = torch.empty(basis.size, dtype=torch.complex128, device='cuda')
+            Solver.solution(eps, 0, v)
+            dJ, dD, dh = Adjoint.energy_gradient(basis, pairs_np, v)
+            Solver.SolverClean(eps)
+            ctx.has_h = hf is not None and hf.numel() > 0
+            ctx.save_for_backward(torch.from_numpy(dJ).to(J.device), torch.from_numpy(dD).to(D.device),
+                                  torch.from_numpy(dh).to(hf.device))
+            return torch.tensor(float(e0), dtype=torch.float64, device=J.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            dJ, dD, dh = ctx.saved_tensors
+            return g * dJ, g * dD, (g * dh if ctx.has_h else None)
+
+    hf = h if h is not None else torch.zeros(0, dtype=torch.float64)
+    return _E0.apply(J, D, hf)

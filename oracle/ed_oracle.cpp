@@ -432,12 +432,12 @@ static inline uint64_t splitmix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 static inline double u01(uint64_t h) { return (double)(h >> 11) * (1.0 / 9007199254740992.0); }
-static void start_vector(uint64_t seed, int64_t n, cplx* v) {
+static void start_vector(uint64_t seed, int64_t n, cplx* v, bool real_only = false) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     uint64_t h1 = splitmix64(seed * 0xD1B54A32D192ED03ull + 2 * (uint64_t)i);
     uint64_t h2 = splitmix64(seed * 0xD1B54A32D192ED03ull + 2 * (uint64_t)i + 1);
-    v[i] = cplx(2.0 * u01(h1) - 1.0, 2.0 * u01(h2) - 1.0);
+    v[i] = cplx(2.0 * u01(h1) - 1.0, real_only ? 0.0 : 2.0 * u01(h2) - 1.0);
   }
 }
 
@@ -521,7 +521,10 @@ static void ks_solve(int64_t n, Apply apply, int nev, int ncv, int mpd, double t
   const int m = ncv;
   std::vector<cplx> V((size_t)(m + 1) * n), w(n);
   std::vector<double> alpha(m + 1, 0.0), beta(m + 1, 0.0), arrow(m + 1, 0.0);
-  start_vector(seed, n, V.data());
+  // The Krylov-Schur start vectors are real (imaginary parts zero): H is real
+  // symmetric, so every Krylov vector then stays exactly real in complex128
+  // arithmetic and its eigenvectors come out real.
+  start_vector(seed, n, V.data(), true);
   auto dotc = [&](const cplx* a, const cplx* b) {  // a^H b
     double re = 0, im = 0;
 #pragma omp parallel for reduction(+ : re, im) schedule(static)
@@ -576,7 +579,7 @@ static void ks_solve(int64_t n, Apply apply, int nev, int ncv, int mpd, double t
         // invariant subspace: continue with a random vector orthogonal to V
         beta[j] = 0.0;
         if (j + 1 < m) {
-          start_vector(rseed++, n, w.data());
+          start_vector(rseed++, n, w.data(), true);
           double nw2, no2;
           std::vector<cplx> h2;
           orthog(j, h2, nw2, no2);

@@ -366,3 +366,43 @@ def squared_sublatt_mag_str(model, sublat, psi):
                     e += model.expect(SISJ, i, j, psi)
     n = model.nspins
     return e * 4.0 / n / (n + 4.0)
+
+
+# ---------------------------------------------------------------------------
+# S(q, w) post-processing, restated from postprocessing/dynamicStep0_preprocess.ipynb
+# (cells 4, 11-13, 15, 17) and the sum-rule check of dynamicStep2_plotSw.ipynb
+# (cell 12), in the notebooks' loop order.
+# ---------------------------------------------------------------------------
+def q_grid(nspins, lx, ly):
+    """cell 4: q_i = ((i // Ly) 2 pi / Lx, (i % Ly) 2 pi / Ly), i < nQ = N."""
+    pi = np.arccos(-1)
+    return np.array([((i // ly) * 2 * pi / lx, (i % ly) * 2 * pi / ly) for i in range(nspins)])
+
+
+def dsf_spectrum(c, dE, positions, qs, nw=5001, w_min=0.0, w_max=5.0, eps=None):
+    """One realisation's S[q][w]: cells 11 (Lorentzian), 12-13 (phase sum,
+    |.|^2 / N) and 15 (sum over levels).  c is (N, nev) complex."""
+    nspins, nev = c.shape
+    eps = 1.0 / nspins if eps is None else eps
+    e2 = eps * eps
+    inv_pi = 1.0 / np.arccos(-1)
+    w = np.linspace(w_min, w_max, nw)
+    factor = np.zeros((len(qs), nev))
+    for iq, q in enumerate(qs):
+        amp = np.zeros(nev, dtype=np.complex128)
+        for i in range(nspins):
+            amp = amp + np.exp(1j * (q[0] * positions[i][0] + q[1] * positions[i][1])) * c[i, :]
+        factor[iq] = np.abs(amp) ** 2 / nspins
+    delta = inv_pi * e2 / (e2 + (w[:, None] - np.asarray(dE)[None, :]) ** 2)  # (nw, nev)
+    return factor @ delta.T  # (nq, nw)
+
+
+def dsf_average(spectra):
+    """cell 17: 2 pi / rep * sum over realisations."""
+    return 2 * np.arccos(-1) * np.sum(spectra, axis=0) / len(spectra)
+
+
+def dsf_sum_rule(S, w_min=0.0, w_max=5.0):
+    """dynamicStep2_plotSw.ipynb cell 12: sum(S) * dw / (2 pi), expected 0.25."""
+    dw = (w_max - w_min) / (S.shape[-1] - 1)
+    return float(np.sum(S) * dw / (2 * np.arccos(-1)))

@@ -467,3 +467,53 @@ def test_golden_dsf_pipeline(ed, envs, golden, tmp_path):
         # sum rule per site: sum_n |c_{i,n}|^2 <= <0|S_i^dag S_i|0> (1/4 for S^z, <= 1 for S^+)
         bound = 0.25 if rec['op'] == 'Sqz' else 1.0
         assert np.all(np.sum(np.abs(c) ** 2, axis=1) <= bound + 1e-12)
+
+
+def test_dsf_spectrum_vs_oracle(ed, envs):
+    """Device S(q, w) (Lorentzian broadening of the DSF weights, the
+    post-processing notebook's cells 11-15) against the oracle's restatement,
+    1e-12 of the largest value; realisations accumulate in place."""
+    N, lx, ly, nev = 16, 4, 4, 40
+    env = envs(N)
+    rng = np.random.default_rng(11)
+    qs = oracle.q_grid(N, lx, ly)
+    pos = np.array([(i // ly, i % ly) for i in range(N)], dtype=np.float64)
+    spectra = []
+    S = None
+    for rep in range(3):
+        c = rng.standard_normal((N, nev)) + 1j * rng.standard_normal((N, nev))
+        dE = np.sort(rng.uniform(0.0, 4.5, nev))
+        ref = oracle.dsf_spectrum(c, dE, pos, qs, nw=5001)
+        one = ed.Phys.dsf_spectrum(env, c, dE, pos, qs, nw=5001).cpu().numpy()
+        assert np.abs(one - ref).max() <= 1e-12 * np.abs(ref).max()
+        S = ed.Phys.dsf_spectrum(env, c, dE, pos, qs, nw=5001, out=S)
+        spectra.append(ref)
+    avg = 2 * np.pi * S.cpu().numpy() / 3
+    ref_avg = oracle.dsf_average(spectra)
+    assert np.abs(avg - ref_avg).max() <= 1e-12 * np.abs(ref_avg).max()
+    with pytest.raises(ValueError):
+        ed.Phys.dsf_spectrum(env, c, dE[:-1], pos, qs)
+
+
+def test_dsf_spectrum_sum_rule(ed, envs):
+    """Full Sz=0 spectrum of a chain (N=8), coefficients from the device:
+    the notebooks' sum rule sum_{q,w} S dw / 2 pi = 1/4 (window widened to
+    [-40, 40] so the Lorentzian tails stay inside; missing weight < 2e-3),
+    and the notebook window [0, 5] equal to the oracle's value."""
+    import torch
+    N = 8
+    env = envs(N)
+    M = Model(0, N, 1, N, 0, 1.0, 1.0, 0.0, 0.0)
+    M.build(3)
+    w, V = np.linalg.eigh(M.dense())
+    b = ed.Basis(env, 0)
+    vecs = np.ascontiguousarray(V.T.astype(np.complex128))
+    c = ed.Phys.dsf_coefficients(env, b, b, 0, vecs[0], torch.from_numpy(vecs))
+    dE = w - w[0]
+    qs = oracle.q_grid(N, 1, N)
+    pos = np.array([(0, i) for i in range(N)], dtype=np.float64)
+    wide = ed.Phys.dsf_spectrum(env, c, dE, pos, qs, nw=160001, w_min=-40.0, w_max=40.0)
+    assert abs(ed.Phys.dsf_sum_rule(2 * np.pi * wide, -40.0, 40.0) - 0.25) < 2e-3
+    S = 2 * np.pi * ed.Phys.dsf_spectrum(env, c, dE, pos, qs, nw=5001).cpu().numpy()
+    ref = oracle.dsf_average([oracle.dsf_spectrum(c, dE, pos, qs)])
+    assert abs(ed.Phys.dsf_sum_rule(S) - oracle.dsf_sum_rule(ref)) <= 1e-12

@@ -234,3 +234,23 @@ def test_dsf_reference_files(golden, orc):
             k = np.dot(ref, ours) / np.dot(ours, ours)
             assert abs(k) <= 1 + 1e-8
             assert np.allclose(ref, k * ours, atol=1e-9), (rec['name'], n, ref, ours)
+
+
+def test_oracle_dsf_sum_rule():
+    """The S(q, w) restatement satisfies the notebooks' sum rule
+    (dynamicStep2_plotSw.ipynb cell 12: sum_{q,w} S dw / 2 pi = 1/4) on the
+    oracle's full Sz=0 spectrum of an N=8 chain.  The window is widened to
+    w in [-40, 40] so that the Lorentzian tails (half width 1/N) stay inside:
+    the missing weight is then below 2e-3."""
+    import oracle
+    from oracle import Model
+    N = 8
+    M = Model(0, N, 1, N, 0, 1.0, 1.0, 0.0, 0.0)
+    M.build(3)
+    w, V = np.linalg.eigh(M.dense())
+    psi0 = V[:, 0].astype(np.complex128)
+    c = np.array([[np.vdot(V[:, n], M.sqz(i, psi0)) for n in range(len(w))] for i in range(N)])
+    assert np.allclose(np.sum(np.abs(c) ** 2, axis=1), 0.25)  # <0|(S^z_i)^2|0> = 1/4
+    S = oracle.dsf_average([oracle.dsf_spectrum(c, w - w[0], [(0, i) for i in range(N)],
+                                                oracle.q_grid(N, 1, N), nw=160001, w_min=-40.0, w_max=40.0)])
+    assert abs(oracle.dsf_sum_rule(S, -40.0, 40.0) - 0.25) < 2e-3
