@@ -410,6 +410,18 @@ def run_ours(args):
         e, err = ed.Solver.eigenvalue(eps, i)
         evals.append(e)
         errs.append(err)
+    # all N^2 <S_i.S_j> in the ground state (measured after the timed solves)
+    sisj = None
+    if not args.no_sisj:
+        _, psi0, _ = ed.Solver.solution(eps, 0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        C = ed.SiSj(env, b).AllPairs(psi0)
+        torch.cuda.synchronize()
+        sisj = {'seconds': time.perf_counter() - t0, 'pairs': N * N,
+                'sum_check': float(np.real(C.sum())),  # <S_tot^2> = S(S+1) = 0 for a singlet ground state
+                'S0_S1': float(np.real(C[0, 1]))}
+        del psi0
     ed.Solver.SolverClean(eps)
     ms_step = ms / args.steps
     if ws > 1:
@@ -497,7 +509,7 @@ def run_ours(args):
                      'traffic_note': traffic_note, 'peak_kind': peak_kind,
                      'bytes_per_row': bytes_row, 'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
                      'launches_timed': n_hv},
-        'hv_gbs': achieved,
+        'hv_gbs': achieved, 'sisj_all_pairs': sisj,
         'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'ortho_passes': st['ortho_passes'],
                    'eigenvalues': evals,
                    'rel_residuals': errs},
@@ -535,6 +547,7 @@ def main():
     ap.add_argument('--workload', default='c5', choices=sorted(WORKLOADS) + ['c3'])
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
     ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')

@@ -110,49 +110,79 @@ __global__ void k_batch_quantize(const double2* __restrict__ x, int64_t n, const
   }
 }
 
-// Batched H.v: one CTA per row at a time; every thread of the CTA sees the
-// same basis state, so the antiparallel test and the rank of the flipped
-// state are uniform across the CTA (shared-memory broadcasts), and the
-// gathers of the B columns of the target row are contiguous.  Exact int64
-// sums of the fixed-point input, rounded once to FP64.
-template <int K>
+// Batched H.v over a [dim][B] block.  A CTA takes a tile of BH_ROWS rows:
+// first its threads resolve every (row, bond) pair of the tile at once (the
+// antiparallel test and the two-table rank of the flipped state, written to
+// shared memory; non-flippable pairs get an invalid target), then each
+// thread owns realisation columns b and gathers the B contiguous values of
+// every target row, four bonds at a time so several loads are in flight.
+// Exact int64 sums of the fixed-point input per coupling type, rounded once.
+#define BH_ROWS 8
+#define BH_NONE 0xFFFFFFFFu
+
+struct BatchBonds {
+  int nb;
+  uint32_t mask[ED_MAX_BONDS];
+  uint8_t type[ED_MAX_BONDS];
+};
+
 __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ states, const double* __restrict__ diag,
                                                   const double2* __restrict__ x, const longlong2* __restrict__ xq,
                                                   const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
-                                                  int64_t dim, int B, const RankTables rt, const BondSet bs) {
-  extern __shared__ uint32_t stab[];
-  ed_load_tables(stab, rt);
+                                                  int64_t dim, int B, const uint16_t* __restrict__ t0,
+                                                  const uint32_t* __restrict__ t1, int w0, const BatchBonds bb,
+                                                  double c0, double c1) {
+  extern __shared__ uint32_t sm[];
+  uint16_t* t0s = (uint16_t*)sm;                       // 2^w0 entries
+  uint32_t* tgt = sm + ((1 << w0) + 1) / 2;            // [BH_ROWS][nb]
+  for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
   const int e_unit = *gmax_p - 1022 - sbits;
   const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
   const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
   const long long kNaN = (long long)0x8000000000000000ull;
-  const double c0 = bs.chalf[0], c1 = bs.chalf[1];
-  for (int64_t r = blockIdx.x; r < dim; r += gridDim.x) {
-    const uint32_t s = states[r];
-    RowRank<K> R;
-    ed_row_rank<K>(s, stab, rt, R);
-    for (int b0 = 0; b0 < B; b0 += blockDim.x) {
-      const int b = b0 + threadIdx.x;
-      const bool act = b < B;
-      long long a0r = 0, a0i = 0, a1r = 0, a1i = 0;
-      bool bad = false;
-      for (int q = 0; q < bs.nb; ++q) {
-        const uint32_t m = bs.mask[q];
-        const uint32_t t = s & m;
-        if (t == 0u || t == m) continue;  // uniform across the CTA
-        const uint32_t c = ed_rank_flip<K>((uint32_t)r, s, stab, rt, R, bs, q);
-        if (act) {
-          const longlong2 v = __ldg(&xq[(size_t)c * B + b]);
-          bad |= (v.x == kNaN) | (v.y == kNaN);
-          if (bs.type[q] == 0) { a0r += v.x; a0i += v.y; } else { a1r += v.x; a1i += v.y; }
+  const uint32_t low = (1u << w0) - 1u;
+  const int nb = bb.nb;
+  for (int64_t r0 = (int64_t)blockIdx.x * BH_ROWS; r0 < dim; r0 += (int64_t)gridDim.x * BH_ROWS) {
+    __syncthreads();  // t0s ready / previous tile's targets consumed
+    for (int it = threadIdx.x; it < BH_ROWS * nb; it += blockDim.x) {
+      const int rr = it / nb, q = it % nb;
+      uint32_t c = BH_NONE;
+      if (r0 + rr < dim) {
+        const uint32_t s = states[r0 + rr], m = bb.mask[q], t = s & m;
+        if (t != 0u && t != m) {
+          const uint32_t f = s ^ m;
+          c = (uint32_t)t0s[f & low] + __ldg(&t1[f >> w0]);
         }
       }
-      if (act) {
-        const size_t k = (size_t)r * B + b;
+      tgt[it] = c;
+    }
+    __syncthreads();
+    const int nrows = (int)(dim - r0 < BH_ROWS ? dim - r0 : BH_ROWS);
+    for (int rr = 0; rr < nrows; ++rr) {
+      const uint32_t* tr = tgt + rr * nb;
+      for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        long long a[4] = {0, 0, 0, 0};
+        bool bad = false;
+        for (int q0 = 0; q0 < nb; q0 += 4) {
+          longlong2 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
+            v[u] = c != BH_NONE ? __ldg(&xq[(size_t)c * B + b]) : make_longlong2(0, 0);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            bad |= (v[u].x == kNaN) | (v[u].y == kNaN);
+            const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
+            a[t1b ? 2 : 0] += v[u].x;
+            a[t1b ? 3 : 1] += v[u].y;
+          }
+        }
+        const size_t k = (size_t)(r0 + rr) * B + b;
         const double d = diag[k];
         const double2 xv = x[k];
-        const double s0r = (double)a0r * s1 * s2, s0i = (double)a0i * s1 * s2;
-        const double t1r = (double)a1r * s1 * s2, t1i = (double)a1i * s1 * s2;
+        const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
+        const double t1r = (double)a[2] * s1 * s2, t1i = (double)a[3] * s1 * s2;
         double yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
         double yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
         if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
@@ -366,8 +396,7 @@ static int batch_dots(ed_batch* bt, const std::vector<const double2*>& V, const 
   return ED_OK;
 }
 
-template <int K>
-static int batch_hv_k(ed_batch* bt, const double2* x, double2* y) {
+static int batch_hv(ed_batch* bt, const double2* x, double2* y) {
   ed_ham* h = bt->h;
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
@@ -382,26 +411,31 @@ static int batch_hv_k(ed_batch* bt, const double2* x, double2* y) {
   ED_CHECK_LAUNCH(ctx);
   k_batch_quantize<<<grid_n(ctx, n), 256, 0, ctx->stream>>>(x, n, bt->d_gmax, sbits, bt->d_xq);
   ED_CHECK_LAUNCH(ctx);
-  const size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
-  ED_CUDA(cudaFuncSetAttribute(k_batch_hv<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  BatchBonds bb;
+  memset(&bb, 0, sizeof(bb));
+  for (int q = 0; q < h->bs.nb; ++q) {
+    if (__builtin_popcount(h->bs.mask[q]) != 2) continue;  // i == j never couples
+    bb.mask[bb.nb] = h->bs.mask[q];
+    bb.type[bb.nb] = (uint8_t)(h->bs.type[q] & 1);
+    ++bb.nb;
+  }
+  const size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)BH_ROWS * std::max(bb.nb, 1));
+  static bool attr = false;
+  if (!attr) {
+    ED_CUDA(cudaFuncSetAttribute(k_batch_hv, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    attr = true;
+  }
   int per_sm = 0;
   const int threads = std::min(256, ((bt->B + 31) / 32) * 32);
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<K>, threads, smem));
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv, threads, smem));
   if (per_sm < 1) per_sm = 1;
-  const int grid = (int)std::min<int64_t>(bt->dim, (int64_t)ctx->num_sms * per_sm);
-  k_batch_hv<K><<<grid, threads, smem, ctx->stream>>>(b->d_states, bt->d_diag, x, bt->d_xq, bt->d_gmax, sbits, y,
-                                                      bt->dim, bt->B, b->rt, h->bs);
+  const int64_t tiles = (bt->dim + BH_ROWS - 1) / BH_ROWS;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
+  k_batch_hv<<<grid, threads, smem, ctx->stream>>>(b->d_states, bt->d_diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim,
+                                                   bt->B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
+                                                   h->bs.chalf[1]);
   ED_CHECK_LAUNCH(ctx);
   return ED_OK;
-}
-
-static int batch_hv(ed_batch* bt, const double2* x, double2* y) {
-  switch (bt->h->basis->rt.K) {
-    case 1: return batch_hv_k<1>(bt, x, y);
-    case 2: return batch_hv_k<2>(bt, x, y);
-    case 3: return batch_hv_k<3>(bt, x, y);
-    default: return batch_hv_k<4>(bt, x, y);
-  }
 }
 
 extern "C" {

@@ -183,6 +183,8 @@ int ed_basis_create(ed_ctx* ctx, int nspins, int total_mag, ed_basis** out) {
   if (e3 != cudaSuccess) { ed_basis_destroy(b); return ed_cuda_fail(e3, "upload rank tables", __FILE__, __LINE__); }
   rc = ed_launch_basis_states(ctx, nspins, b->nup, b->dim, b->d_states);
   if (rc != ED_OK) { ed_basis_destroy(b); return rc; }
+  rc = ed_basis_lin_tables(b);
+  if (rc != ED_OK) { ed_basis_destroy(b); return rc; }
   *out = b;
   return ED_OK;
 }
@@ -194,6 +196,8 @@ int ed_basis_destroy(ed_basis* b) {
   if (!b) return ED_OK;
   if (b->d_states) cudaFree(b->d_states);
   if (b->d_tab) cudaFree(b->d_tab);
+  if (b->d_lin_t0) cudaFree(b->d_lin_t0);
+  if (b->d_lin_t1) cudaFree(b->d_lin_t1);
   delete b;
   return ED_OK;
 }
@@ -537,10 +541,21 @@ int ed_expect_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, const int
 int ed_expect_all_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, ed_cplx* out_host) {
   if (!b || !psi_dev || !out_host) return ed_fail(ED_EINVAL, "null argument");
   const int N = b->nspins;
+  // <O_ji> = conj(<O_ij>) for all four operators (S^z_i S^z_j and S_i.S_j are
+  // Hermitian and symmetric in i, j; S+_j S-_i = (S+_i S-_j)^dagger, likewise
+  // S-S+): evaluate i <= j and mirror.
   std::vector<int32_t> pairs;
   for (int i = 0; i < N; ++i)
-    for (int j = 0; j < N; ++j) { pairs.push_back(i); pairs.push_back(j); }
-  return ed_expect_pairs(b, op, psi_dev, pairs.data(), (int64_t)N * N, out_host);
+    for (int j = i; j < N; ++j) { pairs.push_back(i); pairs.push_back(j); }
+  const int64_t np = (int64_t)pairs.size() / 2;
+  std::vector<ed_cplx> half(np);
+  ED_TRY(ed_expect_pairs(b, op, psi_dev, pairs.data(), np, half.data()));
+  for (int64_t k = 0; k < np; ++k) {
+    const int i = pairs[2 * k], j = pairs[2 * k + 1];
+    out_host[(size_t)i * N + j] = half[k];
+    out_host[(size_t)j * N + i] = ed_cplx{half[k].re, -half[k].im};
+  }
+  return ED_OK;
 }
 
 int ed_dsf_coefficients(const ed_basis* b0, const ed_basis* b1, int op, const ed_cplx* psi0_dev, const ed_cplx* vecs_dev,

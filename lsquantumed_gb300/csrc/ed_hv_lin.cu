@@ -34,9 +34,6 @@ struct LinSegs {
 };
 
 struct ed_lin {
-  int w0 = 0, w1 = 0;
-  uint16_t* d_t0 = nullptr;
-  uint32_t* d_t1 = nullptr;
   LinSegs segs{};
   int built_nb = -1;
   int variant[2] = {-1, -1};  // launch variants (plain, with dot) chosen by lin_autotune; -1: not yet
@@ -49,61 +46,53 @@ static uint64_t binom(int n, int k) {
   return r;
 }
 
-void ed_lin_free(ed_lin* L) {
-  if (!L) return;
-  if (L->d_t0) cudaFree(L->d_t0);
-  if (L->d_t1) cudaFree(L->d_t1);
-  delete L;
+void ed_lin_free(ed_lin* L) { delete L; }
+
+int ed_basis_lin_tables(ed_basis* b) {
+  const int N = b->nspins, nup = b->nup;
+  const int w0 = std::min(LIN_MAX_W0, (N + 1) / 2), w1 = N - w0;
+  std::vector<uint16_t> t0((size_t)1 << w0);
+  std::vector<uint32_t> t1((size_t)1 << w1);
+  for (uint32_t c = 0; c < t0.size(); ++c) {
+    uint64_t v = 0;
+    int k = 0;
+    for (int p = 0; p < w0; ++p)
+      if ((c >> p) & 1u) v += binom(p, ++k);
+    t0[c] = (uint16_t)v;
+  }
+  for (uint32_t c = 0; c < t1.size(); ++c) {
+    const int k0 = nup - __builtin_popcount(c);
+    uint64_t v = 0;
+    if (k0 >= 0 && k0 <= w0) {
+      int k = k0;
+      for (int q = 0; q < w1; ++q)
+        if ((c >> q) & 1u) v += binom(w0 + q, ++k);
+    }
+    t1[c] = (uint32_t)v;
+  }
+  if (cudaMalloc(&b->d_lin_t0, t0.size() * sizeof(uint16_t)) != cudaSuccess ||
+      cudaMalloc(&b->d_lin_t1, t1.size() * sizeof(uint32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    return ed_fail(ED_ENOMEM, "rank tables do not fit in device memory");
+  }
+  cudaError_t e1 = cudaMemcpy(b->d_lin_t0, t0.data(), t0.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+  cudaError_t e2 = cudaMemcpy(b->d_lin_t1, t1.data(), t1.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e1 != cudaSuccess || e2 != cudaSuccess)
+    return ed_cuda_fail(e1 != cudaSuccess ? e1 : e2, "rank table upload", __FILE__, __LINE__);
+  b->lin_w0 = w0;
+  return ED_OK;
 }
 
-// Tables and bond words for h (once per Hamiltonian; the bond set is fixed
-// after build_off_diag).
+// Bond words for h (once per bond set: rebuilt after build_off_diag).
 static int lin_prepare(ed_ham* h) {
   const ed_basis* b = h->basis;
-  const int N = b->nspins, nup = b->nup;
-  if (!h->lin) {
-    ed_lin* L = new ed_lin();
-    L->w0 = std::min(LIN_MAX_W0, (N + 1) / 2);
-    L->w1 = N - L->w0;
-    std::vector<uint16_t> t0((size_t)1 << L->w0);
-    std::vector<uint32_t> t1((size_t)1 << L->w1);
-    for (uint32_t c = 0; c < t0.size(); ++c) {
-      uint64_t v = 0;
-      int k = 0;
-      for (int p = 0; p < L->w0; ++p)
-        if ((c >> p) & 1u) v += binom(p, ++k);
-      t0[c] = (uint16_t)v;
-    }
-    for (uint32_t c = 0; c < t1.size(); ++c) {
-      const int k0 = nup - __builtin_popcount(c);
-      uint64_t v = 0;
-      if (k0 >= 0 && k0 <= L->w0) {
-        int k = k0;
-        for (int q = 0; q < L->w1; ++q)
-          if ((c >> q) & 1u) v += binom(L->w0 + q, ++k);
-      }
-      t1[c] = (uint32_t)v;
-    }
-    if (cudaMalloc(&L->d_t0, t0.size() * sizeof(uint16_t)) != cudaSuccess ||
-        cudaMalloc(&L->d_t1, t1.size() * sizeof(uint32_t)) != cudaSuccess) {
-      cudaGetLastError();
-      ed_lin_free(L);
-      return ed_fail(ED_ENOMEM, "rank tables do not fit in device memory");
-    }
-    cudaError_t e1 = cudaMemcpy(L->d_t0, t0.data(), t0.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
-    cudaError_t e2 = cudaMemcpy(L->d_t1, t1.data(), t1.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
-    if (e1 != cudaSuccess || e2 != cudaSuccess) {
-      ed_lin_free(L);
-      return ed_cuda_fail(e1 != cudaSuccess ? e1 : e2, "rank table upload", __FILE__, __LINE__);
-    }
-    h->lin = L;
-  }
+  if (!h->lin) h->lin = new ed_lin();
   ed_lin* L = h->lin;
   if (L->built_nb != h->bs.nb) {
     LinSegs& sg = L->segs;
     memset(&sg, 0, sizeof(sg));
-    sg.w0 = L->w0;
-    const uint32_t low = (1u << L->w0) - 1u;
+    sg.w0 = b->lin_w0;
+    const uint32_t low = (1u << b->lin_w0) - 1u;
     int n = 0;
     for (int cls = 0; cls < 3; ++cls)
       for (int t = 0; t < 2; ++t) {
@@ -111,7 +100,7 @@ static int lin_prepare(ed_ham* h) {
         for (int q = 0; q < h->bs.nb; ++q) {
           const uint32_t m = h->bs.mask[q];
           if (h->bs.type[q] != t || __builtin_popcount(m) != 2) continue;  // i == j never couples
-          const uint32_t m0 = m & low, m1 = m >> L->w0;
+          const uint32_t m0 = m & low, m1 = m >> b->lin_w0;
           const int c = m1 == 0 ? 0 : (m0 == 0 ? 1 : 2);
           if (c != cls) continue;
           sg.word[n++] = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
@@ -277,7 +266,7 @@ static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, 
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const ed_lin* L = h->lin;
-  const size_t smem = sizeof(uint16_t) * ((size_t)1 << L->w0);
+  const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
   ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
@@ -286,7 +275,7 @@ static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, 
   g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * per_sm));
   const int nblk = (int)g;
   if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
-  k<<<nblk, 256, smem, ctx->stream>>>(b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, L->d_t0, L->d_t1,
+  k<<<nblk, 256, smem, ctx->stream>>>(b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, b->d_lin_t0, b->d_lin_t1,
                                       L->segs, h->bs.chalf[0], h->bs.chalf[1], dot ? ctx->d_red : nullptr);
   ED_CHECK_LAUNCH(ctx);
   if (nblk_out) *nblk_out = nblk;

@@ -105,6 +105,10 @@ struct ed_basis {
   RankTables rt{};
   uint32_t* d_tab = nullptr;
   std::vector<uint32_t> h_tab;    // host copy of the rank tables
+  // two-table rank: rank(s) = lin_t0[s & (2^lin_w0 - 1)] + lin_t1[s >> lin_w0]
+  int lin_w0 = 0;
+  uint16_t* d_lin_t0 = nullptr;
+  uint32_t* d_lin_t1 = nullptr;
 };
 
 struct ed_lin;  // two-table fixed-point H.v state (ed_hv_lin.cu)
@@ -145,6 +149,8 @@ struct ed_ham {
 // Launchers implemented in the .cu files.
 // ---------------------------------------------------------------------------
 int ed_build_rank_tables(int nspins, int nup, RankTables& rt, std::vector<uint32_t>& tab);
+// Two-table rank for b (ed_hv_lin.cu): fills b->lin_w0, d_lin_t0, d_lin_t1.
+int ed_basis_lin_tables(ed_basis* b);
 int ed_launch_basis_states(ed_ctx* ctx, int nspins, int nup, int64_t dim, uint32_t* states);
 int ed_launch_rank(ed_ctx* ctx, const ed_basis* b, const uint32_t* states_dev, int64_t n, int64_t* ranks_dev);
 int ed_launch_unrank(ed_ctx* ctx, const ed_basis* b, const int64_t* ranks_dev, int64_t n, uint32_t* states_dev);

@@ -10,73 +10,82 @@
 #include "ed_internal.h"
 #include "ed_device.cuh"
 #include <algorithm>
+#include <cstring>
 
 #define MEAS_G 8
+#define MEAS_GR 16  // pairs per pass when psi is real
 
 struct PairGroup {
   int n;
-  int32_t i[MEAS_G], j[MEAS_G];
+  int32_t i[MEAS_GR], j[MEAS_GR];
 };
 
-template <int K>
+// Groups of up to G pairs per pass over the basis.  Ranks of flipped states
+// come from the basis's two-table rank (T0 in shared memory, T1 through the
+// read-only cache).  REAL: psi has zero imaginary parts (then every result is
+// real and only real parts are accumulated; G = 16 pairs share one pass).
+template <int G, bool REAL>
 __global__ void __launch_bounds__(256) k_expect(const uint32_t* __restrict__ states, const double2* __restrict__ psi,
-                                                int64_t dim, const RankTables rt, int op, const PairGroup pg,
+                                                int64_t dim, const uint16_t* __restrict__ t0,
+                                                const uint32_t* __restrict__ t1, int w0, int op, const PairGroup pg,
                                                 double* __restrict__ partial, int nblk) {
-  extern __shared__ uint32_t stab[];
-  ed_load_tables(stab, rt);
-  double acc[2 * MEAS_G];
+  extern __shared__ uint16_t t0s[];
+  for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
+  __syncthreads();
+  constexpr int NA = REAL ? G : 2 * G;
+  double acc[NA];
 #pragma unroll
-  for (int k = 0; k < 2 * MEAS_G; ++k) acc[k] = 0.0;
+  for (int k = 0; k < NA; ++k) acc[k] = 0.0;
+  const uint32_t low = (1u << w0) - 1u;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const uint32_t s = states[r];
     const double2 p = psi[r];
-    const double w = fma(p.x, p.x, p.y * p.y);
+    const double w = REAL ? p.x * p.x : fma(p.x, p.x, p.y * p.y);
 #pragma unroll
-    for (int g = 0; g < MEAS_G; ++g) {
-      if (g >= pg.n) break;
-      const int i = pg.i[g], j = pg.j[g];
-      const uint32_t a = (s >> i) & 1u, b = (s >> j) & 1u;
-      double cr = 0.0, ci = 0.0;
-      // S^z_i S^z_j part: psi * conj(0.25 * (+-1) * psi)
-      if (op == ED_OP_SZSZ || op == ED_OP_SISJ) cr += (a ^ b) ? -0.25 * w : 0.25 * w;
-      if (op != ED_OP_SZSZ) {
-        const double half = (op == ED_OP_SISJ) ? 0.5 : 1.0;
-        if (i == j) {
-          // S+S- = n_i (a = 1), S-S+ = 1 - n_i (a = 0)
-          bool on = (op == ED_OP_SPSM) ? (a == 1u) : (op == ED_OP_SMSP) ? (a == 0u) : true;
-          if (on) cr += half * w;
-        } else {
-          bool on = (op == ED_OP_SPSM) ? (a == 0u && b == 1u) : (op == ED_OP_SMSP) ? (a == 1u && b == 0u) : (a != b);
-          if (on) {
-            const uint32_t c = ed_rank<K>(s ^ ((1u << i) | (1u << j)), stab, rt);
-            const double2 q = __ldg(&psi[c]);
-            // psi_r * conj(psi_c)
-            cr += half * fma(p.x, q.x, p.y * q.y);
-            ci += half * fma(p.y, q.x, -p.x * q.y);
+    for (int g = 0; g < G; ++g) {
+      if (g < pg.n) {
+        const int i = pg.i[g], j = pg.j[g];
+        const uint32_t a = (s >> i) & 1u, b = (s >> j) & 1u;
+        double cr = 0.0, ci = 0.0;
+        // S^z_i S^z_j part: psi * conj(0.25 * (+-1) * psi)
+        if (op == ED_OP_SZSZ || op == ED_OP_SISJ) cr += (a ^ b) ? -0.25 * w : 0.25 * w;
+        if (op != ED_OP_SZSZ) {
+          const double half = (op == ED_OP_SISJ) ? 0.5 : 1.0;
+          if (i == j) {
+            // S+S- = n_i (a = 1), S-S+ = 1 - n_i (a = 0)
+            const bool on = (op == ED_OP_SPSM) ? (a == 1u) : (op == ED_OP_SMSP) ? (a == 0u) : true;
+            if (on) cr += half * w;
+          } else {
+            const bool on = (op == ED_OP_SPSM) ? (a == 0u && b == 1u) : (op == ED_OP_SMSP) ? (a == 1u && b == 0u) : (a != b);
+            if (on) {
+              const uint32_t f = s ^ ((1u << i) | (1u << j));
+              const uint32_t c = (uint32_t)t0s[f & low] + __ldg(&t1[f >> w0]);
+              const double2 q = __ldg(&psi[c]);
+              // psi_r * conj(psi_c)
+              if (REAL) {
+                cr += half * (p.x * q.x);
+              } else {
+                cr += half * fma(p.x, q.x, p.y * q.y);
+                ci += half * fma(p.y, q.x, -p.x * q.y);
+              }
+            }
           }
         }
+        if (REAL) {
+          acc[g] += cr;
+        } else {
+          acc[2 * g] += cr;
+          acc[2 * g + 1] += ci;
+        }
       }
-      acc[2 * g] += cr;
-      acc[2 * g + 1] += ci;
     }
   }
-  // block reduction
-  __shared__ double sh[2 * MEAS_G * 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ double sh[NA * 32];
+  ed_block_reduce<NA>(acc, sh);
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int k = 0; k < 2 * MEAS_G; ++k) {
-    double v = acc[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[k * 32 + wid] = v;
-  }
-  __syncthreads();
-  if (wid == 0) {
-    for (int k = 0; k < 2 * MEAS_G; ++k) {
-      double v = lane < nw ? sh[k * 32 + lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) partial[(size_t)k * nblk + blockIdx.x] = v;
-    }
+    for (int k = 0; k < NA; ++k) partial[(size_t)k * nblk + blockIdx.x] = acc[k];
   }
 }
 
@@ -95,42 +104,44 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int nblk, int
   if (threadIdx.x == 0) out[item] = sh[0];
 }
 
-template <int K>
-static int expect_k(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np, double2* out) {
+template <int G, bool REAL>
+static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np, double2* out) {
   ed_ctx* ctx = b->ctx;
   const int64_t dim = b->dim;
-  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 2));
-  const int items = 2 * MEAS_G;
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 4));
+  const int items = REAL ? G : 2 * G;
   ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items + 8));
-  size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
-  ED_CUDA(cudaFuncSetAttribute(k_expect<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
+  const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   double* out_dev = ctx->d_red + (size_t)items * nblk;
-  for (int64_t p0 = 0; p0 < np; p0 += MEAS_G) {
+  for (int64_t p0 = 0; p0 < np; p0 += G) {
     PairGroup pg;
-    pg.n = (int)std::min<int64_t>(MEAS_G, np - p0);
-    for (int g = 0; g < MEAS_G; ++g) {
-      pg.i[g] = g < pg.n ? pairs[2 * (p0 + g)] : 0;
-      pg.j[g] = g < pg.n ? pairs[2 * (p0 + g) + 1] : 0;
+    memset(&pg, 0, sizeof(pg));
+    pg.n = (int)std::min<int64_t>(G, np - p0);
+    for (int g = 0; g < pg.n; ++g) {
+      pg.i[g] = pairs[2 * (p0 + g)];
+      pg.j[g] = pairs[2 * (p0 + g) + 1];
     }
-    k_expect<K><<<nblk, 256, smem, ctx->stream>>>(b->d_states, psi, dim, b->rt, op, pg, ctx->d_red, nblk);
+    k_expect<G, REAL><<<nblk, 256, smem, ctx->stream>>>(b->d_states, psi, dim, b->d_lin_t0, b->d_lin_t1, b->lin_w0, op,
+                                                        pg, ctx->d_red, nblk);
     ED_CHECK_LAUNCH(ctx);
     k_sum_partials<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, items, out_dev);
     ED_CHECK_LAUNCH(ctx);
     ED_CUDA(cudaMemcpyAsync(ctx->h_red, out_dev, sizeof(double) * items, cudaMemcpyDeviceToHost, ctx->stream));
     ED_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int g = 0; g < pg.n; ++g) { out[p0 + g].x = ctx->h_red[2 * g]; out[p0 + g].y = ctx->h_red[2 * g + 1]; }
+    for (int g = 0; g < pg.n; ++g) {
+      out[p0 + g].x = REAL ? ctx->h_red[g] : ctx->h_red[2 * g];
+      out[p0 + g].y = REAL ? 0.0 : ctx->h_red[2 * g + 1];
+    }
   }
   return ED_OK;
 }
 
 int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np,
                            double2* out) {
-  switch (b->rt.K) {
-    case 1: return expect_k<1>(b, op, psi, pairs, np, out);
-    case 2: return expect_k<2>(b, op, psi, pairs, np, out);
-    case 3: return expect_k<3>(b, op, psi, pairs, np, out);
-    default: return expect_k<4>(b, op, psi, pairs, np, out);
-  }
+  bool real = false;
+  ED_TRY(ed_is_real(b->ctx, psi, b->dim, &real));
+  if (real) return expect_g<MEAS_GR, true>(b, op, psi, pairs, np, out);
+  return expect_g<MEAS_G, false>(b, op, psi, pairs, np, out);
 }
 
 // ---------------------------------------------------------------------------
