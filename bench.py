@@ -303,6 +303,14 @@ def run_disorder(args):
     return 0
 
 
+def hv_bytes_per_row(kb, real_gathers):
+    """Algorithmic bytes per row of one matrix-free H.v: x_s (16) + the
+    gathered x_s' (16 per entry, or 8 when the input is real and the
+    fixed-point copy holds only real parts) + y_s (16) + state (4) + diagonal
+    (8)."""
+    return 16 + (8 if real_gathers else 16) * kb + 16 + 4 + 8
+
+
 def run_hv_only(args):
     """Time the matrix-free H.v alone (K launches after W warm-up launches,
     CUDA events on the launching stream) for the workload's Hamiltonian."""
@@ -323,7 +331,10 @@ def run_hv_only(args):
     dim = b.size
     x = torch.empty(dim, dtype=torch.complex128, device='cuda')
     x.real.uniform_(-1, 1)
-    x.imag.uniform_(-1, 1)
+    if args.real_input:
+        x.imag.zero_()
+    else:
+        x.imag.uniform_(-1, 1)
     x /= torch.linalg.vector_norm(x)
     y = torch.empty_like(x)
     for _ in range(args.warmup):
@@ -340,13 +351,16 @@ def run_hv_only(args):
     n_hv, ms_hv = env.profile_read()
     env.profile(False)
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
-    bytes_row = 16 + 16 * kbar(N, b.nspins_up, pairs) + 16 + 4 + 8
+    real_mode = args.real_input and args.acc == 'fixed64'
+    bytes_row = hv_bytes_per_row(kbar(N, b.nspins_up, pairs), real_mode)
     ms = ms_hv / max(n_hv, 1)
     peak, _ = measured_peaks()
     gbs = dim * bytes_row / (ms * 1e-3) / 1e9
-    print(json.dumps({'mode': 'hv-only', 'workload': wl, 'acc': args.acc, 'dim': dim, 'launches': n_hv,
-                      'ms_per_hv': ms, 'ms_per_step_events': e0.elapsed_time(e1) / args.steps,
-                      'algorithmic_gbs': gbs, 'frac_of_measured_hbm': gbs / peak, 'bytes_per_row': bytes_row}))
+    print(json.dumps({'mode': 'hv-only', 'workload': wl, 'acc': args.acc, 'real_input': bool(args.real_input),
+                      'dim': dim, 'launches': n_hv, 'ms_per_hv': ms,
+                      'ms_per_step_events': e0.elapsed_time(e1) / args.steps, 'algorithmic_gbs': gbs,
+                      'frac_of_measured_hbm': gbs / peak, 'bytes_per_row': bytes_row,
+                      'variant': H.hv_variant(False)}))
     return 0
 
 
@@ -432,7 +446,10 @@ def run_ours(args):
     # roofline of the dominant kernel (H.v): algorithmic bytes per launch
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
     kb = kbar(N, b.nspins_up, pairs)
-    bytes_row = 16 + 16 * kb + 16 + 4 + 8
+    # the solve starts from a real vector (H real symmetric): every H.v input
+    # is real and gathers 8-byte real parts of the fixed-point copy
+    bytes_row = hv_bytes_per_row(kb, True)
+    bytes_row_complex = hv_bytes_per_row(kb, False)
     hv_ms = ms_hv / max(n_hv, 1)
     achieved = dim * bytes_row / (hv_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
@@ -507,7 +524,8 @@ def run_ours(args):
                      'kernel': 'matrix-free H.v: k_hv_lin (two-table rank) + k_quantize64 + k_max_exponent',
                      'hv_variant': {'plain': H.hv_variant(False), 'fused_dot': H.hv_variant(True)},
                      'traffic_note': traffic_note, 'peak_kind': peak_kind,
-                     'bytes_per_row': bytes_row, 'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
+                     'bytes_per_row': bytes_row, 'bytes_per_row_complex_input': bytes_row_complex,
+                     'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
                      'launches_timed': n_hv},
         'hv_gbs': achieved, 'sisj_all_pairs': sisj,
         'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'ortho_passes': st['ortho_passes'],
@@ -548,6 +566,7 @@ def main():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
+    ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
     ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')

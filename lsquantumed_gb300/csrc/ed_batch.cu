@@ -336,15 +336,29 @@ __global__ void k_batch_extract(const double2* __restrict__ src, int64_t dim, in
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) dst[r] = src[(size_t)r * B + b];
 }
 
-// copy column b of src into column b of dst (both [dim][B])
-__global__ void k_batch_copy_col(const double2* __restrict__ src, double2* __restrict__ dst, int64_t dim, int B,
-                                 const int* __restrict__ cols, int ncols) {
-  const int64_t n = dim * ncols;
+// dst[r][t] = src[r][keep[t]]: realisation columns keep[0..A2) of a [dim][A]
+// array packed into a [dim][A2] array (the active set after convergence).
+template <typename T>
+__global__ void k_batch_pack(const T* __restrict__ src, T* __restrict__ dst, int64_t dim, int A, int A2,
+                             const int* __restrict__ keep) {
+  const int64_t n = dim * A2;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    const int64_t r = k / ncols;
-    const int b = cols[k % ncols];
-    dst[(size_t)r * B + b] = src[(size_t)r * B + b];
+    const int64_t r = k / A2;
+    dst[k] = src[(size_t)r * A + keep[k % A2]];
+  }
+}
+
+// dst[r][orig[t]] = src[r][slot[t]]: converged slots of a [dim][A] array into
+// their realisations' columns of a [dim][B] array.
+__global__ void k_batch_save(const double2* __restrict__ src, double2* __restrict__ dst, int64_t dim, int A, int B,
+                             const int* __restrict__ slot, const int* __restrict__ orig, int ns) {
+  const int64_t n = dim * ns;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const int64_t r = k / ns;
+    const int t = (int)(k % ns);
+    dst[(size_t)r * B + orig[t]] = src[(size_t)r * A + slot[t]];
   }
 }
 
@@ -371,10 +385,10 @@ static int batch_reduce_buf(ed_batch* bt, size_t doubles) {
 
 // dots of nv vectors against w, per realisation; out (host) [item][B]: item
 // 2i = Re, 2i+1 = Im of V_i^H w, item 2nv = ||w||^2.
-static int batch_dots(ed_batch* bt, const std::vector<const double2*>& V, const double2* w, bool real, bool norm,
+static int batch_dots(ed_batch* bt, int B, const std::vector<const double2*>& V, const double2* w, bool real, bool norm,
                       std::vector<double>& out) {
   ed_ctx* ctx = bt->h->ctx;
-  const int B = bt->B, nv = (int)V.size();
+  const int nv = (int)V.size();
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 2));
   const int64_t items = (int64_t)(2 * nv + 1) * B;
   ED_TRY(batch_reduce_buf(bt, (size_t)items * nblk + (size_t)items));
@@ -396,11 +410,13 @@ static int batch_dots(ed_batch* bt, const std::vector<const double2*>& V, const 
   return ED_OK;
 }
 
-static int batch_hv(ed_batch* bt, const double2* x, double2* y) {
+// y = H_b x for the B (active) realisation columns of x, whose diagonals are
+// the columns of diag ([dim][B]).
+static int batch_hv(ed_batch* bt, int B, const double* diag, const double2* x, double2* y) {
   ed_ham* h = bt->h;
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
-  const int64_t n = bt->dim * bt->B;
+  const int64_t n = bt->dim * B;
   int cnt[2] = {0, 0};
   for (int q = 0; q < h->bs.nb; ++q) cnt[h->bs.type[q] & 1]++;
   int head = 0;
@@ -426,13 +442,13 @@ static int batch_hv(ed_batch* bt, const double2* x, double2* y) {
     attr = true;
   }
   int per_sm = 0;
-  const int threads = std::min(256, ((bt->B + 31) / 32) * 32);
+  const int threads = std::min(256, ((B + 31) / 32) * 32);
   ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv, threads, smem));
   if (per_sm < 1) per_sm = 1;
   const int64_t tiles = (bt->dim + BH_ROWS - 1) / BH_ROWS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
-  k_batch_hv<<<grid, threads, smem, ctx->stream>>>(b->d_states, bt->d_diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim,
-                                                   bt->B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
+  k_batch_hv<<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim, B,
+                                                   b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
                                                    h->bs.chalf[1]);
   ED_CHECK_LAUNCH(ctx);
   return ED_OK;
@@ -501,7 +517,7 @@ int ed_batch_destroy(ed_batch* bt) {
 int ed_batch_apply(ed_batch* bt, const ed_cplx* x_dev, ed_cplx* y_dev) {
   if (!bt || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
   if ((const void*)x_dev == (const void*)y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
-  return batch_hv(bt, (const double2*)x_dev, (double2*)y_dev);
+  return batch_hv(bt, bt->B, bt->d_diag, (const double2*)x_dev, (double2*)y_dev);
 }
 
 int ed_batch_diag_host(ed_batch* bt, double* out_host) {
@@ -513,9 +529,12 @@ int ed_batch_diag_host(ed_batch* bt, double* out_host) {
 }
 
 // Lockstep Krylov-Schur over the batch (same method as ed_eps_solve: local
-// Lanczos projection + one CGS pass with the DGKS refinement test, real
-// coefficients, thick restart), all realisations restarted together keeping
-// l = max(nev + 2, ncv / 2) vectors.
+// Lanczos projection + one CGS pass with the DGKS refinement test, thick
+// restart keeping l = max(nev + 2, ncv / 2) vectors), with exact real
+// arithmetic (real start vectors, real H).  At every restart the
+// realisations whose nev pairs converged save their Ritz vectors and leave
+// the active block, which is packed to the remaining A columns, so the work
+// follows the sum of the realisations' iterations, not B times the slowest.
 int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed, double* evals_host,
                    double* errs_host, int* nconv_host) {
   if (!bt || !evals_host || !errs_host || !nconv_host) return ed_fail(ED_EINVAL, "null argument");
@@ -531,126 +550,129 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   if (tol <= 0) tol = 1e-8;
   if (max_it <= 0) max_it = (int)std::max<int64_t>(100, 2 * dim / std::max(m, 1));
   const int l_keep = std::min(m - 1, std::max(nev + 2, m / 2));
-  const size_t colsz = (size_t)dim * B;
-  // storage: 2m+1 columns of [dim][B] + w
+  const size_t colB = (size_t)dim * B;
+  const int pool_cols = 2 * m + 1;
   double2* pool = nullptr;
   double2* w = nullptr;
-  const int pool_cols = 2 * m + 1;
-  if (cudaMalloc(&pool, sizeof(double2) * colsz * pool_cols) != cudaSuccess ||
-      cudaMalloc(&w, sizeof(double2) * colsz) != cudaSuccess) {
+  double* dg[2] = {nullptr, nullptr};
+  double* d_coef = nullptr;  // [64][B] double2 coefficients / scale factors
+  int* d_idx = nullptr;      // [2][B] slot / realisation index lists
+  double* dY = nullptr;
+  if (cudaMalloc(&pool, sizeof(double2) * colB * pool_cols) != cudaSuccess ||
+      cudaMalloc(&w, sizeof(double2) * colB) != cudaSuccess || cudaMalloc(&dg[0], sizeof(double) * colB) != cudaSuccess ||
+      cudaMalloc(&dg[1], sizeof(double) * colB) != cudaSuccess ||
+      cudaMalloc(&d_coef, sizeof(double2) * 64 * (size_t)B) != cudaSuccess ||
+      cudaMalloc(&d_idx, sizeof(int) * 2 * (size_t)B) != cudaSuccess ||
+      cudaMalloc(&dY, sizeof(double) * (size_t)B * m * l_keep) != cudaSuccess) {
     cudaGetLastError();
-    if (pool) cudaFree(pool);
+    cudaFree(pool); cudaFree(w); cudaFree(dg[0]); cudaFree(dg[1]); cudaFree(d_coef); cudaFree(d_idx); cudaFree(dY);
     return ed_fail(ED_ENOMEM, "batched Krylov basis does not fit in device memory");
   }
   if (bt->d_vecs) cudaFree(bt->d_vecs);
   bt->d_vecs = nullptr;
-  if (cudaMalloc(&bt->d_vecs, sizeof(double2) * colsz * nev) != cudaSuccess) {
+  if (cudaMalloc(&bt->d_vecs, sizeof(double2) * colB * nev) != cudaSuccess) {
     cudaGetLastError();
-    cudaFree(pool);
-    cudaFree(w);
+    cudaFree(pool); cudaFree(w); cudaFree(dg[0]); cudaFree(dg[1]); cudaFree(d_coef); cudaFree(d_idx); cudaFree(dY);
     return ed_fail(ED_ENOMEM, "batched eigenvectors do not fit in device memory");
   }
   std::vector<double2*> col(m + 1), freel;
   for (int i = 0; i < pool_cols; ++i) {
-    double2* p = pool + (size_t)i * colsz;
+    double2* p = pool + (size_t)i * colB;
     if (i <= m) col[i] = p; else freel.push_back(p);
   }
-  double* d_coef = nullptr;  // [64][B] double2 coefficients / scale factors
-  ED_CUDA(cudaMalloc(&d_coef, sizeof(double2) * 64 * (size_t)B));
+  int cur = 0;  // dg[cur] holds the active realisations' diagonals
   int rc = ED_OK;
   std::vector<double> out;
   std::vector<double> alpha((size_t)B * (m + 1)), beta((size_t)B * (m + 1)), arrow((size_t)B * (m + 1));
-  std::vector<int> done(B, 0), nconv(B, 0);
+  std::vector<int> act(B), nconv(B, 0);
+  for (int b = 0; b < B; ++b) act[b] = b;
   bt->evals.assign((size_t)B * nev, 0.0);
   bt->errs.assign((size_t)B * nev, 0.0);
   std::vector<double> theta, Y, T;
-  std::vector<double> Yall((size_t)B * m * l_keep);
-  int k = 0, its = 0, remaining = B;
+  std::vector<double> Yall;
+  int k = 0, its = 0, A = B;
   bt->nhv = 0;
-  auto fail = [&](int code) { rc = code; };
+  ED_CUDA(cudaMemcpyAsync(dg[0], bt->d_diag, sizeof(double) * colB, cudaMemcpyDeviceToDevice, ctx->stream));
   // start vectors, normalised per realisation
-  k_batch_start<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(seed, dim, B, col[0]);
+  k_batch_start<<<grid_n(ctx, (int64_t)colB), 256, 0, ctx->stream>>>(seed, dim, A, col[0]);
   ctx->kernels++;
   {
     std::vector<const double2*> none;
-    if ((rc = batch_dots(bt, none, col[0], true, true, out)) != ED_OK) goto cleanup;
-    std::vector<double> sc(B);
-    for (int b = 0; b < B; ++b) sc[b] = 1.0 / std::sqrt(out[b]);
-    cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * B, cudaMemcpyHostToDevice, ctx->stream);
-    k_batch_scale<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(col[0], col[0], d_coef, dim, B);
+    if ((rc = batch_dots(bt, A, none, col[0], true, true, out)) != ED_OK) goto cleanup;
+    std::vector<double> sc(A);
+    for (int b = 0; b < A; ++b) sc[b] = 1.0 / std::sqrt(out[b]);
+    cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
+    k_batch_scale<<<grid_n(ctx, (int64_t)dim * A), 256, 0, ctx->stream>>>(col[0], col[0], d_coef, dim, A);
     ctx->kernels++;
   }
-  while (remaining > 0 && its < max_it) {
+  while (A > 0 && its < max_it) {
     ++its;
+    const int64_t colA = dim * (int64_t)A;
     for (int j = k; j < m; ++j) {
-      if ((rc = batch_hv(bt, col[j], w)) != ED_OK) goto cleanup;
+      if ((rc = batch_hv(bt, A, dg[cur], col[j], w)) != ED_OK) goto cleanup;
       bt->nhv++;
-      // local projection coefficients: a_b = v_j^H w (real), beta_{j-1}
+      // local projection coefficients: a_b = v_j^H w, beta_{j-1}
       std::vector<const double2*> vj(1, col[j]);
-      if ((rc = batch_dots(bt, vj, w, true, true, out)) != ED_OK) goto cleanup;
-      std::vector<double> yn(B), a(B);
-      for (int b = 0; b < B; ++b) { a[b] = out[(size_t)0 * B + b]; yn[b] = std::sqrt(out[(size_t)2 * B + b]); }
-      // w -= a v_j + beta v_{j-1}
+      if ((rc = batch_dots(bt, A, vj, w, true, true, out)) != ED_OK) goto cleanup;
       {
-        std::vector<double2> hc((size_t)2 * B);
+        std::vector<double2> hc((size_t)2 * A);
         const bool three = j > k && j > 0;
-        for (int b = 0; b < B; ++b) {
-          hc[b] = make_double2(a[b], 0.0);
-          hc[(size_t)B + b] = make_double2(three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0, 0.0);
+        for (int b = 0; b < A; ++b) {
+          const double a = out[b];
+          alpha[(size_t)b * (m + 1) + j] = a;
+          hc[b] = make_double2(a, 0.0);
+          hc[(size_t)A + b] = make_double2(three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0, 0.0);
         }
-        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * 2 * B, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * 2 * A, cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
         vc.p[0] = col[j];
         vc.p[1] = three ? col[j - 1] : col[j];
-        k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, three ? 2 : 1,
-                                                                                   (const double2*)d_coef, w, dim, B);
+        k_batch_update<true><<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, three ? 2 : 1, (const double2*)d_coef, w,
+                                                                         dim, A);
         ctx->kernels++;
-        for (int b = 0; b < B; ++b) {
-          alpha[(size_t)b * (m + 1) + j] = a[b];
-        }
       }
       // full CGS pass (+ DGKS refinement when any realisation needs it)
       std::vector<const double2*> vs(col.begin(), col.begin() + j + 1);
-      std::vector<double> prevn(B, 0.0);
+      std::vector<double> prevn(A, 0.0);
       for (int pass = 0; pass < 2; ++pass) {
-        if ((rc = batch_dots(bt, vs, w, true, true, out)) != ED_OK) goto cleanup;
-        std::vector<double2> hc((size_t)(j + 1) * B);
+        if ((rc = batch_dots(bt, A, vs, w, true, true, out)) != ED_OK) goto cleanup;
+        std::vector<double2> hc((size_t)(j + 1) * A);
         for (int i = 0; i <= j; ++i)
-          for (int b = 0; b < B; ++b) hc[(size_t)i * B + b] = make_double2(out[((size_t)2 * i) * B + b], 0.0);
-        for (int b = 0; b < B; ++b) prevn[b] = std::sqrt(out[((size_t)2 * (j + 1)) * B + b]);
+          for (int b = 0; b < A; ++b) hc[(size_t)i * A + b] = make_double2(out[((size_t)2 * i) * A + b], 0.0);
+        for (int b = 0; b < A; ++b) prevn[b] = std::sqrt(out[((size_t)2 * (j + 1)) * A + b]);
         cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
         for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
-        k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, j + 1, (const double2*)d_coef, w,
-                                                                                   dim, B);
+        k_batch_update<true><<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, j + 1, (const double2*)d_coef, w, dim, A);
         ctx->kernels++;
-        for (int b = 0; b < B; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * B + b].x;
+        for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b].x;
         // norms after the update
         std::vector<const double2*> none;
-        if ((rc = batch_dots(bt, none, w, true, true, out)) != ED_OK) goto cleanup;
+        if ((rc = batch_dots(bt, A, none, w, true, true, out)) != ED_OK) goto cleanup;
         bool again = false;
-        for (int b = 0; b < B; ++b) {
+        for (int b = 0; b < A; ++b) {
           const double nw = std::sqrt(out[b]);
           beta[(size_t)b * (m + 1) + j] = nw;
-          if (!done[b] && nw < 0.7071067811865476 * prevn[b]) again = true;
+          if (nw < 0.7071067811865476 * prevn[b]) again = true;
         }
         if (!again) break;
       }
       // normalise into col[j+1]
-      std::vector<double> sc(B);
-      for (int b = 0; b < B; ++b) {
+      std::vector<double> sc(A);
+      for (int b = 0; b < A; ++b) {
         const double nb = beta[(size_t)b * (m + 1) + j];
         sc[b] = nb > 1e-300 ? 1.0 / nb : 0.0;
       }
-      cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * B, cudaMemcpyHostToDevice, ctx->stream);
-      k_batch_scale<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, B);
+      cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
+      k_batch_scale<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A);
       ctx->kernels++;
     }
-    // projected problems, convergence and restart, per realisation
-    std::vector<int> newly;
-    for (int b = 0; b < B; ++b) {
+    // projected problems, convergence and restart, per active realisation
+    std::vector<int> conv_slots, keep_slots;
+    Yall.assign((size_t)A * m * l_keep, 0.0);
+    for (int b = 0; b < A; ++b) {
       T.assign((size_t)m * m, 0.0);
       const double* al = &alpha[(size_t)b * (m + 1)];
       const double* be = &beta[(size_t)b * (m + 1)];
@@ -670,15 +692,12 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
         const double res = std::fabs(bm * Y[(size_t)(m - 1) * m + i]);
         if (res / std::max(std::fabs(theta[i]), 1e-300) < tol) ++nc; else break;
       }
-      for (int i = 0; i < l_keep; ++i)
-        for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = 0.0;
       for (int i = 0; i < m; ++i)
         for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = Y[(size_t)i * m + c];
-      if (!done[b]) {
-        nconv[b] = nc;
-        for (int i = 0; i < nev; ++i) bt->evals[(size_t)b * nev + i] = theta[i];
-        if (nc >= nev || its >= max_it) { newly.push_back(b); }
-      }
+      const int o = act[b];
+      nconv[o] = nc;
+      for (int i = 0; i < nev; ++i) bt->evals[(size_t)o * nev + i] = theta[i];
+      if (nc >= nev || its >= max_it) conv_slots.push_back(b); else keep_slots.push_back(b);
       // kept Ritz values and arrow couplings for the next cycle
       for (int i = 0; i < l_keep; ++i) {
         alpha[(size_t)b * (m + 1) + i] = theta[i];
@@ -686,69 +705,100 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       }
     }
     // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
+    std::vector<double2*> outc(freel.begin(), freel.begin() + l_keep);
     {
-      double* dY = nullptr;
-      ED_CUDA(cudaMalloc(&dY, sizeof(double) * Yall.size()));
-      cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream);
+      ED_CUDA(cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream));
       BCols vin, vout;
       memset(&vin, 0, sizeof(vin));
       memset(&vout, 0, sizeof(vout));
       for (int i = 0; i < m; ++i) vin.p[i] = col[i];
-      std::vector<double2*> outc(freel.begin(), freel.begin() + l_keep);
       for (int c = 0; c < l_keep; ++c) vout.p[c] = outc[c];
       for (int c0 = 0; c0 < l_keep; c0 += 8) {
-        k_batch_restart<<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vin, m, dY, l_keep, vout, c0,
-                                                                              std::min(8, l_keep - c0), dim, B);
+        k_batch_restart<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vin, m, dY, l_keep, vout, c0,
+                                                                    std::min(8, l_keep - c0), dim, A);
         ctx->kernels++;
       }
-      cudaStreamSynchronize(ctx->stream);
-      cudaFree(dY);
-      // save converged realisations' Ritz vectors
-      if (!newly.empty()) {
-        int* dcols = nullptr;
-        ED_CUDA(cudaMalloc(&dcols, sizeof(int) * newly.size()));
-        cudaMemcpyAsync(dcols, newly.data(), sizeof(int) * newly.size(), cudaMemcpyHostToDevice, ctx->stream);
-        for (int i = 0; i < nev; ++i) {
-          k_batch_copy_col<<<grid_n(ctx, dim * (int64_t)newly.size()), 256, 0, ctx->stream>>>(
-              outc[i], bt->d_vecs + (size_t)i * colsz, dim, B, dcols, (int)newly.size());
-          ctx->kernels++;
-        }
-        cudaStreamSynchronize(ctx->stream);
-        cudaFree(dcols);
-        for (int b : newly) { done[b] = 1; --remaining; }
-      }
-      std::vector<double2*> newcol(m + 1, nullptr);
-      for (int c = 0; c < l_keep; ++c) newcol[c] = outc[c];
-      newcol[l_keep] = col[m];
-      std::vector<double2*> nf(freel.begin() + l_keep, freel.end());
-      for (int c = 0; c < m; ++c) nf.push_back(col[c]);
-      for (int c = l_keep + 1; c <= m; ++c) { newcol[c] = nf.back(); nf.pop_back(); }
-      col.swap(newcol);
-      freel.swap(nf);
     }
+    // converged realisations: save their Ritz vectors
+    if (!conv_slots.empty()) {
+      const int ns = (int)conv_slots.size();
+      std::vector<int> idx(2 * (size_t)ns);
+      for (int t = 0; t < ns; ++t) { idx[t] = conv_slots[t]; idx[(size_t)ns + t] = act[conv_slots[t]]; }
+      ED_CUDA(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, ctx->stream));
+      for (int i = 0; i < nev; ++i) {
+        k_batch_save<<<grid_n(ctx, dim * (int64_t)ns), 256, 0, ctx->stream>>>(outc[i], bt->d_vecs + (size_t)i * colB,
+                                                                              dim, A, B, d_idx, d_idx + ns, ns);
+        ctx->kernels++;
+      }
+    }
+    // new column order: restarted vectors, then the residual vector
+    std::vector<double2*> newcol(m + 1, nullptr);
+    for (int c = 0; c < l_keep; ++c) newcol[c] = outc[c];
+    newcol[l_keep] = col[m];
+    std::vector<double2*> nf(freel.begin() + l_keep, freel.end());
+    for (int c = 0; c < m; ++c) nf.push_back(col[c]);
+    // pack the live columns and the diagonals to the realisations still active
+    const int A2 = (int)keep_slots.size();
+    if (A2 > 0 && A2 < A) {
+      ED_CUDA(cudaMemcpyAsync(d_idx, keep_slots.data(), sizeof(int) * A2, cudaMemcpyHostToDevice, ctx->stream));
+      for (int c = 0; c <= l_keep; ++c) {
+        double2* dst = nf.back();
+        nf.pop_back();
+        k_batch_pack<double2><<<grid_n(ctx, dim * (int64_t)A2), 256, 0, ctx->stream>>>(newcol[c], dst, dim, A, A2,
+                                                                                      d_idx);
+        ctx->kernels++;
+        nf.push_back(newcol[c]);
+        newcol[c] = dst;
+      }
+      k_batch_pack<double><<<grid_n(ctx, dim * (int64_t)A2), 256, 0, ctx->stream>>>(dg[cur], dg[1 - cur], dim, A, A2,
+                                                                                   d_idx);
+      ctx->kernels++;
+      cur = 1 - cur;
+      std::vector<double> a2((size_t)A2 * (m + 1)), b2((size_t)A2 * (m + 1)), r2((size_t)A2 * (m + 1));
+      std::vector<int> act2(A2);
+      for (int t = 0; t < A2; ++t) {
+        const int sl = keep_slots[t];
+        act2[t] = act[sl];
+        for (int i = 0; i <= m; ++i) {
+          a2[(size_t)t * (m + 1) + i] = alpha[(size_t)sl * (m + 1) + i];
+          b2[(size_t)t * (m + 1) + i] = beta[(size_t)sl * (m + 1) + i];
+          r2[(size_t)t * (m + 1) + i] = arrow[(size_t)sl * (m + 1) + i];
+        }
+      }
+      std::copy(a2.begin(), a2.end(), alpha.begin());
+      std::copy(b2.begin(), b2.end(), beta.begin());
+      std::copy(r2.begin(), r2.end(), arrow.begin());
+      act.swap(act2);
+    } else if (A2 == 0) {
+      act.clear();
+    }
+    for (int c = l_keep + 1; c <= m; ++c) { newcol[c] = nf.back(); nf.pop_back(); }
+    col.swap(newcol);
+    freel.swap(nf);
+    // the host index lists above are reused by the next cycle's copies
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));
+    A = A2;
     k = l_keep;
   }
   // true relative residuals ||H x - theta x|| / |theta| of the saved vectors
   for (int i = 0; i < nev; ++i) {
-    double2* xv = bt->d_vecs + (size_t)i * colsz;
-    if ((rc = batch_hv(bt, xv, w)) != ED_OK) goto cleanup;
-    std::vector<double> th(B);
-    for (int b = 0; b < B; ++b) th[b] = bt->evals[(size_t)b * nev + i];
-    // w -= theta x  (per realisation), then ||w||, ||x||
+    double2* xv = bt->d_vecs + (size_t)i * colB;
+    if ((rc = batch_hv(bt, B, bt->d_diag, xv, w)) != ED_OK) goto cleanup;
     std::vector<double2> hc(B);
-    for (int b = 0; b < B; ++b) hc[b] = make_double2(th[b], 0.0);
+    for (int b = 0; b < B; ++b) hc[b] = make_double2(bt->evals[(size_t)b * nev + i], 0.0);
     cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * B, cudaMemcpyHostToDevice, ctx->stream);
     BCols vc;
     memset(&vc, 0, sizeof(vc));
     vc.p[0] = xv;
-    k_batch_update<true><<<grid_n(ctx, (int64_t)colsz), 256, 0, ctx->stream>>>(vc, 1, (const double2*)d_coef, w, dim, B);
+    k_batch_update<true><<<grid_n(ctx, (int64_t)colB), 256, 0, ctx->stream>>>(vc, 1, (const double2*)d_coef, w, dim, B);
     ctx->kernels++;
     std::vector<const double2*> none;
-    if ((rc = batch_dots(bt, none, w, true, true, out)) != ED_OK) goto cleanup;
+    if ((rc = batch_dots(bt, B, none, w, true, true, out)) != ED_OK) goto cleanup;
     std::vector<double> r2(out.begin(), out.begin() + B);
-    if ((rc = batch_dots(bt, none, xv, true, true, out)) != ED_OK) goto cleanup;
+    if ((rc = batch_dots(bt, B, none, xv, true, true, out)) != ED_OK) goto cleanup;
     for (int b = 0; b < B; ++b)
-      bt->errs[(size_t)b * nev + i] = std::sqrt(r2[b]) / std::max(std::fabs(th[b]) * std::sqrt(out[b]), 1e-300);
+      bt->errs[(size_t)b * nev + i] =
+          std::sqrt(r2[b]) / std::max(std::fabs(bt->evals[(size_t)b * nev + i]) * std::sqrt(out[b]), 1e-300);
   }
   bt->nev = nev;
   bt->nrep = nev;
@@ -762,11 +812,14 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     }
   }
 cleanup:
-  (void)fail;
   cudaStreamSynchronize(ctx->stream);
   cudaFree(pool);
   cudaFree(w);
+  cudaFree(dg[0]);
+  cudaFree(dg[1]);
   cudaFree(d_coef);
+  cudaFree(d_idx);
+  cudaFree(dY);
   return rc;
 }
 

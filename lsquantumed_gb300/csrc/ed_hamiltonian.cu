@@ -422,28 +422,37 @@ __global__ void __launch_bounds__(256) k_hv_fixed(const uint32_t* __restrict__ s
 // term is then one 64-bit add; the sums are exact and rounded once to FP64.
 // Quantisation error per entry <= 2^-(S+1) of the largest |v|.
 // ---------------------------------------------------------------------------
+// gmax[0] = largest finite biased exponent, gmax[1] |= some entry not
+// finite, and with imag != nullptr *imag |= some imaginary part nonzero.
 __global__ void __launch_bounds__(256) k_max_exponent(const double2* __restrict__ x, int64_t dim,
-                                                      int* __restrict__ gmax, int* __restrict__ nonfinite) {
-  int m = 0, nf = 0;
+                                                      int* __restrict__ gmax, int* __restrict__ nonfinite,
+                                                      int* __restrict__ imag) {
+  int m = 0, nf = 0, im = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const double2 v = x[r];
     const int er = (int)(((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7FF);
     const int ei = (int)(((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7FF);
     nf |= (er == 0x7FF) | (ei == 0x7FF);
+    im |= v.y != 0.0;
     m = max(m, max(er == 0x7FF ? 0 : er, ei == 0x7FF ? 0 : ei));
   }
   m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
   nf = (int)__reduce_or_sync(0xffffffffu, (unsigned)nf);
+  im = (int)__reduce_or_sync(0xffffffffu, (unsigned)im);
   if ((threadIdx.x & 31) == 0) {
     if (m > 0) atomicMax(gmax, m);
     if (nf) atomicOr(nonfinite, 1);
+    if (im && imag) atomicOr(imag, 1);
   }
 }
 
+// With imag_p != nullptr and *imag_p == 0 (every imaginary part zero) only
+// the real parts are stored, as int64[dim] at the start of xq.
 __global__ void __launch_bounds__(256) k_quantize64(const double2* __restrict__ x, int64_t dim, const int* __restrict__ gmax_p,
-                                                    int sbits, longlong2* __restrict__ xq) {
+                                                    int sbits, longlong2* __restrict__ xq, const int* __restrict__ imag_p) {
   const int emax = *gmax_p;
+  const bool real_only = imag_p && *imag_p == 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const double2 v = x[r];
@@ -468,7 +477,8 @@ __global__ void __launch_bounds__(256) k_quantize64(const double2* __restrict__ 
       }
       q[k] = m;
     }
-    xq[r] = make_longlong2(q[0], q[1]);
+    if (real_only) ((long long*)xq)[r] = q[0];
+    else xq[r] = make_longlong2(q[0], q[1]);
   }
 }
 
@@ -577,7 +587,7 @@ static int ensure_fixed_buffers(ed_ham* h) {
   if (!h->d_xq) {
     if (cudaMalloc(&h->d_xq, sizeof(longlong2) * (size_t)dim) != cudaSuccess ||
         cudaMalloc(&h->d_xe, sizeof(uint16_t) * (size_t)((dim + 31) / 32)) != cudaSuccess ||
-        cudaMalloc(&h->d_gmax, 2 * sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&h->d_gmax, 4 * sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
       return ed_fail(ED_ENOMEM, "H.v scratch does not fit in device memory");
     }
@@ -622,11 +632,11 @@ int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits) {
   int head = 0;
   while ((1 << head) < max_type_count(h->bs) + 1) ++head;
   *sbits = 62 - head;
-  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 2 * sizeof(int), ctx->stream));
+  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 3 * sizeof(int), ctx->stream));
   const int g = grid_cap(ctx, b->dim, 256, 8);
-  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1, h->d_gmax + 2);
   ED_CHECK_LAUNCH(ctx);
-  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, *sbits, h->d_xq);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, *sbits, h->d_xq, h->d_gmax + 2);
   ED_CHECK_LAUNCH(ctx);
   return ED_OK;
 }
@@ -641,9 +651,9 @@ static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
   const int sbits = 62 - head;
   ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 2 * sizeof(int), ctx->stream));
   const int g = grid_cap(ctx, b->dim, 256, 8);
-  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1, nullptr);
   ED_CHECK_LAUNCH(ctx);
-  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, sbits, h->d_xq);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, sbits, h->d_xq, nullptr);
   ED_CHECK_LAUNCH(ctx);
   size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
   static bool attr_set[5] = {false};
@@ -960,9 +970,9 @@ static int launch_hv_noalloc_k(ed_ham* h, const double2* x, double2* y, unsigned
   const int sbits = 62 - head;
   ED_CUDA(cudaMemsetAsync(gmax, 0, 2 * sizeof(int), ctx->stream));
   const int g = grid_cap(ctx, b->dim, 256, 8);
-  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, gmax + 1);
+  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, gmax + 1, nullptr);
   ED_CHECK_LAUNCH(ctx);
-  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, sbits, xq);
+  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, gmax, sbits, xq, nullptr);
   ED_CHECK_LAUNCH(ctx);
   size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
   ED_CUDA(cudaFuncSetAttribute(k_hv_fx64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));

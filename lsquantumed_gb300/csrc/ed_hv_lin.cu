@@ -113,7 +113,7 @@ static int lin_prepare(ed_ham* h) {
 }
 
 // Bonds inside one half: the flipped state's rank is rb + T[c ^ m].
-template <bool CHECK, bool HIGH, int U>
+template <bool CHECK, bool HIGH, int U, bool RX>
 __device__ __forceinline__ void lin_half(const LinSegs& sg, int b0, int b1, uint32_t c, uint32_t rb,
                                          const uint16_t* __restrict__ t0s, const uint32_t* __restrict__ t1,
                                          const longlong2* __restrict__ xq, long long& ar, long long& ai, bool& bad) {
@@ -130,20 +130,32 @@ __device__ __forceinline__ void lin_half(const LinSegs& sg, int b0, int b1, uint
       on[u] = t != 0u && t != m;  // m == 0 (past the end) is never on
       tgt[u] = rb + (HIGH ? __ldg(&t1[c ^ m]) : (uint32_t)t0s[c ^ m]);
     }
-    longlong2 q[U];
+    if (RX) {
+      const long long* xr = (const long long*)xq;
+      long long q[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+      for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xr[tgt[u]]) : 0ll;
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
-      ar += q[u].x;
-      ai += q[u].y;
+      for (int u = 0; u < U; ++u) {
+        if (CHECK) bad |= q[u] == kNaN;
+        ar += q[u];
+      }
+    } else {
+      longlong2 q[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
+        ar += q[u].x;
+        ai += q[u].y;
+      }
     }
   }
 }
 
 // Bonds across the halves: one site in each, the rank is T0[c0 ^ m0] + T1[c1 ^ m1].
-template <bool CHECK, int U>
+template <bool CHECK, int U, bool RX>
 __device__ __forceinline__ void lin_cross(const LinSegs& sg, int b0, int b1, uint32_t c0, uint32_t c1,
                                           const uint16_t* __restrict__ t0s, const uint32_t* __restrict__ t1,
                                           const longlong2* __restrict__ xq, long long& ar, long long& ai, bool& bad) {
@@ -159,19 +171,31 @@ __device__ __forceinline__ void lin_cross(const LinSegs& sg, int b0, int b1, uin
       on[u] = inb && (((c0 & m0) != 0u) != ((c1 & m1) != 0u));
       tgt[u] = (uint32_t)t0s[c0 ^ m0] + __ldg(&t1[c1 ^ m1]);
     }
-    longlong2 q[U];
+    if (RX) {
+      const long long* xr = (const long long*)xq;
+      long long q[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+      for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xr[tgt[u]]) : 0ll;
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
-      ar += q[u].x;
-      ai += q[u].y;
+      for (int u = 0; u < U; ++u) {
+        if (CHECK) bad |= q[u] == kNaN;
+        ar += q[u];
+      }
+    } else {
+      longlong2 q[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) q[u] = on[u] ? __ldg(&xq[tgt[u]]) : make_longlong2(0, 0);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (CHECK) bad |= (q[u].x == kNaN) | (q[u].y == kNaN);
+        ar += q[u].x;
+        ai += q[u].y;
+      }
     }
   }
 }
 
-template <bool CHECK, bool DOT, int U>
+template <bool CHECK, bool DOT, int U, bool RX>
 __device__ __forceinline__ void lin_rows(const uint32_t* __restrict__ states, const double* __restrict__ diag,
                                          const double2* __restrict__ x, const longlong2* __restrict__ xq,
                                          double2* __restrict__ y, int64_t dim, const uint16_t* __restrict__ t0s,
@@ -187,12 +211,12 @@ __device__ __forceinline__ void lin_rows(const uint32_t* __restrict__ states, co
     const uint32_t rb1 = rr - __ldg(&t1[c1]);
     long long a[4] = {0, 0, 0, 0};  // nn re, nn im, nnn re, nnn im
     bool bad = false;
-    lin_half<CHECK, false, U>(sg, sg.seg[0], sg.seg[1], c0, rb0, t0s, t1, xq, a[0], a[1], bad);
-    lin_half<CHECK, false, U>(sg, sg.seg[1], sg.seg[2], c0, rb0, t0s, t1, xq, a[2], a[3], bad);
-    lin_half<CHECK, true, U>(sg, sg.seg[2], sg.seg[3], c1, rb1, t0s, t1, xq, a[0], a[1], bad);
-    lin_half<CHECK, true, U>(sg, sg.seg[3], sg.seg[4], c1, rb1, t0s, t1, xq, a[2], a[3], bad);
-    lin_cross<CHECK, U>(sg, sg.seg[4], sg.seg[5], c0, c1, t0s, t1, xq, a[0], a[1], bad);
-    lin_cross<CHECK, U>(sg, sg.seg[5], sg.seg[6], c0, c1, t0s, t1, xq, a[2], a[3], bad);
+    lin_half<CHECK, false, U, RX>(sg, sg.seg[0], sg.seg[1], c0, rb0, t0s, t1, xq, a[0], a[1], bad);
+    lin_half<CHECK, false, U, RX>(sg, sg.seg[1], sg.seg[2], c0, rb0, t0s, t1, xq, a[2], a[3], bad);
+    lin_half<CHECK, true, U, RX>(sg, sg.seg[2], sg.seg[3], c1, rb1, t0s, t1, xq, a[0], a[1], bad);
+    lin_half<CHECK, true, U, RX>(sg, sg.seg[3], sg.seg[4], c1, rb1, t0s, t1, xq, a[2], a[3], bad);
+    lin_cross<CHECK, U, RX>(sg, sg.seg[4], sg.seg[5], c0, c1, t0s, t1, xq, a[0], a[1], bad);
+    lin_cross<CHECK, U, RX>(sg, sg.seg[5], sg.seg[6], c0, c1, t0s, t1, xq, a[2], a[3], bad);
     const double d = diag[r];
     const double2 xv = x[r];
     const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
@@ -227,10 +251,16 @@ __global__ void __launch_bounds__(256, MINB) k_hv_lin(const uint32_t* __restrict
   const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
   const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
   double dacc[3] = {0.0, 0.0, 0.0};
-  if (gmax_p[1])  // some input entry is not finite: track the rows that gather it
-    lin_rows<true, DOT, U>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
-  else
-    lin_rows<false, DOT, U>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+  // gmax_p[1]: some input entry is not finite (track the rows that gather it);
+  // gmax_p[2] == 0: x is real and xq holds only real parts
+  const bool rx = gmax_p[2] == 0;
+  if (gmax_p[1]) {
+    if (rx) lin_rows<true, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+    else lin_rows<true, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+  } else {
+    if (rx) lin_rows<false, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+    else lin_rows<false, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+  }
   if (DOT) {
     __shared__ double sh[3 * 32];
     ed_block_reduce<3>(dacc, sh);
@@ -256,7 +286,7 @@ struct LinVariant {
 };
 static const LinVariant kLinVariants[] = {
     {k_hv_lin<false, 4, 6>, k_hv_lin<true, 4, 5>, "u4-b6"},
-    {k_hv_lin<false, 4, 8>, k_hv_lin<true, 4, 6>, "u4-b8"},
+    {k_hv_lin<false, 4, 4>, k_hv_lin<true, 4, 4>, "u4-b4"},
     {k_hv_lin<false, 8, 4>, k_hv_lin<true, 8, 4>, "u8-b4"},
     {k_hv_lin<false, 8, 1>, k_hv_lin<true, 8, 1>, "u8-b1"},
 };

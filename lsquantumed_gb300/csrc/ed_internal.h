@@ -160,8 +160,9 @@ int ed_launch_hv(ed_ham* h, const double2* x, double2* y);
 // y = H x and, in the same pass over the rows, dot = x^H y and *y2 = ||y||^2.
 // Returns ED_ENOTSUP (nothing launched) where the operator has no fused form.
 int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, double* y2);
-// Fixed-point copy of x into h->d_xq (largest exponent and non-finite flag in
-// h->d_gmax[0..1]); *sbits = the fixed-point scale used.
+// Fixed-point copy of x into h->d_xq: largest exponent, non-finite flag and
+// imaginary-nonzero flag in h->d_gmax[0..2]; when every imaginary part is
+// zero only the real parts are stored (int64[dim]).  *sbits = the scale.
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
 bool ed_lin_supported(const ed_ham* h);
 int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out);
