@@ -257,6 +257,30 @@ def test_hv_nonfinite_input(ed, envs):
         assert np.all(np.isnan(y[cols]))
 
 
+@pytest.mark.parametrize('case', [
+    (0, 16, 1, 16, 0, 1.0, 1.0, 0.3, 0.3),
+    (1, 20, 4, 5, 0, 1.0, 1.0, 0.5, 0.5),
+    (1, 24, 4, 6, 1, 1.0, 0.7, 0.55, 0.55),
+])
+def test_hv_real_input(ed, envs, case):
+    """Real input (imaginary parts exactly zero): the fixed-point path keeps
+    real parts only.  Within 1e-14 * ||x||_2 of the oracle, imaginary output
+    exactly zero, and non-finite entries reach exactly the rows that gather
+    them (the allocation-free kernel, which always gathers (re, im)
+    pairs, is compared bit for bit in test_zz_no_alloc.py)."""
+    ltype, N, lx, ly, mag, J1, D1, J2, D2 = case
+    env, b, h, M = make_pair(ed, envs, ltype, N, lx, ly, mag, J1, D1, J2, D2)
+    x = oracle.start_vector(6, b.size).real.astype(np.complex128)
+    y = h.apply(x).cpu().numpy()
+    assert np.abs(y - M.apply(x)).max() <= 1e-14 * np.linalg.norm(x)
+    assert np.all(y.imag == 0.0)
+    x[7] = np.inf
+    y = h.apply(x).cpu().numpy()
+    cols = set(M.scipy()[:, 7].nonzero()[0]) | {7}
+    bad = set(np.nonzero(~np.isfinite(y.real))[0])
+    assert bad == cols
+
+
 def test_hv_edge_cases(ed, envs):
     # one-state sector, all-up: H is the 1x1 diagonal
     env, b, h, M = make_pair(ed, envs, 0, 8, 1, 8, 4, 1.0, 1.0, 0.0, 0.0)

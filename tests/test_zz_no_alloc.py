@@ -78,3 +78,25 @@ def test_noalloc_rejects_large_basis(setup):
     rc = lib.ed_ham_apply_noalloc(h.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()))
     assert rc == ed.capi.ED_EINVAL
     assert 'at most' in ed.capi.last_error()
+
+
+def test_noalloc_real_input_bit_identical(setup):
+    """A real input (imaginary parts exactly zero) takes ed_ham_apply through
+    the real-part gathers; the allocation-free kernel always gathers (re, im)
+    pairs.  Both sum the same exact integers and round once, so the results
+    must agree bit for bit."""
+    import torch
+    ed = setup
+    lib = ed.capi.lib()
+    env = ed.Environment(nspins=20)
+    b, h = _ham(ed, env, 20, 4, 5, 0)
+    gen = torch.Generator(device='cuda').manual_seed(99)
+    x = torch.complex(torch.rand(b.size, dtype=torch.float64, device='cuda', generator=gen) * 2 - 1,
+                      torch.zeros(b.size, dtype=torch.float64, device='cuda'))
+    y_ref = torch.empty_like(x)
+    y_new = torch.empty_like(x)
+    assert lib.ed_ham_apply(h.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y_ref.data_ptr())) == 0
+    rc = lib.ed_ham_apply_noalloc(h.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y_new.data_ptr()))
+    assert rc == 0, ed.capi.last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(y_new).view(torch.int64), torch.view_as_real(y_ref).view(torch.int64))
