@@ -220,7 +220,45 @@ def workload_config(wl):
                         'matrix-free complex128 H.v' % (wl, ltype, N, lx, ly, J1, J2, mag, nev, ncv or 'decide', tol),
             'nspins': N, 'lattice': ltype, 'lx': lx, 'ly': ly, 'J1': J1, 'J2': J2, 'Delta': 1.0, 'sz': mag,
             'nev': nev, 'ncv': ncv, 'eps_tol': tol, 'dim': math.comb(N, mag + N // 2), 'seed': 0,
-            'l2': 'inputs larger than L2 (each vector %.2f GB)' % (16 * math.comb(N, mag + N // 2) / 1e9)}
+            'l2': ('inputs larger than L2 (each vector %.2f GB)' if 16 * math.comb(N, mag + N // 2) > 129e6 else
+                   'inputs smaller than L2, not flushed (each vector %.4f GB): an outputs/parity case, not the '
+                   'headline workload') % (16 * math.comb(N, mag + N // 2) / 1e9)}
+
+
+def workload_outputs(ed, env, b, lat, wl, eps, evals):
+    """The measurements the C1 / C2 configurations ask for, from the last
+    solve (outside the timed region).
+    C1 (chain N=16): E0, <S_0.S_r> for every r, m^2_AF.
+    C2 (4x5 J1-J2): all N^2 <S_i.S_j> and the DSF weights
+    |<n|S^z_q|0>|^2 over the nev levels at q = (pi, pi) and (pi, 0), with
+    r_i = (i // ly, i % ly); ly = 5 is odd, so q_y = pi is off the lattice's
+    grid and the nearest grid value 4 pi / 5 is used (stated in the line)."""
+    import numpy as np
+    import torch
+    N = env.nspins
+    _, psi0, _ = ed.Solver.solution(eps, 0)
+    out = {'E': [float(e) for e in evals]}
+    t0 = time.perf_counter()
+    if wl == 'c1':
+        r = ed.SiSj(env, b).ExpectValPairs([(0, j) for j in range(N)], psi0)
+        out['S0_Sr'] = [float(np.real(v)) for v in r]
+        out['m2_af'] = float(np.real(ed.Phys.SquaredSubLattMagAF(env, b, ed.AF(lat), psi0)))
+    else:
+        C = ed.SiSj(env, b).AllPairs(psi0)
+        out['sisj_sum'] = float(np.real(C.sum()))
+        out['S0_S1'] = float(np.real(C[0, 1]))
+        n = len(evals)
+        V = torch.stack([ed.Solver.solution(eps, i)[1] for i in range(n)])
+        c = ed.Phys.dsf_coefficients(env, b, b, 0, psi0, V)
+        pos = ed.Phys.site_positions(lat)
+        lx, ly = lat.nspins_x, lat.nspins_y
+        q_grid = [(np.pi, 2 * np.pi * round(ly / 2 - 0.5) / ly), (np.pi, 0.0)]
+        out['dsf'] = {'q_requested': [[np.pi, np.pi], [np.pi, 0.0]], 'q_used': [list(q) for q in q_grid],
+                      'dE': [float(e - evals[0]) for e in evals],
+                      'weights': [[float(w) for w in ed.Phys.dsf_weights(c, pos, q)] for q in q_grid]}
+    torch.cuda.synchronize()
+    out['seconds'] = time.perf_counter() - t0
+    return out
 
 
 def run_disorder(args):
@@ -328,6 +366,8 @@ def run_hv_only(args):
     H.build_diag(env)
     H.build_off_diag(env)
     H.set_accumulation(args.acc)
+    if args.variant != 'auto':
+        H.set_hv_variant(args.variant)
     dim = b.size
     x = torch.empty(dim, dtype=torch.complex128, device='cuda')
     x.real.uniform_(-1, 1)
@@ -436,6 +476,7 @@ def run_ours(args):
                 'sum_check': float(np.real(C.sum())),  # <S_tot^2> = S(S+1) = 0 for a singlet ground state
                 'S0_S1': float(np.real(C[0, 1]))}
         del psi0
+    outputs = workload_outputs(ed, env, b, lat, wl, eps, evals) if wl in ('c1', 'c2') else None
     ed.Solver.SolverClean(eps)
     ms_step = ms / args.steps
     if ws > 1:
@@ -527,7 +568,7 @@ def run_ours(args):
                      'bytes_per_row': bytes_row, 'bytes_per_row_complex_input': bytes_row_complex,
                      'rows_per_launch': dim, 'avg_launch_ms': hv_ms,
                      'launches_timed': n_hv},
-        'hv_gbs': achieved, 'sisj_all_pairs': sisj,
+        'hv_gbs': achieved, 'sisj_all_pairs': sisj, 'outputs': outputs,
         'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'ortho_passes': st['ortho_passes'],
                    'eigenvalues': evals,
                    'rel_residuals': errs},
@@ -567,6 +608,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
+    ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
     ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, 'libedgb300.so')
 
 SOURCES = ['ed_capi.cu', 'ed_basis.cu', 'ed_hamiltonian.cu', 'ed_linalg.cu', 'ed_eps.cu', 'ed_measure.cu',
            'ed_batch.cu', 'ed_adjoint.cu', 'ed_hv_lin.cu',
-           'ed_spectrum.cu']
+           'ed_spectrum.cu', 'ed_hv_jit.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
          '--expt-relaxed-constexpr', '-I' + os.path.join(ROOT, 'include')]
@@ -40,18 +40,25 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def cuda_lib_dir(cc):
+    """The toolkit's library directory next to nvcc (libnvrtc for the
+    run-time specialised H.v is loaded from there)."""
+    return os.path.normpath(os.path.join(os.path.dirname(os.path.realpath(cc)), '..', 'lib64'))
+
+
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.h', '.cuh'))]
     headers.append(os.path.join(ROOT, 'include', 'ed_capi.h'))
     cc = nvcc()
+    defs = ['-DED_CUDA_LIB_DIR="%s"' % cuda_lib_dir(cc)]
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src.replace('.cu', '.o'))
         if force or _stale(o, [s] + headers):
-            jobs.append([cc] + ARCH + FLAGS + ['-c', s, '-o', o])
+            jobs.append([cc] + ARCH + FLAGS + defs + ['-c', s, '-o', o])
     if jobs:
         with concurrent.futures.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             res = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
@@ -63,7 +70,7 @@ def build(force=False, verbose=False):
     objs = [os.path.join(BUILD, s.replace('.cu', '.o')) for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + '.tmp%d' % os.getpid()
-        cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-cudart', 'static']
+        cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-cudart', 'static', '-ldl']
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

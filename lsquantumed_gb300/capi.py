@@ -75,6 +75,7 @@ SIGNATURES = {
     'ed_ham_diag_host': [vp, vp],
     'ed_ham_size': [vp, P(i64)],
     'ed_ham_hv_variant': [vp, i32, vp, ctypes.c_size_t],
+    'ed_ham_set_hv_variant': [vp, ctypes.c_char_p],
     'ed_eps_create': [vp, i32, i32, i32, P(vp)],
     'ed_eps_set_dimensions': [vp, i32, i32, i32],
     'ed_eps_set_tolerances': [vp, dbl, i32],

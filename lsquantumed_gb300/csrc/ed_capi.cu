@@ -515,6 +515,12 @@ int ed_ham_size(const ed_ham* h, int64_t* size) {
   return ED_OK;
 }
 
+int ed_ham_set_hv_variant(ed_ham* h, const char* name) {
+  if (!h || !name) return ed_fail(ED_EINVAL, "null argument");
+  if (!ed_lin_supported(h)) return ed_fail(ED_ENOTSUP, "this operator does not use the two-table H.v");
+  return ed_lin_set_variant(h, name);
+}
+
 int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len) {
   if (!h || !buf || len == 0) return ed_fail(ED_EINVAL, "null argument");
   const char* name = ed_lin_variant_name(h, dot);

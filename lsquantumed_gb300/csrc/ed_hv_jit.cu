@@ -1,0 +1,385 @@
+// Run-time specialised two-table H.v: the bond masks of one operator become
+// immediates of a kernel compiled for it with NVRTC (sm_103a cubin), so each
+// bond slot costs only its flip test, one table lookup and the gather (no
+// bond-word loads, no loop bookkeeping, all bonds of a row unrolled).  Same
+// arithmetic as k_hv_lin (exact int64 sums per coupling type, one rounding),
+// so the results are bit-identical; the autotuner in ed_hv_lin.cu times it
+// beside the static variants.  NVRTC is loaded with dlopen and the driver
+// API through cudaGetDriverEntryPointByVersion, so the library needs neither
+// at link time; where either is missing this variant is simply unavailable.
+#include "ed_internal.h"
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <cstdio>
+#include <cstdlib>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#ifndef ED_CUDA_LIB_DIR
+#define ED_CUDA_LIB_DIR "/usr/local/cuda/lib64"
+#endif
+
+namespace {
+
+struct Nvrtc {
+  bool ok = false;
+  nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*) = nullptr;
+  nvrtcResult (*compile)(nvrtcProgram, int, const char* const*) = nullptr;
+  nvrtcResult (*cubin_size)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*cubin)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*log_size)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*log)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*destroy)(nvrtcProgram*) = nullptr;
+};
+
+struct Driver {
+  bool ok = false;
+  CUresult (*load)(CUmodule*, const void*) = nullptr;
+  CUresult (*get)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
+                     void**, void**) = nullptr;
+  CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+};
+
+std::mutex g_mu;
+Nvrtc g_nvrtc;
+Driver g_drv;
+bool g_loaded = false;
+std::string g_why;
+
+template <typename F>
+bool sym(void* lib, const char* name, F& f) {
+  f = reinterpret_cast<F>(dlsym(lib, name));
+  return f != nullptr;
+}
+
+template <typename F>
+bool drv_sym(const char* name, F& f) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p) {
+    cudaGetLastError();
+    return false;
+  }
+  f = reinterpret_cast<F>(p);
+  return true;
+}
+
+void load_apis() {
+  if (g_loaded) return;
+  g_loaded = true;
+  const char* names[] = {ED_CUDA_LIB_DIR "/libnvrtc.so.13", ED_CUDA_LIB_DIR "/libnvrtc.so", "libnvrtc.so.13",
+                         "libnvrtc.so"};
+  void* lib = nullptr;
+  for (const char* n : names)
+    if ((lib = dlopen(n, RTLD_NOW | RTLD_LOCAL)) != nullptr) break;
+  if (!lib) {
+    g_why = "libnvrtc not found";
+    return;
+  }
+  Nvrtc& r = g_nvrtc;
+  r.ok = sym(lib, "nvrtcCreateProgram", r.create) && sym(lib, "nvrtcCompileProgram", r.compile) &&
+         sym(lib, "nvrtcGetCUBINSize", r.cubin_size) && sym(lib, "nvrtcGetCUBIN", r.cubin) &&
+         sym(lib, "nvrtcGetProgramLogSize", r.log_size) && sym(lib, "nvrtcGetProgramLog", r.log) &&
+         sym(lib, "nvrtcDestroyProgram", r.destroy);
+  Driver& d = g_drv;
+  d.ok = drv_sym("cuModuleLoadData", d.load) && drv_sym("cuModuleGetFunction", d.get) &&
+         drv_sym("cuLaunchKernel", d.launch) && drv_sym("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
+  if (!r.ok) g_why = "NVRTC symbols missing";
+  if (!d.ok) g_why = "driver entry points missing";
+}
+
+// Generated source.  The kernel names are fixed; one module per operator.
+const char* kPrelude = R"(
+typedef unsigned int u32;
+typedef long long i64;
+typedef unsigned long long u64;
+struct alignas(16) D2 { double x, y; };
+struct alignas(16) L2 { i64 x, y; };
+#define NAN_Q ((i64)0x8000000000000000ull)
+)";
+
+const char* kKernels = R"(
+template <bool CHECK, bool RX>
+__device__ __forceinline__ void gather(const L2* __restrict__ xq, u32 g, bool on, i64& ar, i64& ai, bool& bad) {
+  if (RX) {
+    const i64 q = on ? ((const i64*)xq)[g] : 0ll;
+    if (CHECK) bad |= q == NAN_Q;
+    ar += q;
+  } else {
+    L2 q;
+    if (on) q = xq[g]; else { q.x = 0; q.y = 0; }
+    if (CHECK) bad |= (q.x == NAN_Q) | (q.y == NAN_Q);
+    ar += q.x;
+    ai += q.y;
+  }
+}
+
+template <bool CHECK, bool RX, bool DOT>
+__device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
+                                     const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
+                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
+                                     double c0c, double c1c, double s1, double s2, double* dacc) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const u32 s = states[r];
+    const u32 c0 = s & LOWMASK, c1 = s >> W0;
+    const u32 rr = (u32)r;
+    const u32 rb0 = rr - (u32)t0s[c0];
+    const u32 rb1 = rr - t1[c1];
+    i64 a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    bool bad = false;
+    BONDS
+    const double d = diag[r];
+    const D2 xv = x[r];
+    const double s0r = (double)a0 * s1 * s2, s0i = (double)a1 * s1 * s2;
+    const double s1r = (double)a2 * s1 * s2, s1i = (double)a3 * s1 * s2;
+    double yr = fma(d, xv.x, fma(c0c, s0r, c1c * s1r));
+    double yi = fma(d, xv.y, fma(c0c, s0i, c1c * s1i));
+    if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
+    D2 o; o.x = yr; o.y = yi;
+    y[r] = o;
+    if (DOT) {
+      dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
+      dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
+      dacc[2] = fma(yr, yr, fma(yi, yi, dacc[2]));
+    }
+  }
+}
+
+template <bool DOT>
+__device__ __forceinline__ void body(const u32* __restrict__ states, const double* __restrict__ diag,
+                                     const D2* __restrict__ x, const L2* __restrict__ xq,
+                                     const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
+                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, double c0c,
+                                     double c1c, double* __restrict__ partial) {
+  extern __shared__ unsigned short t0s[];
+  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
+  __syncthreads();
+  const int e_unit = gmax_p[0] - 1022 - sbits;
+  const double s1 = __longlong_as_double((i64)(e_unit / 2 + 1023) << 52);
+  const double s2 = __longlong_as_double((i64)(e_unit - e_unit / 2 + 1023) << 52);
+  double dacc[3] = {0.0, 0.0, 0.0};
+  const bool rx = gmax_p[2] == 0;
+  if (gmax_p[1]) {
+    if (rx) rows<true, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    else rows<true, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+  } else {
+    if (rx) rows<false, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    else rows<false, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+  }
+  if (DOT) {
+    __shared__ double sh[3 * 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < 3; ++k) {
+      double a = dacc[k];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0) sh[k * 32 + wid] = a;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      for (int k = 0; k < 3; ++k) {
+        double a = lane < nw ? sh[k * 32 + lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) partial[k * gridDim.x + blockIdx.x] = a;
+      }
+    }
+  }
+}
+
+extern "C" __global__ void __launch_bounds__(256) k_hv_jit(const u32* states, const double* diag, const D2* x,
+    const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0, const u32* t1, double c0c,
+    double c1c, double* partial) {
+  body<false>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);
+}
+
+extern "C" __global__ void __launch_bounds__(256) k_hv_jit_dot(const u32* states, const double* diag, const D2* x,
+    const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0, const u32* t1, double c0c,
+    double c1c, double* partial) {
+  body<true>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);
+}
+)";
+
+struct JitModule {
+  bool ok = false;
+  CUfunction plain = nullptr, dot = nullptr;
+  int per_sm[2] = {1, 1};
+};
+
+std::map<std::tuple<int, uint64_t>, JitModule> g_modules;
+
+// On-disk cache of compiled modules (the compile takes seconds): directory
+// $ED_JIT_CACHE, else $XDG_CACHE_HOME/lsquantumed_gb300, else
+// $HOME/.cache/lsquantumed_gb300; file name = hash of the source and options.
+std::string cache_dir() {
+  if (const char* d = getenv("ED_JIT_CACHE")) return d;
+  if (const char* d = getenv("XDG_CACHE_HOME")) return std::string(d) + "/lsquantumed_gb300";
+  if (const char* d = getenv("HOME")) return std::string(d) + "/.cache/lsquantumed_gb300";
+  return "";
+}
+
+uint64_t fnv(const std::string& s) {
+  uint64_t z = 1469598103934665603ull;
+  for (unsigned char c : s) { z ^= c; z *= 1099511628211ull; }
+  return z;
+}
+
+bool cache_read(const std::string& path, std::vector<char>& out) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  out.resize(n > 0 ? (size_t)n : 0);
+  const bool ok = n > 0 && fread(out.data(), 1, (size_t)n, f) == (size_t)n;
+  fclose(f);
+  return ok;
+}
+
+void cache_write(const std::string& dir, const std::string& path, const std::vector<char>& data) {
+  if (dir.empty()) return;
+  std::string cur;
+  for (size_t i = 0; i <= dir.size(); ++i) {  // mkdir -p
+    if (i == dir.size() || dir[i] == '/') {
+      if (!cur.empty()) mkdir(cur.c_str(), 0755);
+    }
+    if (i < dir.size()) cur += dir[i];
+  }
+  const std::string tmp = path + ".tmp" + std::to_string((long)getpid());
+  FILE* f = fopen(tmp.c_str(), "wb");
+  if (!f) return;
+  const bool ok = fwrite(data.data(), 1, data.size(), f) == data.size();
+  fclose(f);
+  if (ok) rename(tmp.c_str(), path.c_str());
+  else remove(tmp.c_str());
+}
+
+std::string hex(uint32_t v) {
+  char b[16];
+  snprintf(b, sizeof(b), "0x%xu", v);
+  return b;
+}
+
+// One bond's code: class 0 (inside the low half), 1 (inside the high half),
+// 2 (across); type selects the accumulators (nn: a0/a1, nnn: a2/a3).
+std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
+  std::ostringstream o;
+  const char* ar = type ? "a2" : "a0";
+  const char* ai = type ? "a3" : "a1";
+  o << "{ ";
+  if (cls == 0) {
+    o << "const u32 t = c0 & " << hex(m0) << "; const bool on = (t != 0u) & (t != " << hex(m0)
+      << "); const u32 g = rb0 + (u32)t0s[c0 ^ " << hex(m0) << "]; ";
+  } else if (cls == 1) {
+    o << "const u32 t = c1 & " << hex(m1) << "; const bool on = (t != 0u) & (t != " << hex(m1)
+      << "); const u32 g = rb1 + t1[c1 ^ " << hex(m1) << "]; ";
+  } else {
+    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = (u32)t0s[c0 ^ "
+      << hex(m0) << "] + t1[c1 ^ " << hex(m1) << "]; ";
+  }
+  o << "gather<CHECK, RX>(xq, g, on, " << ar << ", " << ai << ", bad); }\n    ";
+  return o.str();
+}
+
+}  // namespace
+
+// Signature of the operator's bond words (the same hash the autotuner keys on).
+int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, bool dot, int sbits, int* nblk_out,
+                  const unsigned long long* words, const int* seg, int w0) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  JitModule* mod = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    load_apis();
+    if (!g_nvrtc.ok || !g_drv.ok) return ed_fail(ED_ENOTSUP, "run-time compilation unavailable: " + g_why);
+    auto key = std::make_tuple(ctx->device, signature);
+    auto it = g_modules.find(key);
+    if (it == g_modules.end()) {
+      JitModule jm;
+      std::ostringstream bonds;
+      for (int cls = 0; cls < 3; ++cls)
+        for (int t = 0; t < 2; ++t)
+          for (int q = seg[cls * 2 + t]; q < seg[cls * 2 + t + 1]; ++q)
+            bonds << bond_code(cls, t, (uint32_t)words[q], (uint32_t)(words[q] >> 32));
+      std::string kern = kKernels;
+      const size_t at = kern.find("BONDS");
+      kern.replace(at, 5, bonds.str());
+      std::string src = std::string(kPrelude) + "#define W0 " + std::to_string(w0) + "\n#define LOWMASK " +
+                        hex((1u << w0) - 1u) + "\n" + kern;
+      const char* opts[] = {"-arch=sm_103a", "-std=c++17", "-default-device"};
+      const std::string dir = cache_dir();
+      char name[40];
+      snprintf(name, sizeof(name), "/hv_%016llx.cubin",
+               (unsigned long long)fnv(src + opts[0] + opts[1] + opts[2]));
+      const std::string path = dir.empty() ? std::string() : dir + name;
+      std::vector<char> cubin;
+      if (path.empty() || !cache_read(path, cubin)) {
+        nvrtcProgram prog;
+        if (g_nvrtc.create(&prog, src.c_str(), "ed_hv_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+          return ed_fail(ED_ENOTSUP, "nvrtcCreateProgram failed");
+        nvrtcResult cr = g_nvrtc.compile(prog, 3, opts);
+        if (cr != NVRTC_SUCCESS) {
+          size_t n = 0;
+          g_nvrtc.log_size(prog, &n);
+          std::string log(n, '\0');
+          if (n) g_nvrtc.log(prog, &log[0]);
+          g_nvrtc.destroy(&prog);
+          g_modules[key] = jm;  // remember the failure: do not retry every call
+          return ed_fail(ED_ENOTSUP, "run-time compilation failed: " + log.substr(0, 400));
+        }
+        size_t n = 0;
+        g_nvrtc.cubin_size(prog, &n);
+        cubin.resize(n);
+        g_nvrtc.cubin(prog, cubin.data());
+        g_nvrtc.destroy(&prog);
+        cache_write(dir, path, cubin);
+      }
+      CUmodule m = nullptr;
+      if (g_drv.load(&m, cubin.data()) != CUDA_SUCCESS || g_drv.get(&jm.plain, m, "k_hv_jit") != CUDA_SUCCESS ||
+          g_drv.get(&jm.dot, m, "k_hv_jit_dot") != CUDA_SUCCESS) {
+        g_modules[key] = jm;
+        return ed_fail(ED_ENOTSUP, "loading the compiled H.v module failed");
+      }
+      const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
+      for (int k = 0; k < 2; ++k) {
+        int ps = 0;
+        if (g_drv.occupancy(&ps, k ? jm.dot : jm.plain, 256, smem) != CUDA_SUCCESS || ps < 1) ps = 1;
+        jm.per_sm[k] = ps;
+      }
+      jm.ok = true;
+      it = g_modules.emplace(key, jm).first;
+    }
+    if (!it->second.ok) return ed_fail(ED_ENOTSUP, "run-time compiled H.v unavailable for this operator");
+    mod = &it->second;
+  }
+  const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
+  int64_t g = (b->dim + 255) / 256;
+  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[dot ? 1 : 0]));
+  const int nblk = (int)g;
+  if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
+  const uint32_t* states = b->d_states;
+  const double* diag = h->d_diag;
+  const longlong2* xq = h->d_xq;
+  const int* gmax = h->d_gmax;
+  int64_t dim = b->dim;
+  const uint16_t* t0 = b->d_lin_t0;
+  const uint32_t* t1 = b->d_lin_t1;
+  double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
+  double* partial = dot ? ctx->d_red : nullptr;
+  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  CUresult r = g_drv.launch(dot ? mod->dot : mod->plain, (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
+                            (CUstream)ctx->stream, args, nullptr);
+  if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");
+  ctx->kernels++;
+  if (nblk_out) *nblk_out = nblk;
+  return ED_OK;
+}

@@ -20,6 +20,9 @@
 #include "ed_device.cuh"
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #define LIN_MAX_W0 14
@@ -292,10 +295,16 @@ static const LinVariant kLinVariants[] = {
 };
 static const int kNumLinVariants = (int)(sizeof(kLinVariants) / sizeof(kLinVariants[0]));
 
+// Variant kNumLinVariants is the run-time specialised kernel (ed_hv_jit.cu).
+static const int kJitVariant = kNumLinVariants;
+static uint64_t lin_signature(const ed_ham* h);
+
 static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, int sbits, int* nblk_out) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const ed_lin* L = h->lin;
+  if (v == kJitVariant)
+    return ed_jit_launch(h, lin_signature(h), x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg, L->segs.w0);
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
@@ -312,6 +321,23 @@ static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, 
   return ED_OK;
 }
 
+// Autotuner choices, shared by every operator of the same structure (device,
+// sector, bond words): a second Hamiltonian of a lattice does not time again.
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, uint64_t, int>, int> g_tune;
+
+static uint64_t lin_signature(const ed_ham* h) {
+  uint64_t z = 1469598103934665603ull;  // FNV-1a over the segment table and words
+  const LinSegs& sg = h->lin->segs;
+  auto mix = [&](uint64_t v) {
+    for (int k = 0; k < 8; ++k) { z ^= (v >> (8 * k)) & 0xFF; z *= 1099511628211ull; }
+  };
+  mix((uint64_t)sg.w0);
+  for (int i = 0; i < 7; ++i) mix((uint64_t)sg.seg[i]);
+  for (int i = 0; i < sg.seg[6]; ++i) mix(sg.word[i]);
+  return z;
+}
+
 // First H.v (and first fused H.v + dot) of a large operator: time each
 // variant (two launches after one warm-up, CUDA events on the context's
 // stream) and keep the fastest.  The timing synchronises the stream once.
@@ -321,13 +347,26 @@ static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool
   int& chosen = L->variant[dot ? 1 : 0];
   chosen = 0;
   if (h->basis->dim < (int64_t)1 << 20) return ED_OK;
+  const auto key = std::make_tuple(ctx->device, h->basis->nspins, h->basis->nup, lin_signature(h), dot ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      chosen = it->second;
+      return ED_OK;
+    }
+  }
   cudaEvent_t e0, e1;
   ED_CUDA(cudaEventCreate(&e0));
   ED_CUDA(cudaEventCreate(&e1));
   float best = 0.0f;
   int rc = ED_OK;
-  for (int v = 0; v < kNumLinVariants && rc == ED_OK; ++v) {
+  for (int v = 0; v <= kJitVariant && rc == ED_OK; ++v) {
     rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
+    if (v == kJitVariant && rc == ED_ENOTSUP) {  // no run-time compiler here: keep the static choice
+      rc = ED_OK;
+      break;
+    }
     if (rc == ED_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
     for (int it = 0; it < 2 && rc == ED_OK; ++it) rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
     if (rc == ED_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
@@ -341,6 +380,10 @@ static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc == ED_OK) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = chosen;
+  }
   return rc;
 }
 
@@ -356,9 +399,26 @@ int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nbl
   return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out);
 }
 
+// Force a launch variant by name ("auto" re-enables the autotuner); for tests
+// and tuning.  Returns ED_EINVAL for an unknown name.
+int ed_lin_set_variant(ed_ham* h, const char* name) {
+  ED_TRY(lin_prepare(h));
+  int v = -2;
+  if (strcmp(name, "auto") == 0) v = -1;
+  else if (strcmp(name, "jit") == 0) v = kJitVariant;
+  else
+    for (int i = 0; i < kNumLinVariants; ++i)
+      if (strcmp(name, kLinVariants[i].name) == 0) v = i;
+  if (v == -2) return ed_fail(ED_EINVAL, std::string("unknown H.v variant ") + name);
+  h->lin->variant[0] = h->lin->variant[1] = v;
+  return ED_OK;
+}
+
 const char* ed_lin_variant_name(const ed_ham* h, int dot) {
   const int which = dot ? 1 : 0;
-  return (h->lin && h->lin->variant[which] >= 0) ? kLinVariants[h->lin->variant[which]].name : "";
+  if (!h->lin || h->lin->variant[which] < 0) return "";
+  if (h->lin->variant[which] == kJitVariant) return "jit";
+  return kLinVariants[h->lin->variant[which]].name;
 }
 
 void ed_lin_invalidate(ed_lin* L) {

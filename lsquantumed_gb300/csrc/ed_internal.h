@@ -166,8 +166,13 @@ int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, doub
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
 bool ed_lin_supported(const ed_ham* h);
 int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out);
+// The two-table H.v compiled at run time for one operator's bond words
+// (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
+int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, bool dot, int sbits, int* nblk_out,
+                  const unsigned long long* words, const int* seg, int w0);
 void ed_lin_invalidate(ed_lin* L);
 const char* ed_lin_variant_name(const ed_ham* h, int dot);
+int ed_lin_set_variant(ed_ham* h, const char* name);
 void ed_lin_free(ed_lin* L);
 int ed_launch_csr_build(ed_ham* h);
 int ed_launch_csr_spmv(ed_ham* h, const double2* x, double2* y);

@@ -331,6 +331,10 @@ class Hamiltonian:
         k = {'exact': capi.ED_ACC_EXACT, 'fixed64': capi.ED_ACC_FIXED64, 'fp64': capi.ED_ACC_FP64}[kind]
         call('ed_ham_set_accumulation', self._h, k)
 
+    def set_hv_variant(self, name):
+        """Force the matrix-free H.v launch variant ('auto' = autotuner)."""
+        call('ed_ham_set_hv_variant', self._h, name.encode())
+
     def hv_variant(self, dot=False):
         """Launch variant of the matrix-free H.v chosen by the autotuner."""
         buf = ctypes.create_string_buffer(64)
