@@ -164,9 +164,9 @@ int ed_ham_size(const ed_ham* h, int64_t* size);
  * reference; for reports. */
 int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len);
 /* Force the matrix-free H.v launch variant: "u4-b6", "u4-b4", "u8-b4",
- * "u8-b1" (static kernels: unroll depth and register budget), "jit" (kernel
- * compiled at run time for this operator's bonds) or "auto" (autotuner, the
- * default).  All variants give bit-identical results.  ED_ENOTSUP for
+ * "u8-b1" (static kernels: unroll depth and register budget), "jit" /
+ * "jit-b4" (kernel compiled at run time for this operator's bonds, without a
+ * register limit / with 4 blocks per SM) or "auto" (autotuner, the default).  All variants give bit-identical results.  ED_ENOTSUP for
  * operators that do not use the two-table kernel (per-bond, CSR, FP64 or
  * 128-bit accumulation).  No counterpart in the reference. */
 int ed_ham_set_hv_variant(ed_ham* h, const char* name);

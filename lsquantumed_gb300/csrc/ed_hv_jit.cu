@@ -195,23 +195,23 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   }
 }
 
-extern "C" __global__ void __launch_bounds__(256) k_hv_jit(const u32* states, const double* diag, const D2* x,
-    const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0, const u32* t1, double c0c,
-    double c1c, double* partial) {
-  body<false>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);
-}
-
-extern "C" __global__ void __launch_bounds__(256) k_hv_jit_dot(const u32* states, const double* diag, const D2* x,
-    const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0, const u32* t1, double c0c,
-    double c1c, double* partial) {
-  body<true>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);
-}
+#define JIT_KERNEL(NAME, DOT, MINB)                                                                       \
+  extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
+      const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
+      const u32* t1, double c0c, double c1c, double* partial) {                                             \
+    body<DOT>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);                       \
+  }
+// register budgets: all loads of a row in flight (2 blocks of 256 per SM), or 4 blocks per SM
+JIT_KERNEL(k_hv_jit_b2, false, 1)
+JIT_KERNEL(k_hv_jit_dot_b2, true, 1)
+JIT_KERNEL(k_hv_jit_b4, false, 4)
+JIT_KERNEL(k_hv_jit_dot_b4, true, 4)
 )";
 
 struct JitModule {
   bool ok = false;
-  CUfunction plain = nullptr, dot = nullptr;
-  int per_sm[2] = {1, 1};
+  CUfunction fn[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [budget][dot]
+  int per_sm[2][2] = {{1, 1}, {1, 1}};
 };
 
 std::map<std::tuple<int, uint64_t>, JitModule> g_modules;
@@ -292,8 +292,8 @@ std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
 }  // namespace
 
 // Signature of the operator's bond words (the same hash the autotuner keys on).
-int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, bool dot, int sbits, int* nblk_out,
-                  const unsigned long long* words, const int* seg, int w0) {
+int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const double2* x, double2* y, bool dot, int sbits,
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   JitModule* mod = nullptr;
@@ -344,17 +344,21 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, b
         cache_write(dir, path, cubin);
       }
       CUmodule m = nullptr;
-      if (g_drv.load(&m, cubin.data()) != CUDA_SUCCESS || g_drv.get(&jm.plain, m, "k_hv_jit") != CUDA_SUCCESS ||
-          g_drv.get(&jm.dot, m, "k_hv_jit_dot") != CUDA_SUCCESS) {
+      const char* names[2][2] = {{"k_hv_jit_b2", "k_hv_jit_dot_b2"}, {"k_hv_jit_b4", "k_hv_jit_dot_b4"}};
+      bool got = g_drv.load(&m, cubin.data()) == CUDA_SUCCESS;
+      for (int bg = 0; bg < 2 && got; ++bg)
+        for (int k = 0; k < 2 && got; ++k) got = g_drv.get(&jm.fn[bg][k], m, names[bg][k]) == CUDA_SUCCESS;
+      if (!got) {
         g_modules[key] = jm;
         return ed_fail(ED_ENOTSUP, "loading the compiled H.v module failed");
       }
       const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
-      for (int k = 0; k < 2; ++k) {
-        int ps = 0;
-        if (g_drv.occupancy(&ps, k ? jm.dot : jm.plain, 256, smem) != CUDA_SUCCESS || ps < 1) ps = 1;
-        jm.per_sm[k] = ps;
-      }
+      for (int bg = 0; bg < 2; ++bg)
+        for (int k = 0; k < 2; ++k) {
+          int ps = 0;
+          if (g_drv.occupancy(&ps, jm.fn[bg][k], 256, smem) != CUDA_SUCCESS || ps < 1) ps = 1;
+          jm.per_sm[bg][k] = ps;
+        }
       jm.ok = true;
       it = g_modules.emplace(key, jm).first;
     }
@@ -363,7 +367,8 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, b
   }
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
   int64_t g = (b->dim + 255) / 256;
-  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[dot ? 1 : 0]));
+  const int bg = budget ? 1 : 0;
+  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[bg][dot ? 1 : 0]));
   const int nblk = (int)g;
   if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
   const uint32_t* states = b->d_states;
@@ -376,7 +381,7 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, b
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
   void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
-  CUresult r = g_drv.launch(dot ? mod->dot : mod->plain, (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
+  CUresult r = g_drv.launch(mod->fn[bg][dot ? 1 : 0], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);
   if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");
   ctx->kernels++;

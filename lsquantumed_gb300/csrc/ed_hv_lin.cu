@@ -295,16 +295,19 @@ static const LinVariant kLinVariants[] = {
 };
 static const int kNumLinVariants = (int)(sizeof(kLinVariants) / sizeof(kLinVariants[0]));
 
-// Variant kNumLinVariants is the run-time specialised kernel (ed_hv_jit.cu).
+// Variants kNumLinVariants and +1 are the run-time specialised kernel
+// (ed_hv_jit.cu) with two register budgets.
 static const int kJitVariant = kNumLinVariants;
+static const int kNumAllVariants = kNumLinVariants + 2;
 static uint64_t lin_signature(const ed_ham* h);
 
 static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, int sbits, int* nblk_out) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const ed_lin* L = h->lin;
-  if (v == kJitVariant)
-    return ed_jit_launch(h, lin_signature(h), x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg, L->segs.w0);
+  if (v >= kJitVariant)
+    return ed_jit_launch(h, lin_signature(h), v - kJitVariant, x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg,
+                         L->segs.w0);
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
@@ -361,9 +364,9 @@ static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool
   ED_CUDA(cudaEventCreate(&e1));
   float best = 0.0f;
   int rc = ED_OK;
-  for (int v = 0; v <= kJitVariant && rc == ED_OK; ++v) {
+  for (int v = 0; v < kNumAllVariants && rc == ED_OK; ++v) {
     rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
-    if (v == kJitVariant && rc == ED_ENOTSUP) {  // no run-time compiler here: keep the static choice
+    if (v >= kJitVariant && rc == ED_ENOTSUP) {  // no run-time compiler here: keep the static choice
       rc = ED_OK;
       break;
     }
@@ -406,6 +409,7 @@ int ed_lin_set_variant(ed_ham* h, const char* name) {
   int v = -2;
   if (strcmp(name, "auto") == 0) v = -1;
   else if (strcmp(name, "jit") == 0) v = kJitVariant;
+  else if (strcmp(name, "jit-b4") == 0) v = kJitVariant + 1;
   else
     for (int i = 0; i < kNumLinVariants; ++i)
       if (strcmp(name, kLinVariants[i].name) == 0) v = i;
@@ -418,6 +422,7 @@ const char* ed_lin_variant_name(const ed_ham* h, int dot) {
   const int which = dot ? 1 : 0;
   if (!h->lin || h->lin->variant[which] < 0) return "";
   if (h->lin->variant[which] == kJitVariant) return "jit";
+  if (h->lin->variant[which] == kJitVariant + 1) return "jit-b4";
   return kLinVariants[h->lin->variant[which]].name;
 }
 

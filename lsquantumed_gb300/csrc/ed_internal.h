@@ -168,8 +168,9 @@ bool ed_lin_supported(const ed_ham* h);
 int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out);
 // The two-table H.v compiled at run time for one operator's bond words
 // (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
-int ed_jit_launch(ed_ham* h, uint64_t signature, const double2* x, double2* y, bool dot, int sbits, int* nblk_out,
-                  const unsigned long long* words, const int* seg, int w0);
+// budget 0: no register limit (2 blocks of 256 per SM); 1: 4 blocks per SM.
+int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const double2* x, double2* y, bool dot, int sbits,
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0);
 void ed_lin_invalidate(ed_lin* L);
 const char* ed_lin_variant_name(const ed_ham* h, int dot);
 int ed_lin_set_variant(ed_ham* h, const char* name);

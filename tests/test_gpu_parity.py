@@ -291,7 +291,7 @@ def test_hv_variants_bit_identical(ed, envs):
     xc = oracle.start_vector(8, b.size)
     xr = xc.real.astype(np.complex128)
     ref = {}
-    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit'):
+    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4'):
         h.set_hv_variant(v)
         for name, x in (('complex', xc), ('real', xr)):
             y = h.apply(x).cpu().numpy()
