@@ -341,12 +341,16 @@ def run_disorder(args):
     return 0
 
 
-def hv_bytes_per_row(kb, real_gathers):
-    """Algorithmic bytes per row of one matrix-free H.v: x_s (16) + the
-    gathered x_s' (16 per entry, or 8 when the input is real and the
-    fixed-point copy holds only real parts) + y_s (16) + state (4) + diagonal
-    (8)."""
-    return 16 + (8 if real_gathers else 16) * kb + 16 + 4 + 8
+def hv_bytes_per_row(kb, mode):
+    """Algorithmic bytes per row of one matrix-free H.v: x_s + the gathered
+    x_s' (k-bar entries) + y_s + state (4) + diagonal (8).
+    mode 'complex': complex128 vectors, 16-byte gathers;
+    'real_gathers': complex128 vectors whose imaginary parts are zero, the
+    fixed-point copy holds real parts (8-byte gathers);
+    'real_storage': vectors stored as their real parts (the real-mode solve):
+    8-byte x_s, gathers and y_s."""
+    vec, gat = {'complex': (16, 16), 'real_gathers': (16, 8), 'real_storage': (8, 8)}[mode]
+    return vec + gat * kb + vec + 4 + 8
 
 
 def run_hv_only(args):
@@ -392,7 +396,7 @@ def run_hv_only(args):
     env.profile(False)
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
     real_mode = args.real_input and args.acc == 'fixed64'
-    bytes_row = hv_bytes_per_row(kbar(N, b.nspins_up, pairs), real_mode)
+    bytes_row = hv_bytes_per_row(kbar(N, b.nspins_up, pairs), 'real_gathers' if real_mode else 'complex')
     ms = ms_hv / max(n_hv, 1)
     peak, _ = measured_peaks()
     gbs = dim * bytes_row / (ms * 1e-3) / 1e9
@@ -487,10 +491,10 @@ def run_ours(args):
     # roofline of the dominant kernel (H.v): algorithmic bytes per launch
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
     kb = kbar(N, b.nspins_up, pairs)
-    # the solve starts from a real vector (H real symmetric): every H.v input
-    # is real and gathers 8-byte real parts of the fixed-point copy
-    bytes_row = hv_bytes_per_row(kb, True)
-    bytes_row_complex = hv_bytes_per_row(kb, False)
+    # the solve starts from a real vector (H real symmetric): the basis is
+    # stored as its real parts and every H.v reads and writes 8-byte entries
+    bytes_row = hv_bytes_per_row(kb, 'real_storage')
+    bytes_row_complex = hv_bytes_per_row(kb, 'complex')
     hv_ms = ms_hv / max(n_hv, 1)
     achieved = dim * bytes_row / (hv_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()

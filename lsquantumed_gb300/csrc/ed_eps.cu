@@ -34,6 +34,13 @@ struct ed_eps {
   double2* w = nullptr;
   std::vector<double2*> col;          // current basis columns (after solve: Ritz vectors)
   double2* v0 = nullptr;              // user initial vector (EPSSetInitialSpace)
+  // real storage (real mode with the two-table H.v): columns hold only the
+  // real parts of the basis, whose imaginary parts are exactly zero
+  bool real_storage = false;
+  double* pool_r = nullptr;
+  double* w_r = nullptr;
+  std::vector<double*> col_r;
+  double2* xbuf = nullptr;            // complex128 staging of a real column for host copies
 };
 
 void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, std::vector<double>& Y) {
@@ -89,9 +96,17 @@ void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, st
 static void eps_free(ed_eps* e) {
   if (e->pool) cudaFree(e->pool);
   if (e->w) cudaFree(e->w);
+  if (e->pool_r) cudaFree(e->pool_r);
+  if (e->w_r) cudaFree(e->w_r);
+  if (e->xbuf) cudaFree(e->xbuf);
   e->pool = nullptr;
   e->w = nullptr;
+  e->pool_r = nullptr;
+  e->w_r = nullptr;
+  e->xbuf = nullptr;
   e->col.clear();
+  e->col_r.clear();
+  e->real_storage = false;
   e->pool_cols = 0;
 }
 
@@ -178,6 +193,176 @@ static int orthogonalize(ed_eps* e, int j, std::vector<double2>& h, double* nw, 
   return ED_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Real storage.  With a real start vector and H real symmetric the whole
+// Krylov-Schur run has exactly zero imaginary parts (real mode, above); the
+// basis then keeps only its real parts, which halves its memory and the
+// traffic of every projection, update and restart.  The steps are those of
+// orthogonalize_lanczos / eps_solve_impl; only the storage differs.
+// ---------------------------------------------------------------------------
+static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, double a, double y2,
+                                   std::vector<double>& h, double* nw, double* norig) {
+  ed_ctx* ctx = e->h->ctx;
+  const int64_t n = e->h->basis->dim;
+  std::vector<const double*> cols(e->col_r.begin(), e->col_r.begin() + j + 1);
+  h.assign(j + 1, 0.0);
+  *norig = std::sqrt(y2);
+  const bool three_term = j > k && j > 0;
+  std::vector<double> c(j + 1);
+  double w2 = 0.0, n2 = 0.0;
+  ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
+                       beta_prev, c.data(), &w2));
+  double n0 = std::sqrt(w2);
+  h[j] += a;
+  if (three_term) h[j - 1] += beta_prev;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1)
+      ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
+    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2));
+    for (int i = 0; i <= j; ++i) h[i] += c[i];
+    *nw = std::sqrt(n2);
+    e->ortho_passes++;
+    if (*nw >= 0.7071067811865476 * n0) break;
+    n0 = *nw;
+  }
+  return ED_OK;
+}
+
+static int orthogonalize_r(ed_eps* e, int j, double* nw) {
+  ed_ctx* ctx = e->h->ctx;
+  const int64_t n = e->h->basis->dim;
+  std::vector<const double*> cols(e->col_r.begin(), e->col_r.begin() + j + 1);
+  std::vector<double> c(j + 1);
+  double w2 = 0.0, n2 = 0.0;
+  ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), &w2));
+  double n0 = std::sqrt(w2);
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1)
+      ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
+    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2));
+    *nw = std::sqrt(n2);
+    if (*nw >= 0.7071067811865476 * n0) break;
+    n0 = *nw;
+  }
+  return ED_OK;
+}
+
+static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol, int max_it) {
+  ed_ham* H = e->h;
+  ed_ctx* ctx = H->ctx;
+  const int64_t n = H->basis->dim;
+  e->pool_cols = 2 * m + 1;
+  if (cudaMalloc(&e->pool_r, sizeof(double) * (size_t)n * e->pool_cols) != cudaSuccess ||
+      cudaMalloc(&e->w_r, sizeof(double) * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    eps_free(e);
+    return ed_fail(ED_ENOMEM, "Krylov basis does not fit in device memory");
+  }
+  e->real_storage = true;
+  e->real_coeffs = true;
+  std::vector<double*> freelist;
+  e->col_r.assign(m + 1, nullptr);
+  for (int i = 0; i < e->pool_cols; ++i) {
+    double* p = e->pool_r + (size_t)i * n;
+    if (i <= m) e->col_r[i] = p; else freelist.push_back(p);
+  }
+  std::vector<double> alpha(m + 1, 0.0), beta(m + 1, 0.0), arrow(m + 1, 0.0);
+  if (e->v0) ED_TRY(ed_complex_to_real(ctx, e->v0, e->col_r[0], n));
+  else ED_TRY(ed_start_vector_r(ctx, e->seed, n, e->col_r[0]));
+  {
+    double v2 = 0.0;
+    ED_TRY(ed_multidot_r(ctx, nullptr, 0, e->col_r[0], n, nullptr, 0.0, nullptr, 0.0, nullptr, &v2));
+    ED_TRY(ed_scale_copy_r(ctx, e->col_r[0], e->col_r[0], 1.0 / std::sqrt(v2), n));
+  }
+  uint64_t rseed = e->seed + 0x51ED2701ull;
+  e->nhv = 0;
+  e->ortho_passes = 0;
+  int k = 0, nconv = 0, its = 0;
+  std::vector<double> theta, Y, h;
+  bool done = false;
+  while (!done) {
+    ++its;
+    for (int j = k; j < m; ++j) {
+      double2 pre_a;
+      double pre_y2 = 0.0;
+      ED_TRY(ed_launch_hv_dot_any(H, e->col_r[j], e->w_r, true, &pre_a, &pre_y2));
+      e->nhv++;
+      double nw, norig;
+      ED_TRY(orthogonalize_lanczos_r(e, j, k, j > 0 ? beta[j - 1] : 0.0, pre_a.x, pre_y2, h, &nw, &norig));
+      alpha[j] = h[j];
+      if (nw <= 1e-13 * norig) {
+        // invariant subspace: continue with a (real) random vector orthogonal to V
+        beta[j] = 0.0;
+        if (j + 1 < m) {
+          ED_TRY(ed_start_vector_r(ctx, rseed++, n, e->w_r));
+          double nw2;
+          ED_TRY(orthogonalize_r(e, j, &nw2));
+          ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw2, n));
+        } else {
+          ED_CUDA(cudaMemsetAsync(e->col_r[j + 1], 0, sizeof(double) * (size_t)n, ctx->stream));
+        }
+      } else {
+        ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw, n));
+        beta[j] = nw;
+      }
+    }
+    std::vector<double> T((size_t)m * m, 0.0);
+    for (int i = 0; i < k; ++i) {
+      T[(size_t)i * m + i] = alpha[i];
+      T[(size_t)i * m + k] = T[(size_t)k * m + i] = arrow[i];
+    }
+    for (int j = k; j < m; ++j) {
+      T[(size_t)j * m + j] = alpha[j];
+      if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = beta[j];
+    }
+    ed_jacobi_eig(m, T, theta, Y);
+    const double bm = beta[m - 1];
+    nconv = 0;
+    for (int i = 0; i < m; ++i) {
+      double res = std::fabs(bm * Y[(size_t)(m - 1) * m + i]);
+      double rel = res / std::max(std::fabs(theta[i]), 1e-300);
+      if (rel < tol) ++nconv; else break;
+    }
+    if (nconv >= nev || its >= max_it) done = true;
+    int l;
+    if (done) l = std::min(m, std::max(nconv, nev));
+    else {
+      l = nconv + std::max(1, (m - nconv) / 2);
+      if (l > m - 1) l = m - 1;
+    }
+    std::vector<double*> outc(freelist.begin(), freelist.begin() + l);
+    std::vector<const double*> inc(e->col_r.begin(), e->col_r.begin() + m);
+    ED_TRY(ed_restart_combine_r(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n));
+    std::vector<double*> newcol(m + 1, nullptr);
+    for (int c = 0; c < l; ++c) newcol[c] = outc[c];
+    newcol[l] = e->col_r[m];
+    std::vector<double*> newfree(freelist.begin() + l, freelist.end());
+    for (int c = 0; c < m; ++c) newfree.push_back(e->col_r[c]);
+    for (int c = l + 1; c <= m; ++c) { newcol[c] = newfree.back(); newfree.pop_back(); }
+    e->col_r.swap(newcol);
+    freelist.swap(newfree);
+    if (done) {
+      e->nrep = l;
+      e->nconv = std::min(nconv, l);
+      e->evals.assign(theta.begin(), theta.begin() + l);
+      e->errs.assign(l, 0.0);
+      for (int c = 0; c < l; ++c) {
+        ED_TRY(ed_launch_hv_r(H, e->col_r[c], e->w_r));
+        double r2, x2;
+        ED_TRY(ed_residual_norm2_r(ctx, e->w_r, e->col_r[c], theta[c], n, &r2, &x2));
+        e->errs[c] = std::sqrt(r2) / std::max(std::fabs(theta[c]) * std::sqrt(x2), 1e-300);
+      }
+      break;
+    }
+    for (int i = 0; i < l; ++i) { alpha[i] = theta[i]; arrow[i] = bm * Y[(size_t)(m - 1) * m + i]; }
+    k = l;
+  }
+  e->its = its;
+  e->solved = true;
+  *nconv_out = e->nconv;
+  return ED_OK;
+}
+
 static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   ed_ham* H = e->h;
   ed_ctx* ctx = H->ctx;
@@ -191,6 +376,11 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
   const int max_it = e->max_it > 0 ? e->max_it : (int)std::max<int64_t>(100, 2 * n / std::max(ncv, 1));
   const int m = ncv;
   eps_free(e);
+  {
+    bool real_start = true;
+    if (e->v0) ED_TRY(ed_is_real(ctx, e->v0, n, &real_start));
+    if (real_start && ed_lin_supported(H)) return eps_solve_real(e, nconv_out, m, nev, tol, max_it);
+  }
   e->pool_cols = 2 * m + 1;
   if (cudaMalloc(&e->pool, sizeof(double2) * (size_t)n * e->pool_cols) != cudaSuccess ||
       cudaMalloc(&e->w, sizeof(double2) * (size_t)n) != cudaSuccess) {
@@ -388,7 +578,10 @@ int ed_eps_get_eigenpair(ed_eps* e, int i, double* eig, double* rel_err, ed_cplx
   if (i < 0 || i >= e->nrep) return ed_fail(ED_EINVAL, "eigenpair index out of range");
   if (eig) *eig = e->evals[i];
   if (rel_err) *rel_err = e->errs[i];
-  if (vec_dev) ED_TRY(ed_copy(e->h->ctx, e->col[i], (double2*)vec_dev, e->h->basis->dim));
+  if (vec_dev) {
+    if (e->real_storage) ED_TRY(ed_real_to_complex(e->h->ctx, e->col_r[i], (double2*)vec_dev, e->h->basis->dim));
+    else ED_TRY(ed_copy(e->h->ctx, e->col[i], (double2*)vec_dev, e->h->basis->dim));
+  }
   return ED_OK;
 }
 
@@ -397,8 +590,17 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host) {
   if (!e->solved) return ed_fail(ED_ESTATE, "eigenvector requested before solve");
   if (i < 0 || i >= e->nrep) return ed_fail(ED_EINVAL, "eigenpair index out of range");
   ed_ctx* ctx = e->h->ctx;
-  ED_CUDA(cudaMemcpyAsync(vec_host, e->col[i], sizeof(double2) * (size_t)e->h->basis->dim, cudaMemcpyDeviceToHost,
-                          ctx->stream));
+  const int64_t n = e->h->basis->dim;
+  const double2* src = e->real_storage ? nullptr : e->col[i];
+  if (e->real_storage) {
+    if (!e->xbuf && cudaMalloc(&e->xbuf, sizeof(double2) * (size_t)n) != cudaSuccess) {
+      cudaGetLastError();
+      return ed_fail(ED_ENOMEM, "no room to stage the eigenvector");
+    }
+    ED_TRY(ed_real_to_complex(ctx, e->col_r[i], e->xbuf, n));
+    src = e->xbuf;
+  }
+  ED_CUDA(cudaMemcpyAsync(vec_host, src, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   return ED_OK;
 }

@@ -625,6 +625,66 @@ static int max_type_count(const BondSet& bs) {
   return c[0] > c[1] ? c[0] : c[1];
 }
 
+// The same two passes for a real input stored as double[dim] (real-mode
+// solves): the imaginary-nonzero flag stays 0, only real parts are written.
+__global__ void __launch_bounds__(256) k_max_exponent_r(const double* __restrict__ x, int64_t dim,
+                                                        int* __restrict__ gmax, int* __restrict__ nonfinite) {
+  int m = 0, nf = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const int e = (int)(((unsigned long long)__double_as_longlong(x[r]) >> 52) & 0x7FF);
+    nf |= e == 0x7FF;
+    m = max(m, e == 0x7FF ? 0 : e);
+  }
+  m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+  nf = (int)__reduce_or_sync(0xffffffffu, (unsigned)nf);
+  if ((threadIdx.x & 31) == 0) {
+    if (m > 0) atomicMax(gmax, m);
+    if (nf) atomicOr(nonfinite, 1);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_quantize64_r(const double* __restrict__ x, int64_t dim,
+                                                      const int* __restrict__ gmax_p, int sbits,
+                                                      long long* __restrict__ xq) {
+  const int emax = *gmax_p;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x[r]);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    long long m = 0;
+    if (e == 0x7FF) {
+      m = (long long)0x8000000000000000ull;  // non-finite sentinel
+    } else if (e != 0) {
+      const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+      const int sh = e - emax + sbits - 53;
+      unsigned long long a;
+      if (sh >= 0) a = mant << sh;
+      else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);  // round half up in magnitude
+      else a = 0;
+      m = (long long)a;
+      if (bits >> 63) m = -m;
+    }
+    xq[r] = m;
+  }
+}
+
+int ed_fx64_quantize_r(ed_ham* h, const double* x, int* sbits) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  ED_TRY(ensure_fixed_buffers(h));
+  int head = 0;
+  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
+  *sbits = 62 - head;
+  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 3 * sizeof(int), ctx->stream));
+  const int g = grid_cap(ctx, b->dim, 256, 8);
+  k_max_exponent_r<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
+  ED_CHECK_LAUNCH(ctx);
+  k_quantize64_r<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, *sbits, (long long*)h->d_xq);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
@@ -674,7 +734,7 @@ static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
 static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
   if (h->mode == ED_HAM_CSR && h->d_rowptr) return ed_launch_csr_spmv(h, x, y);
   const bool pb = h->bs.per_bond != 0;
-  if (ed_lin_supported(h)) return ed_launch_hv_lin(h, x, y, false, nullptr);
+  if (ed_lin_supported(h)) return ed_launch_hv_lin(h, x, y, false, nullptr, false);
   if (!pb && h->hv_kernel == 2) {
     switch (h->basis->rt.K) {
       case 1: return launch_hv_fx64_k<1>(h, x, y);
@@ -699,6 +759,11 @@ static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
   }
 }
 
+int ed_launch_hv_r(ed_ham* h, const double* x, double* y) {
+  if (!ed_lin_supported(h)) return ed_fail(ED_ENOTSUP, "real-storage H.v needs the two-table kernel");
+  return ed_launch_hv_lin(h, x, y, false, nullptr, true);
+}
+
 int ed_launch_hv(ed_ham* h, const double2* x, double2* y) {
   ed_ctx* ctx = h->ctx;
   if (!ctx->profiling) return launch_hv_dispatch(h, x, y);
@@ -714,6 +779,10 @@ int ed_launch_hv(ed_ham* h, const double2* x, double2* y) {
 }
 
 int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, double* y2) {
+  return ed_launch_hv_dot_any(h, x, y, false, dot, y2);
+}
+
+int ed_launch_hv_dot_any(ed_ham* h, const void* x, void* y, bool rio, double2* dot, double* y2) {
   ed_ctx* ctx = h->ctx;
   if (!ed_lin_supported(h)) return ED_ENOTSUP;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -723,7 +792,7 @@ int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, doub
     ED_CUDA(cudaEventRecord(e0, ctx->stream));
   }
   int nblk = 0;
-  ED_TRY(ed_launch_hv_lin(h, x, y, true, &nblk));
+  ED_TRY(ed_launch_hv_lin(h, x, y, true, &nblk, rio));
   if (ctx->profiling) {
     ED_CUDA(cudaEventRecord(e1, ctx->stream));
     ctx->prof_events.push_back(e0);

@@ -127,7 +127,7 @@ template <bool CHECK, bool RX, bool DOT>
 __device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                      i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
-                                     double c0c, double c1c, double s1, double s2, double* dacc) {
+                                     double c0c, double c1c, double s1, double s2, double* dacc, bool rio) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const u32 s = states[r];
@@ -139,14 +139,15 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     bool bad = false;
     BONDS
     const double d = diag[r];
-    const D2 xv = x[r];
+    D2 xv;
+    if (rio) { xv.x = ((const double*)x)[r]; xv.y = 0.0; } else xv = x[r];
     const double s0r = (double)a0 * s1 * s2, s0i = (double)a1 * s1 * s2;
     const double s1r = (double)a2 * s1 * s2, s1i = (double)a3 * s1 * s2;
     double yr = fma(d, xv.x, fma(c0c, s0r, c1c * s1r));
     double yi = fma(d, xv.y, fma(c0c, s0i, c1c * s1i));
     if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
-    D2 o; o.x = yr; o.y = yi;
-    y[r] = o;
+    if (rio) ((double*)y)[r] = yr;
+    else { D2 o; o.x = yr; o.y = yi; y[r] = o; }
     if (DOT) {
       dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
       dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
@@ -160,8 +161,9 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
                                      const D2* __restrict__ x, const L2* __restrict__ xq,
                                      const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
                                      const unsigned short* __restrict__ t0, const u32* __restrict__ t1, double c0c,
-                                     double c1c, double* __restrict__ partial) {
+                                     double c1c, double* __restrict__ partial, int rio_flag) {
   extern __shared__ unsigned short t0s[];
+  const bool rio = rio_flag != 0;
   for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
   const int e_unit = gmax_p[0] - 1022 - sbits;
@@ -170,11 +172,11 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   double dacc[3] = {0.0, 0.0, 0.0};
   const bool rx = gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) rows<true, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
-    else rows<true, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    if (rx) rows<true, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
+    else rows<true, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
   } else {
-    if (rx) rows<false, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
-    else rows<false, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    if (rx) rows<false, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
+    else rows<false, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -198,8 +200,8 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
 #define JIT_KERNEL(NAME, DOT, MINB)                                                                       \
   extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
-      const u32* t1, double c0c, double c1c, double* partial) {                                             \
-    body<DOT>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);                       \
+      const u32* t1, double c0c, double c1c, double* partial, int rio) {                                    \
+    body<DOT>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial, rio);                  \
   }
 // register budgets: all loads of a row in flight (2 blocks of 256 per SM), or 4 blocks per SM
 JIT_KERNEL(k_hv_jit_b2, false, 1)
@@ -292,8 +294,8 @@ std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
 }  // namespace
 
 // Signature of the operator's bond words (the same hash the autotuner keys on).
-int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const double2* x, double2* y, bool dot, int sbits,
-                  int* nblk_out, const unsigned long long* words, const int* seg, int w0) {
+int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   JitModule* mod = nullptr;
@@ -380,7 +382,8 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const double2* x, d
   const uint32_t* t1 = b->d_lin_t1;
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
-  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  int rio_flag = rio ? 1 : 0;
+  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial, &rio_flag};
   CUresult r = g_drv.launch(mod->fn[bg][dot ? 1 : 0], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);
   if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");

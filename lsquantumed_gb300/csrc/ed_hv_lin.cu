@@ -198,12 +198,13 @@ __device__ __forceinline__ void lin_cross(const LinSegs& sg, int b0, int b1, uin
   }
 }
 
+// rio: x and y are real storage (double[dim]); the input is then real (RX).
 template <bool CHECK, bool DOT, int U, bool RX>
 __device__ __forceinline__ void lin_rows(const uint32_t* __restrict__ states, const double* __restrict__ diag,
                                          const double2* __restrict__ x, const longlong2* __restrict__ xq,
                                          double2* __restrict__ y, int64_t dim, const uint16_t* __restrict__ t0s,
                                          const uint32_t* __restrict__ t1, const LinSegs& sg, double c0c, double c1c,
-                                         double s1, double s2, double (&dacc)[3]) {
+                                         double s1, double s2, double (&dacc)[3], bool rio) {
   const uint32_t low = (1u << sg.w0) - 1u;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
@@ -221,13 +222,14 @@ __device__ __forceinline__ void lin_rows(const uint32_t* __restrict__ states, co
     lin_cross<CHECK, U, RX>(sg, sg.seg[4], sg.seg[5], c0, c1, t0s, t1, xq, a[0], a[1], bad);
     lin_cross<CHECK, U, RX>(sg, sg.seg[5], sg.seg[6], c0, c1, t0s, t1, xq, a[2], a[3], bad);
     const double d = diag[r];
-    const double2 xv = x[r];
+    const double2 xv = rio ? make_double2(((const double*)x)[r], 0.0) : x[r];
     const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
     const double s1r = (double)a[2] * s1 * s2, s1i = (double)a[3] * s1 * s2;
     double yr = fma(d, xv.x, fma(c0c, s0r, c1c * s1r));
     double yi = fma(d, xv.y, fma(c0c, s0i, c1c * s1i));
     if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
-    y[r] = make_double2(yr, yi);
+    if (rio) ((double*)y)[r] = yr;
+    else y[r] = make_double2(yr, yi);
     if (DOT) {
       dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
       dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
@@ -245,8 +247,9 @@ __global__ void __launch_bounds__(256, MINB) k_hv_lin(const uint32_t* __restrict
                                                 const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
                                                 int64_t dim, const uint16_t* __restrict__ t0,
                                                 const uint32_t* __restrict__ t1, const LinSegs sg, double c0c,
-                                                double c1c, double* __restrict__ partial) {
+                                                double c1c, double* __restrict__ partial, int rio_flag) {
   extern __shared__ uint16_t t0s[];
+  const bool rio = rio_flag != 0;
   const int n0 = 1 << sg.w0;
   for (int i = threadIdx.x; i < n0; i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
@@ -258,11 +261,11 @@ __global__ void __launch_bounds__(256, MINB) k_hv_lin(const uint32_t* __restrict
   // gmax_p[2] == 0: x is real and xq holds only real parts
   const bool rx = gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) lin_rows<true, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
-    else lin_rows<true, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+    if (rx) lin_rows<true, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc, rio);
+    else lin_rows<true, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc, rio);
   } else {
-    if (rx) lin_rows<false, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
-    else lin_rows<false, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc);
+    if (rx) lin_rows<false, DOT, U, true>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc, rio);
+    else lin_rows<false, DOT, U, false>(states, diag, x, xq, y, dim, t0s, t1, sg, c0c, c1c, s1, s2, dacc, rio);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -282,7 +285,7 @@ bool ed_lin_supported(const ed_ham* h) {
 // Launch variants (same results: the integer sums are exact, so the unroll
 // depth and register budget change only the speed).
 typedef void (*LinKernel)(const uint32_t*, const double*, const double2*, const longlong2*, const int*, int, double2*,
-                          int64_t, const uint16_t*, const uint32_t*, const LinSegs, double, double, double*);
+                          int64_t, const uint16_t*, const uint32_t*, const LinSegs, double, double, double*, int);
 struct LinVariant {
   LinKernel plain, dot;
   const char* name;
@@ -301,13 +304,13 @@ static const int kJitVariant = kNumLinVariants;
 static const int kNumAllVariants = kNumLinVariants + 2;
 static uint64_t lin_signature(const ed_ham* h);
 
-static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, int sbits, int* nblk_out) {
+static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sbits, int* nblk_out, bool rio) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const ed_lin* L = h->lin;
   if (v >= kJitVariant)
     return ed_jit_launch(h, lin_signature(h), v - kJitVariant, x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg,
-                         L->segs.w0);
+                         L->segs.w0, rio);
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
@@ -317,8 +320,9 @@ static int lin_launch(ed_ham* h, int v, const double2* x, double2* y, bool dot, 
   g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * per_sm));
   const int nblk = (int)g;
   if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
-  k<<<nblk, 256, smem, ctx->stream>>>(b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, b->d_lin_t0, b->d_lin_t1,
-                                      L->segs, h->bs.chalf[0], h->bs.chalf[1], dot ? ctx->d_red : nullptr);
+  k<<<nblk, 256, smem, ctx->stream>>>(b->d_states, h->d_diag, (const double2*)x, h->d_xq, h->d_gmax, sbits,
+                                      (double2*)y, b->dim, b->d_lin_t0, b->d_lin_t1, L->segs, h->bs.chalf[0],
+                                      h->bs.chalf[1], dot ? ctx->d_red : nullptr, rio ? 1 : 0);
   ED_CHECK_LAUNCH(ctx);
   if (nblk_out) *nblk_out = nblk;
   return ED_OK;
@@ -344,7 +348,7 @@ static uint64_t lin_signature(const ed_ham* h) {
 // First H.v (and first fused H.v + dot) of a large operator: time each
 // variant (two launches after one warm-up, CUDA events on the context's
 // stream) and keep the fastest.  The timing synchronises the stream once.
-static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool dot) {
+static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, bool rio) {
   ed_lin* L = h->lin;
   ed_ctx* ctx = h->ctx;
   int& chosen = L->variant[dot ? 1 : 0];
@@ -365,13 +369,13 @@ static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool
   float best = 0.0f;
   int rc = ED_OK;
   for (int v = 0; v < kNumAllVariants && rc == ED_OK; ++v) {
-    rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
+    rc = lin_launch(h, v, x, y, dot, sbits, nullptr, rio);
     if (v >= kJitVariant && rc == ED_ENOTSUP) {  // no run-time compiler here: keep the static choice
       rc = ED_OK;
       break;
     }
     if (rc == ED_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
-    for (int it = 0; it < 2 && rc == ED_OK; ++it) rc = lin_launch(h, v, x, y, dot, sbits, nullptr);
+    for (int it = 0; it < 2 && rc == ED_OK; ++it) rc = lin_launch(h, v, x, y, dot, sbits, nullptr, rio);
     if (rc == ED_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = ed_fail(ED_ECUDA, "event record");
     float ms = 0.0f;
     if (rc == ED_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
@@ -393,13 +397,14 @@ static int lin_autotune(ed_ham* h, const double2* x, double2* y, int sbits, bool
 // y = H x through the two-table kernel.  With dot set, the kernel also leaves
 // per-block partials of Re/Im x^H y and ||y||^2 in ctx->d_red (3 items of
 // *nblk_out blocks each, for ed_finish_reduce).
-int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out) {
+int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio) {
   ED_TRY(lin_prepare(h));
   int sbits = 0;
-  ED_TRY(ed_fx64_quantize(h, x, &sbits));
+  if (rio) ED_TRY(ed_fx64_quantize_r(h, (const double*)x, &sbits));
+  else ED_TRY(ed_fx64_quantize(h, (const double2*)x, &sbits));
   const int which = dot ? 1 : 0;
-  if (h->lin->variant[which] < 0) ED_TRY(lin_autotune(h, x, y, sbits, dot));
-  return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out);
+  if (h->lin->variant[which] < 0) ED_TRY(lin_autotune(h, x, y, sbits, dot, rio));
+  return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out, rio);
 }
 
 // Force a launch variant by name ("auto" re-enables the autotuner); for tests

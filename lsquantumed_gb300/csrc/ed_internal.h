@@ -160,17 +160,23 @@ int ed_launch_hv(ed_ham* h, const double2* x, double2* y);
 // y = H x and, in the same pass over the rows, dot = x^H y and *y2 = ||y||^2.
 // Returns ED_ENOTSUP (nothing launched) where the operator has no fused form.
 int ed_launch_hv_dot(ed_ham* h, const double2* x, double2* y, double2* dot, double* y2);
+// Same for x, y complex (rio false) or real storage double[dim] (rio true).
+int ed_launch_hv_dot_any(ed_ham* h, const void* x, void* y, bool rio, double2* dot, double* y2);
+// y = H x with real storage (two-table kernel only).
+int ed_launch_hv_r(ed_ham* h, const double* x, double* y);
 // Fixed-point copy of x into h->d_xq: largest exponent, non-finite flag and
 // imaginary-nonzero flag in h->d_gmax[0..2]; when every imaginary part is
 // zero only the real parts are stored (int64[dim]).  *sbits = the scale.
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
+int ed_fx64_quantize_r(ed_ham* h, const double* x, int* sbits);
 bool ed_lin_supported(const ed_ham* h);
-int ed_launch_hv_lin(ed_ham* h, const double2* x, double2* y, bool dot, int* nblk_out);
+// rio: x and y are real storage (double[dim]) instead of complex128.
+int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio);
 // The two-table H.v compiled at run time for one operator's bond words
 // (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
 // budget 0: no register limit (2 blocks of 256 per SM); 1: 4 blocks per SM.
-int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const double2* x, double2* y, bool dot, int sbits,
-                  int* nblk_out, const unsigned long long* words, const int* seg, int w0);
+int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio);
 void ed_lin_invalidate(ed_lin* L);
 const char* ed_lin_variant_name(const ed_ham* h, int dot);
 int ed_lin_set_variant(ed_ham* h, const char* name);
@@ -206,6 +212,19 @@ int ed_restart_combine(ed_ctx* ctx, const double2* const* cols, int m, const dou
 int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double theta, int64_t n, double* r2_host,
                       double* x2_host);
 int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);
+// Real storage (real-mode solves keep only the real parts of the basis).
+int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
+                  const double* vjm1, double b, double* h_host, double* wnorm2_host);
+int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
+                double* wnorm2_host);
+int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);
+int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
+                         double* const* out, int64_t n);
+int ed_residual_norm2_r(ed_ctx* ctx, const double* hx, const double* x, double theta, int64_t n, double* r2_host,
+                        double* x2_host);
+int ed_start_vector_r(ed_ctx* ctx, uint64_t seed, int64_t n, double* v);
+int ed_real_to_complex(ed_ctx* ctx, const double* src, double2* dst, int64_t n);
+int ed_complex_to_real(ed_ctx* ctx, const double2* src, double* dst, int64_t n);
 
 // measurements
 int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const int32_t* pairs_host, int64_t np,

@@ -429,3 +429,266 @@ int ed_is_real(ed_ctx* ctx, const double2* v, int64_t n, bool* real) {
   *real = h_any == 0;
   return ED_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Real storage.  A Krylov basis grown by a real symmetric H from a real start
+// vector has exactly zero imaginary parts; the real-mode solver stores only
+// the real parts (double[n] per column).  These kernels are the complex ones
+// above restricted to those real parts: the products they skip are the
+// exact zeros, so every value equals what the complex kernels give.
+// ---------------------------------------------------------------------------
+#define ED_GROUP_R 16
+
+struct ColPtrsR {
+  const double* p[128];
+};
+
+static ColPtrsR make_cols_r(const double* const* cols, int nv) {
+  ColPtrsR c;
+  for (int i = 0; i < 128; ++i) c.p[i] = nullptr;
+  for (int i = 0; i < nv && i < 128; ++i) c.p[i] = cols[i];
+  return c;
+}
+
+// partial[item * nblk + blk]: items v0..v0+ng-1 = V_i^T w; item v0+ng = ||w||^2
+// (with_norm).  LOCAL: first w <- w - a vj - b vjm1 (vjm1 may be null),
+// written back.
+template <int G, bool LOCAL>
+__global__ void __launch_bounds__(ED_RED_THREADS) k_multidot_r(const ColPtrsR cp, int v0, int ng, double* __restrict__ w,
+                                                               int64_t n, const double* __restrict__ vj, double a,
+                                                               const double* __restrict__ vjm1, double b, int with_norm,
+                                                               double* __restrict__ partial, int nblk) {
+  double acc[G + 1];
+#pragma unroll
+  for (int k = 0; k <= G; ++k) acc[k] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    double wv = w[r];
+    if (LOCAL) {
+      wv = fma(-a, vj[r], wv);
+      if (vjm1) wv = fma(-b, vjm1[r], wv);
+      w[r] = wv;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (g < ng) acc[g] = fma(cp.p[v0 + g][r], wv, acc[g]);
+    if (with_norm) acc[G] = fma(wv, wv, acc[G]);
+  }
+  __shared__ double sh[(G + 1) * 32];
+  ed_block_reduce<G + 1>(acc, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (g < ng) partial[(size_t)(v0 + g) * nblk + blockIdx.x] = acc[g];
+    if (with_norm) partial[(size_t)(v0 + ng) * nblk + blockIdx.x] = acc[G];
+  }
+}
+
+// h_host[i] = V_i^T w (i < nv), *wnorm2_host = ||w||^2 (after the local step
+// when vj is given: w <- w - a vj - b vjm1 first, in the same pass as the
+// first group of dots).
+int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
+                  const double* vjm1, double b, double* h_host, double* wnorm2_host) {
+  if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  const int nblk = red_blocks(ctx, n);
+  const int items = nv + 1;
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items));
+  ColPtrsR cp = make_cols_r(cols, nv);
+  const int ngroups = std::max(1, (nv + ED_GROUP_R - 1) / ED_GROUP_R);
+  for (int gidx = 0; gidx < ngroups; ++gidx) {
+    const int v0 = gidx * ED_GROUP_R;
+    const int ng = std::max(0, std::min(ED_GROUP_R, nv - v0));
+    const int last = gidx == ngroups - 1;
+    if (gidx == 0 && vj)
+      k_multidot_r<ED_GROUP_R, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, vj, a, vjm1, b, last,
+                                                                              ctx->d_red, nblk);
+    else
+      k_multidot_r<ED_GROUP_R, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, nullptr, 0.0, nullptr,
+                                                                               0.0, last, ctx->d_red, nblk);
+    ED_CHECK_LAUNCH(ctx);
+  }
+  std::vector<double> out(items);
+  ED_TRY(ed_finish_reduce(ctx, items, nblk, out.data()));
+  for (int i = 0; i < nv; ++i) h_host[i] = out[i];
+  if (wnorm2_host) *wnorm2_host = out[nv];
+  return ED_OK;
+}
+
+// w <- w - sum_i V_i h_i; partial ||w||^2.  Two rows per thread, columns
+// unrolled by four.
+__global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, int nv, const double* __restrict__ h,
+                                                             double* __restrict__ w, int64_t n,
+                                                             double* __restrict__ partial) {
+  __shared__ double sh_h[128];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) sh_h[i] = h[i];
+  __syncthreads();
+  double acc[1] = {0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < n; r0 += 2 * stride) {
+    const int64_t r1 = r0 + stride;
+    const bool has1 = r1 < n;
+    double w0 = w[r0];
+    double w1 = has1 ? w[r1] : 0.0;
+#pragma unroll 4
+    for (int i = 0; i < nv; ++i) {
+      const double* col = cp.p[i];
+      const double c = sh_h[i];
+      w0 = fma(-col[r0], c, w0);
+      if (has1) w1 = fma(-col[r1], c, w1);
+    }
+    w[r0] = w0;
+    acc[0] = fma(w0, w0, acc[0]);
+    if (has1) {
+      w[r1] = w1;
+      acc[0] = fma(w1, w1, acc[0]);
+    }
+  }
+  __shared__ double shr[32];
+  ed_block_reduce<1>(acc, shr);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
+}
+
+int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
+                double* wnorm2_host) {
+  if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  const int nblk = red_blocks(ctx, n);
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)nblk + 4 + 128));
+  double* h_dev = ctx->d_red + nblk + 2;
+  ED_CUDA(cudaMemcpyAsync(h_dev, h_host, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
+  ColPtrsR cp = make_cols_r(cols, nv);
+  k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red);
+  ED_CHECK_LAUNCH(ctx);
+  double out;
+  ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));
+  if (wnorm2_host) *wnorm2_host = out;
+  return ED_OK;
+}
+
+__global__ void k_scale_copy_r(const double* __restrict__ src, double* __restrict__ dst, double s, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) dst[r] = src[r] * s;
+}
+
+int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n) {
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
+  k_scale_copy_r<<<g, 256, 0, ctx->stream>>>(src, dst, s, n);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+// out_c = sum_i V_i * Y[i*ldY + c], c in [c0, c0+nc), nc <= 8.
+__global__ void __launch_bounds__(256) k_restart_r(const ColPtrsR cp, int m, const double* __restrict__ Y, int ldY,
+                                                   int c0, int nc, const ColPtrs outp, int64_t n) {
+  extern __shared__ double shY[];  // m x 8
+  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) {
+    int i = k / 8, c = k % 8;
+    shY[k] = (c < nc) ? Y[(size_t)i * ldY + c0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    double ar[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) ar[c] = 0.0;
+    for (int i = 0; i < m; ++i) {
+      const double v = cp.p[i][r];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) ar[c] = fma(v, shY[i * 8 + c], ar[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < nc) ((double*)outp.p[c0 + c])[r] = ar[c];
+  }
+}
+
+int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
+                         double* const* out, int64_t n) {
+  if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  ColPtrsR cp = make_cols_r(cols, m);
+  ColPtrs op;
+  for (int i = 0; i < 128; ++i) op.p[i] = nullptr;
+  for (int i = 0; i < l && i < 128; ++i) op.p[i] = (const double2*)out[i];
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)m * ldY + 16));
+  double* dY = ctx->d_red;
+  ED_CUDA(cudaMemcpyAsync(dY, Y, sizeof(double) * (size_t)m * ldY, cudaMemcpyHostToDevice, ctx->stream));
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 4));
+  size_t smem = sizeof(double) * (size_t)m * 8;
+  for (int c0 = 0; c0 < l; c0 += 8) {
+    int nc = std::min(8, l - c0);
+    k_restart_r<<<g, 256, smem, ctx->stream>>>(cp, m, dY, ldY, c0, nc, op, n);
+    ED_CHECK_LAUNCH(ctx);
+  }
+  return ED_OK;
+}
+
+__global__ void __launch_bounds__(ED_RED_THREADS) k_residual_r(const double* __restrict__ hx, const double* __restrict__ x,
+                                                               double theta, int64_t n, double* __restrict__ partial,
+                                                               int nblk) {
+  double acc[2] = {0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const double d = fma(-theta, x[r], hx[r]);
+    acc[0] = fma(d, d, acc[0]);
+    acc[1] = fma(x[r], x[r], acc[1]);
+  }
+  __shared__ double sh[64];
+  ed_block_reduce<2>(acc, sh);
+  if (threadIdx.x == 0) { partial[blockIdx.x] = acc[0]; partial[nblk + blockIdx.x] = acc[1]; }
+}
+
+int ed_residual_norm2_r(ed_ctx* ctx, const double* hx, const double* x, double theta, int64_t n, double* r2_host,
+                        double* x2_host) {
+  const int nblk = red_blocks(ctx, n);
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)2 * nblk + 2));
+  k_residual_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(hx, x, theta, n, ctx->d_red, nblk);
+  ED_CHECK_LAUNCH(ctx);
+  double out[2];
+  ED_TRY(ed_finish_reduce(ctx, 2, nblk, out));
+  *r2_host = out[0];
+  *x2_host = out[1];
+  return ED_OK;
+}
+
+// Real parts of the seeded start vector (the same values k_start_vector
+// writes into the real parts).
+__global__ void k_start_vector_r(uint64_t seed, int64_t n, double* __restrict__ v) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const uint64_t base = seed * 0xD1B54A32D192ED03ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t h1 = ed_splitmix64(base + 2 * (uint64_t)i);
+    const double u1 = (double)(h1 >> 11) * (1.0 / 9007199254740992.0);
+    v[i] = 2.0 * u1 - 1.0;
+  }
+}
+
+int ed_start_vector_r(ed_ctx* ctx, uint64_t seed, int64_t n, double* v) {
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
+  k_start_vector_r<<<g, 256, 0, ctx->stream>>>(seed, n, v);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+__global__ void k_real_to_complex(const double* __restrict__ src, double2* __restrict__ dst, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    dst[i] = make_double2(src[i], 0.0);
+}
+
+__global__ void k_complex_to_real(const double2* __restrict__ src, double* __restrict__ dst, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i].x;
+}
+
+int ed_real_to_complex(ed_ctx* ctx, const double* src, double2* dst, int64_t n) {
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
+  k_real_to_complex<<<g, 256, 0, ctx->stream>>>(src, dst, n);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+int ed_complex_to_real(ed_ctx* ctx, const double2* src, double* dst, int64_t n) {
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
+  k_complex_to_real<<<g, 256, 0, ctx->stream>>>(src, dst, n);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}

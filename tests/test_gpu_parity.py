@@ -361,6 +361,34 @@ def solve(ed, env, h, nev, tol=1e-12, ncv=None):
     return eps, nconv, np.array(evals), np.array(errs)
 
 
+def test_real_storage_matches_complex_path(ed, envs):
+    """The seeded (real) start vector runs the real-storage solver; a complex
+    start vector runs the complex path.  Same eigenvalues (1e-10 relative),
+    residuals within tol, and the real-storage eigenvectors come back as
+    complex128 with exactly zero imaginary parts."""
+    hi = oracle.rd_hi(4, 16, -1.0, 1.0)  # fields lift the lattice degeneracies
+    env, b, h, M = make_pair(ed, envs, 0, 16, 1, 16, 0, 1.0, 1.0, 0.3, 0.3,
+                             ('build_diag', 'build_off_diag', 'build_disorder'), hi)
+    eps, nconv, ev_r, err_r = solve(ed, env, h, 4, tol=1e-11, ncv=16)
+    ev_r, err_r = ev_r[:4], err_r[:4]
+    vecs = [ed.Solver.solution(eps, i)[1].cpu().numpy() for i in range(4)]
+    host = ed.Solver.solution_host(eps, 0)
+    ed.Solver.SolverClean(eps)
+    for v in vecs:
+        assert np.all(v.imag == 0.0)
+    assert np.array_equal(host.view(np.uint64), vecs[0].view(np.uint64))
+    eps = ed.Solver.SolverInit(h, 4, 16)
+    ed.Solver.EPSSetTolerances(eps, 1e-11)
+    eps.set_initial_vector(oracle.start_vector(3, b.size))
+    ed.Solver.solve(env, eps)
+    ev_c = [ed.Solver.eigenvalue(eps, i)[0] for i in range(4)]
+    ed.Solver.SolverClean(eps)
+    assert np.allclose(ev_r, ev_c, rtol=1e-10, atol=0), (ev_r, ev_c)
+    w = np.linalg.eigvalsh(M.dense())
+    assert np.allclose(ev_r, w[:4], rtol=1e-10, atol=0)
+    assert max(err_r) <= 1e-11
+
+
 def test_golden_eigenvalues(ed, envs, golden):
     for rec in golden['solver']:
         env, b, h, M = make_pair(ed, envs, rec['ltype'], rec['N'], rec['lx'], rec['ly'], rec['mag'], rec['J1'],
