@@ -27,7 +27,7 @@ struct ed_batch {
   int64_t nhv = 0;
   std::vector<double> evals, errs;  // [B][nrep]
   std::vector<int> nconv;           // [B]
-  double2* d_vecs = nullptr;        // [nrep][dim][B] saved Ritz vectors
+  double* d_vecs = nullptr;         // [nrep][dim][B] saved Ritz vectors (real parts)
   double* d_red = nullptr;
   size_t red_cap = 0;
   double* h_red = nullptr;
@@ -110,6 +110,42 @@ __global__ void k_batch_quantize(const double2* __restrict__ x, int64_t n, const
   }
 }
 
+// The same two passes for the real-storage block of the batched solve.
+__global__ void k_batch_maxexp_r(const double* __restrict__ x, int64_t n, int* __restrict__ gmax) {
+  int m = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int e = (int)(((unsigned long long)__double_as_longlong(x[r]) >> 52) & 0x7FF);
+    m = max(m, e == 0x7FF ? 0 : e);
+  }
+  m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(gmax, m);
+}
+
+__global__ void k_batch_quantize_r(const double* __restrict__ x, int64_t n, const int* __restrict__ gmax_p, int sbits,
+                                   long long* __restrict__ xq) {
+  const int emax = *gmax_p;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x[r]);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    long long m = 0;
+    if (e == 0x7FF) {
+      m = (long long)0x8000000000000000ull;
+    } else if (e != 0) {
+      const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+      const int sh = e - emax + sbits - 53;
+      unsigned long long a;
+      if (sh >= 0) a = mant << sh;
+      else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);
+      else a = 0;
+      m = (long long)a;
+      if (bits >> 63) m = -m;
+    }
+    xq[r] = m;
+  }
+}
+
 // Batched H.v over a [dim][B] block.  A CTA takes a tile of BH_ROWS rows:
 // first its threads resolve every (row, bond) pair of the tile at once (the
 // antiparallel test and the two-table rank of the flipped state, written to
@@ -126,12 +162,19 @@ struct BatchBonds {
   uint8_t type[ED_MAX_BONDS];
 };
 
+// RS: real storage (x, y double[dim][B], fixed-point copy int64[dim][B]);
+// else complex128 blocks with (re, im) fixed-point pairs.
+template <bool RS>
 __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ states, const double* __restrict__ diag,
-                                                  const double2* __restrict__ x, const longlong2* __restrict__ xq,
-                                                  const int* __restrict__ gmax_p, int sbits, double2* __restrict__ y,
+                                                  const void* __restrict__ xv_, const void* __restrict__ xq_,
+                                                  const int* __restrict__ gmax_p, int sbits, void* __restrict__ y_,
                                                   int64_t dim, int B, const uint16_t* __restrict__ t0,
                                                   const uint32_t* __restrict__ t1, int w0, const BatchBonds bb,
                                                   double c0, double c1) {
+  const double2* __restrict__ x = (const double2*)xv_;
+  const longlong2* __restrict__ xq = (const longlong2*)xq_;
+  const double* __restrict__ xr = (const double*)xv_;
+  const long long* __restrict__ xqr = (const long long*)xq_;
   extern __shared__ uint32_t sm[];
   uint16_t* t0s = (uint16_t*)sm;                       // 2^w0 entries
   uint32_t* tgt = sm + ((1 << w0) + 1) / 2;            // [BH_ROWS][nb]
@@ -164,80 +207,88 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
         long long a[4] = {0, 0, 0, 0};
         bool bad = false;
         for (int q0 = 0; q0 < nb; q0 += 4) {
-          longlong2 v[4];
+          if (RS) {
+            long long v[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
-            v[u] = c != BH_NONE ? __ldg(&xq[(size_t)c * B + b]) : make_longlong2(0, 0);
-          }
+            for (int u = 0; u < 4; ++u) {
+              const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
+              v[u] = c != BH_NONE ? __ldg(&xqr[(size_t)c * B + b]) : 0ll;
+            }
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            bad |= (v[u].x == kNaN) | (v[u].y == kNaN);
-            const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
-            a[t1b ? 2 : 0] += v[u].x;
-            a[t1b ? 3 : 1] += v[u].y;
+            for (int u = 0; u < 4; ++u) {
+              bad |= v[u] == kNaN;
+              const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
+              // selects, not a runtime index: a[] must stay in registers
+              a[0] += t1b ? 0ll : v[u];
+              a[2] += t1b ? v[u] : 0ll;
+            }
+          } else {
+            longlong2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
+              v[u] = c != BH_NONE ? __ldg(&xq[(size_t)c * B + b]) : make_longlong2(0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              bad |= (v[u].x == kNaN) | (v[u].y == kNaN);
+              const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
+              a[0] += t1b ? 0ll : v[u].x;
+              a[1] += t1b ? 0ll : v[u].y;
+              a[2] += t1b ? v[u].x : 0ll;
+              a[3] += t1b ? v[u].y : 0ll;
+            }
           }
         }
         const size_t k = (size_t)(r0 + rr) * B + b;
         const double d = diag[k];
-        const double2 xv = x[k];
+        const double2 xv = RS ? make_double2(xr[k], 0.0) : x[k];
         const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
         const double t1r = (double)a[2] * s1 * s2, t1i = (double)a[3] * s1 * s2;
         double yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
         double yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
         if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
-        y[k] = make_double2(yr, yi);
+        if (RS) ((double*)y_)[k] = yr;
+        else ((double2*)y_)[k] = make_double2(yr, yi);
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Column-wise (per realisation) linear algebra on [dim][B] arrays.
+// Column-wise (per realisation) linear algebra on [dim][B] arrays of the
+// batched solve.  Its basis is exactly real (real start vectors, real H), so
+// the block holds the real parts only (double[dim][B]).
 // ---------------------------------------------------------------------------
 struct BCols {
-  const double2* p[64];
+  const double* p[64];
 };
 
-// partial[(item * B + b) * nblk + blk]; items: nv dots (real or complex) + norm
-template <bool REAL>
-__global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const double2* __restrict__ w, int64_t dim,
+// partial[(item * B + b) * nblk + blk]; items 0..nv-1 = V_i^T w, item nv = ||w||^2
+__global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const double* __restrict__ w, int64_t dim,
                                                     int B, int with_norm, double* __restrict__ partial, int nblk) {
   // each block: rows [r0, r1), one thread per column b (loop over b chunks)
   const int64_t rows_per = (dim + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * rows_per, r1 = min(dim, r0 + rows_per);
   for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    double acc_re[16], acc_im[16];
+    double acc[16];
     double nrm = 0.0;
     for (int i0 = 0; i0 < max(nv, 1); i0 += 16) {
       const int ni = max(0, min(16, nv - i0));
 #pragma unroll
-      for (int i = 0; i < 16; ++i) { acc_re[i] = 0.0; acc_im[i] = 0.0; }
+      for (int i = 0; i < 16; ++i) acc[i] = 0.0;
       for (int64_t r = r0; r < r1; ++r) {
-        const double2 wv = w[(size_t)r * B + b];
+        const double wv = w[(size_t)r * B + b];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          if (i < ni) {
-            const double2 v = V.p[i0 + i][(size_t)r * B + b];
-            if (REAL) {
-              acc_re[i] = fma(v.x, wv.x, acc_re[i]);
-            } else {
-              acc_re[i] = fma(v.x, wv.x, fma(v.y, wv.y, acc_re[i]));
-              acc_im[i] = fma(v.x, wv.y, fma(-v.y, wv.x, acc_im[i]));
-            }
-          }
-        }
-        if (with_norm && i0 == 0) nrm = REAL ? fma(wv.x, wv.x, nrm) : fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
+        for (int i = 0; i < 16; ++i)
+          if (i < ni) acc[i] = fma(V.p[i0 + i][(size_t)r * B + b], wv, acc[i]);
+        if (with_norm && i0 == 0) nrm = fma(wv, wv, nrm);
       }
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        if (i < ni) {
-          partial[((size_t)(2 * (i0 + i)) * B + b) * nblk + blockIdx.x] = acc_re[i];
-          partial[((size_t)(2 * (i0 + i) + 1) * B + b) * nblk + blockIdx.x] = REAL ? 0.0 : acc_im[i];
-        }
-      }
+      for (int i = 0; i < 16; ++i)
+        if (i < ni) partial[((size_t)(i0 + i) * B + b) * nblk + blockIdx.x] = acc[i];
     }
-    if (with_norm) partial[((size_t)(2 * nv) * B + b) * nblk + blockIdx.x] = nrm;
+    if (with_norm) partial[((size_t)nv * B + b) * nblk + blockIdx.x] = nrm;
   }
 }
 
@@ -250,45 +301,29 @@ __global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int
   }
 }
 
-// w[:, b] <- w[:, b] - sum_i V_i[:, b] h[i][b] (h real when REAL); also the
-// local Lanczos terms a[b] v_j + bet[b] v_jm1 (applied first when given).
-template <bool REAL>
-__global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, const double2* __restrict__ h /* [nv][B] */,
-                                                      double2* __restrict__ w, int64_t dim, int B) {
+// w[:, b] <- w[:, b] - sum_i V_i[:, b] h[i][b]
+__global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, const double* __restrict__ h /* [nv][B] */,
+                                                      double* __restrict__ w, int64_t dim, int B) {
   const int64_t n = dim * B;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
     const int b = (int)(k % B);
-    double2 wv = w[k];
-    for (int i = 0; i < nv; ++i) {
-      const double2 v = V.p[i][k];
-      const double2 c = h[(size_t)i * B + b];
-      if (REAL) {
-        wv.x = fma(-v.x, c.x, wv.x);
-      } else {
-        wv.x = fma(-v.x, c.x, fma(v.y, c.y, wv.x));
-        wv.y = fma(-v.x, c.y, fma(-v.y, c.x, wv.y));
-      }
-    }
+    double wv = w[k];
+#pragma unroll 4
+    for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
     w[k] = wv;
   }
 }
 
 // dst[:, b] = src[:, b] * s[b]
-__global__ void k_batch_scale(const double2* __restrict__ src, double2* __restrict__ dst, const double* __restrict__ s,
+__global__ void k_batch_scale(const double* __restrict__ src, double* __restrict__ dst, const double* __restrict__ s,
                               int64_t dim, int B) {
   const int64_t n = dim * B;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    const double f = s[k % B];
-    const double2 v = src[k];
-    dst[k] = make_double2(v.x * f, v.y * f);
-  }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k] * s[k % B];
 }
 
 // out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation).
-// The batched solve keeps its basis exactly real (real start vectors, real H),
-// so only the real parts are formed.
 __global__ void __launch_bounds__(256) k_batch_restart(const BCols V, int m, const double* __restrict__ Y, int l,
                                                        BCols out, int c0, int nc, int64_t dim, int B) {
   const int64_t n = dim * B;
@@ -300,25 +335,20 @@ __global__ void __launch_bounds__(256) k_batch_restart(const BCols V, int m, con
 #pragma unroll
     for (int c = 0; c < 8; ++c) ar[c] = 0.0;
     for (int i = 0; i < m; ++i) {
-      const double vx = V.p[i][k].x;
+      const double vx = V.p[i][k];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        if (c < nc) {
-          const double y = Yb[(size_t)i * l + c0 + c];
-          ar[c] = fma(vx, y, ar[c]);
-        }
-      }
+      for (int c = 0; c < 8; ++c)
+        if (c < nc) ar[c] = fma(vx, Yb[(size_t)i * l + c0 + c], ar[c]);
     }
 #pragma unroll
     for (int c = 0; c < 8; ++c)
-      if (c < nc) ((double2*)out.p[c0 + c])[k] = make_double2(ar[c], 0.0);
+      if (c < nc) ((double*)out.p[c0 + c])[k] = ar[c];
   }
 }
 
-// start vectors: every realisation starts from the plain solver's seeded
-// real start vector (imaginary parts zero, so the basis stays exactly real
-// and the real-coefficient kernels are exact)
-__global__ void k_batch_start(uint64_t seed, int64_t dim, int B, double2* __restrict__ v) {
+// start vectors: every realisation starts from the real parts of the plain
+// solver's seeded start vector
+__global__ void k_batch_start(uint64_t seed, int64_t dim, int B, double* __restrict__ v) {
   const int64_t n = dim * B;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const uint64_t base = seed * 0xD1B54A32D192ED03ull;
@@ -326,14 +356,15 @@ __global__ void k_batch_start(uint64_t seed, int64_t dim, int B, double2* __rest
     const uint64_t i = (uint64_t)(k / B);
     const uint64_t h1 = ed_splitmix64(base + 2 * i);
     const double u1 = (double)(h1 >> 11) * (1.0 / 9007199254740992.0);
-    v[k] = make_double2(2.0 * u1 - 1.0, 0.0);
+    v[k] = 2.0 * u1 - 1.0;
   }
 }
 
-// copy realisation b's column of a [dim][B] array into a contiguous vector
-__global__ void k_batch_extract(const double2* __restrict__ src, int64_t dim, int B, int b, double2* __restrict__ dst) {
+// realisation b's column of a real [dim][B] array as a complex128 vector
+__global__ void k_batch_extract(const double* __restrict__ src, int64_t dim, int B, int b, double2* __restrict__ dst) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) dst[r] = src[(size_t)r * B + b];
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride)
+    dst[r] = make_double2(src[(size_t)r * B + b], 0.0);
 }
 
 // dst[r][t] = src[r][keep[t]]: realisation columns keep[0..A2) of a [dim][A]
@@ -351,7 +382,7 @@ __global__ void k_batch_pack(const T* __restrict__ src, T* __restrict__ dst, int
 
 // dst[r][orig[t]] = src[r][slot[t]]: converged slots of a [dim][A] array into
 // their realisations' columns of a [dim][B] array.
-__global__ void k_batch_save(const double2* __restrict__ src, double2* __restrict__ dst, int64_t dim, int A, int B,
+__global__ void k_batch_save(const double* __restrict__ src, double* __restrict__ dst, int64_t dim, int A, int B,
                              const int* __restrict__ slot, const int* __restrict__ orig, int ns) {
   const int64_t n = dim * ns;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -383,23 +414,20 @@ static int batch_reduce_buf(ed_batch* bt, size_t doubles) {
   return ED_OK;
 }
 
-// dots of nv vectors against w, per realisation; out (host) [item][B]: item
-// 2i = Re, 2i+1 = Im of V_i^H w, item 2nv = ||w||^2.
-static int batch_dots(ed_batch* bt, int B, const std::vector<const double2*>& V, const double2* w, bool real, bool norm,
+// dots of nv real columns against w, per realisation; out (host) [item][B]:
+// item i < nv = V_i^T w, item nv = ||w||^2.
+static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, const double* w, bool norm,
                       std::vector<double>& out) {
   ed_ctx* ctx = bt->h->ctx;
   const int nv = (int)V.size();
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 2));
-  const int64_t items = (int64_t)(2 * nv + 1) * B;
+  const int64_t items = (int64_t)(nv + 1) * B;
   ED_TRY(batch_reduce_buf(bt, (size_t)items * nblk + (size_t)items));
   BCols vc;
   memset(&vc, 0, sizeof(vc));
   for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
   const int threads = std::min(256, ((B + 31) / 32) * 32);
-  if (real)
-    k_batch_dots<true><<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
-  else
-    k_batch_dots<false><<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
+  k_batch_dots<<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
   k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
@@ -411,8 +439,9 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double2*>& V,
 }
 
 // y = H_b x for the B (active) realisation columns of x, whose diagonals are
-// the columns of diag ([dim][B]).
-static int batch_hv(ed_batch* bt, int B, const double* diag, const double2* x, double2* y) {
+// the columns of diag ([dim][B]).  rs: x, y are real storage double[dim][B]
+// (the solve), else complex128 blocks (ed_batch_apply).
+static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void* y, bool rs) {
   ed_ham* h = bt->h;
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
@@ -423,9 +452,16 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const double2* x, d
   while ((1 << head) < std::max(cnt[0], cnt[1]) + 1) ++head;
   const int sbits = 62 - head;
   ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
-  k_batch_maxexp<<<grid_n(ctx, n), 256, 0, ctx->stream>>>(x, n, bt->d_gmax);
-  ED_CHECK_LAUNCH(ctx);
-  k_batch_quantize<<<grid_n(ctx, n), 256, 0, ctx->stream>>>(x, n, bt->d_gmax, sbits, bt->d_xq);
+  if (rs) {
+    k_batch_maxexp_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax);
+    ED_CHECK_LAUNCH(ctx);
+    k_batch_quantize_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, sbits,
+                                                                 (long long*)bt->d_xq);
+  } else {
+    k_batch_maxexp<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double2*)x, n, bt->d_gmax);
+    ED_CHECK_LAUNCH(ctx);
+    k_batch_quantize<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double2*)x, n, bt->d_gmax, sbits, bt->d_xq);
+  }
   ED_CHECK_LAUNCH(ctx);
   BatchBonds bb;
   memset(&bb, 0, sizeof(bb));
@@ -438,18 +474,25 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const double2* x, d
   const size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)BH_ROWS * std::max(bb.nb, 1));
   static bool attr = false;
   if (!attr) {
-    ED_CUDA(cudaFuncSetAttribute(k_batch_hv, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    ED_CUDA(cudaFuncSetAttribute(k_batch_hv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    ED_CUDA(cudaFuncSetAttribute(k_batch_hv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
     attr = true;
   }
   int per_sm = 0;
   const int threads = std::min(256, ((B + 31) / 32) * 32);
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv, threads, smem));
+  if (rs) ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<true>, threads, smem));
+  else ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<false>, threads, smem));
   if (per_sm < 1) per_sm = 1;
   const int64_t tiles = (bt->dim + BH_ROWS - 1) / BH_ROWS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
-  k_batch_hv<<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim, B,
-                                                   b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
-                                                   h->bs.chalf[1]);
+  if (rs)
+    k_batch_hv<true><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim,
+                                                           B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
+                                                           h->bs.chalf[1]);
+  else
+    k_batch_hv<false><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y,
+                                                            bt->dim, B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb,
+                                                            h->bs.chalf[0], h->bs.chalf[1]);
   ED_CHECK_LAUNCH(ctx);
   return ED_OK;
 }
@@ -517,7 +560,7 @@ int ed_batch_destroy(ed_batch* bt) {
 int ed_batch_apply(ed_batch* bt, const ed_cplx* x_dev, ed_cplx* y_dev) {
   if (!bt || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
   if ((const void*)x_dev == (const void*)y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
-  return batch_hv(bt, bt->B, bt->d_diag, (const double2*)x_dev, (double2*)y_dev);
+  return batch_hv(bt, bt->B, bt->d_diag, x_dev, y_dev, false);
 }
 
 int ed_batch_diag_host(ed_batch* bt, double* out_host) {
@@ -552,14 +595,14 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   const int l_keep = std::min(m - 1, std::max(nev + 2, m / 2));
   const size_t colB = (size_t)dim * B;
   const int pool_cols = 2 * m + 1;
-  double2* pool = nullptr;
-  double2* w = nullptr;
+  double* pool = nullptr;
+  double* w = nullptr;
   double* dg[2] = {nullptr, nullptr};
   double* d_coef = nullptr;  // [64][B] double2 coefficients / scale factors
   int* d_idx = nullptr;      // [2][B] slot / realisation index lists
   double* dY = nullptr;
-  if (cudaMalloc(&pool, sizeof(double2) * colB * pool_cols) != cudaSuccess ||
-      cudaMalloc(&w, sizeof(double2) * colB) != cudaSuccess || cudaMalloc(&dg[0], sizeof(double) * colB) != cudaSuccess ||
+  if (cudaMalloc(&pool, sizeof(double) * colB * pool_cols) != cudaSuccess ||
+      cudaMalloc(&w, sizeof(double) * colB) != cudaSuccess || cudaMalloc(&dg[0], sizeof(double) * colB) != cudaSuccess ||
       cudaMalloc(&dg[1], sizeof(double) * colB) != cudaSuccess ||
       cudaMalloc(&d_coef, sizeof(double2) * 64 * (size_t)B) != cudaSuccess ||
       cudaMalloc(&d_idx, sizeof(int) * 2 * (size_t)B) != cudaSuccess ||
@@ -570,14 +613,14 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
   if (bt->d_vecs) cudaFree(bt->d_vecs);
   bt->d_vecs = nullptr;
-  if (cudaMalloc(&bt->d_vecs, sizeof(double2) * colB * nev) != cudaSuccess) {
+  if (cudaMalloc(&bt->d_vecs, sizeof(double) * colB * nev) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(pool); cudaFree(w); cudaFree(dg[0]); cudaFree(dg[1]); cudaFree(d_coef); cudaFree(d_idx); cudaFree(dY);
     return ed_fail(ED_ENOMEM, "batched eigenvectors do not fit in device memory");
   }
-  std::vector<double2*> col(m + 1), freel;
+  std::vector<double*> col(m + 1), freel;
   for (int i = 0; i < pool_cols; ++i) {
-    double2* p = pool + (size_t)i * colB;
+    double* p = pool + (size_t)i * colB;
     if (i <= m) col[i] = p; else freel.push_back(p);
   }
   int cur = 0;  // dg[cur] holds the active realisations' diagonals
@@ -597,8 +640,8 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   k_batch_start<<<grid_n(ctx, (int64_t)colB), 256, 0, ctx->stream>>>(seed, dim, A, col[0]);
   ctx->kernels++;
   {
-    std::vector<const double2*> none;
-    if ((rc = batch_dots(bt, A, none, col[0], true, true, out)) != ED_OK) goto cleanup;
+    std::vector<const double*> none;
+    if ((rc = batch_dots(bt, A, none, col[0], true, out)) != ED_OK) goto cleanup;
     std::vector<double> sc(A);
     for (int b = 0; b < A; ++b) sc[b] = 1.0 / std::sqrt(out[b]);
     cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
@@ -609,48 +652,45 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     ++its;
     const int64_t colA = dim * (int64_t)A;
     for (int j = k; j < m; ++j) {
-      if ((rc = batch_hv(bt, A, dg[cur], col[j], w)) != ED_OK) goto cleanup;
+      if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true)) != ED_OK) goto cleanup;
       bt->nhv++;
       // local projection coefficients: a_b = v_j^H w, beta_{j-1}
-      std::vector<const double2*> vj(1, col[j]);
-      if ((rc = batch_dots(bt, A, vj, w, true, true, out)) != ED_OK) goto cleanup;
+      std::vector<const double*> vj(1, col[j]);
+      if ((rc = batch_dots(bt, A, vj, w, true, out)) != ED_OK) goto cleanup;
       {
-        std::vector<double2> hc((size_t)2 * A);
+        std::vector<double> hc((size_t)2 * A);
         const bool three = j > k && j > 0;
         for (int b = 0; b < A; ++b) {
           const double a = out[b];
           alpha[(size_t)b * (m + 1) + j] = a;
-          hc[b] = make_double2(a, 0.0);
-          hc[(size_t)A + b] = make_double2(three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0, 0.0);
+          hc[b] = a;
+          hc[(size_t)A + b] = three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0;
         }
-        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * 2 * A, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * 2 * A, cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
         vc.p[0] = col[j];
         vc.p[1] = three ? col[j - 1] : col[j];
-        k_batch_update<true><<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, three ? 2 : 1, (const double2*)d_coef, w,
-                                                                         dim, A);
+        k_batch_update<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, three ? 2 : 1, d_coef, w, dim, A);
         ctx->kernels++;
       }
       // full CGS pass (+ DGKS refinement when any realisation needs it)
-      std::vector<const double2*> vs(col.begin(), col.begin() + j + 1);
+      std::vector<const double*> vs(col.begin(), col.begin() + j + 1);
       std::vector<double> prevn(A, 0.0);
       for (int pass = 0; pass < 2; ++pass) {
-        if ((rc = batch_dots(bt, A, vs, w, true, true, out)) != ED_OK) goto cleanup;
-        std::vector<double2> hc((size_t)(j + 1) * A);
-        for (int i = 0; i <= j; ++i)
-          for (int b = 0; b < A; ++b) hc[(size_t)i * A + b] = make_double2(out[((size_t)2 * i) * A + b], 0.0);
-        for (int b = 0; b < A; ++b) prevn[b] = std::sqrt(out[((size_t)2 * (j + 1)) * A + b]);
-        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
+        if ((rc = batch_dots(bt, A, vs, w, true, out)) != ED_OK) goto cleanup;
+        std::vector<double> hc(out.begin(), out.begin() + (size_t)(j + 1) * A);
+        for (int b = 0; b < A; ++b) prevn[b] = std::sqrt(out[(size_t)(j + 1) * A + b]);
+        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
         for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
-        k_batch_update<true><<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, j + 1, (const double2*)d_coef, w, dim, A);
+        k_batch_update<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A);
         ctx->kernels++;
-        for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b].x;
+        for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b];
         // norms after the update
-        std::vector<const double2*> none;
-        if ((rc = batch_dots(bt, A, none, w, true, true, out)) != ED_OK) goto cleanup;
+        std::vector<const double*> none;
+        if ((rc = batch_dots(bt, A, none, w, true, out)) != ED_OK) goto cleanup;
         bool again = false;
         for (int b = 0; b < A; ++b) {
           const double nw = std::sqrt(out[b]);
@@ -705,7 +745,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       }
     }
     // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
-    std::vector<double2*> outc(freel.begin(), freel.begin() + l_keep);
+    std::vector<double*> outc(freel.begin(), freel.begin() + l_keep);
     {
       ED_CUDA(cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream));
       BCols vin, vout;
@@ -732,19 +772,19 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       }
     }
     // new column order: restarted vectors, then the residual vector
-    std::vector<double2*> newcol(m + 1, nullptr);
+    std::vector<double*> newcol(m + 1, nullptr);
     for (int c = 0; c < l_keep; ++c) newcol[c] = outc[c];
     newcol[l_keep] = col[m];
-    std::vector<double2*> nf(freel.begin() + l_keep, freel.end());
+    std::vector<double*> nf(freel.begin() + l_keep, freel.end());
     for (int c = 0; c < m; ++c) nf.push_back(col[c]);
     // pack the live columns and the diagonals to the realisations still active
     const int A2 = (int)keep_slots.size();
     if (A2 > 0 && A2 < A) {
       ED_CUDA(cudaMemcpyAsync(d_idx, keep_slots.data(), sizeof(int) * A2, cudaMemcpyHostToDevice, ctx->stream));
       for (int c = 0; c <= l_keep; ++c) {
-        double2* dst = nf.back();
+        double* dst = nf.back();
         nf.pop_back();
-        k_batch_pack<double2><<<grid_n(ctx, dim * (int64_t)A2), 256, 0, ctx->stream>>>(newcol[c], dst, dim, A, A2,
+        k_batch_pack<double><<<grid_n(ctx, dim * (int64_t)A2), 256, 0, ctx->stream>>>(newcol[c], dst, dim, A, A2,
                                                                                       d_idx);
         ctx->kernels++;
         nf.push_back(newcol[c]);
@@ -782,20 +822,20 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
   // true relative residuals ||H x - theta x|| / |theta| of the saved vectors
   for (int i = 0; i < nev; ++i) {
-    double2* xv = bt->d_vecs + (size_t)i * colB;
-    if ((rc = batch_hv(bt, B, bt->d_diag, xv, w)) != ED_OK) goto cleanup;
-    std::vector<double2> hc(B);
-    for (int b = 0; b < B; ++b) hc[b] = make_double2(bt->evals[(size_t)b * nev + i], 0.0);
-    cudaMemcpyAsync(d_coef, hc.data(), sizeof(double2) * B, cudaMemcpyHostToDevice, ctx->stream);
+    double* xv = bt->d_vecs + (size_t)i * colB;
+    if ((rc = batch_hv(bt, B, bt->d_diag, xv, w, true)) != ED_OK) goto cleanup;
+    std::vector<double> hc(B);
+    for (int b = 0; b < B; ++b) hc[b] = bt->evals[(size_t)b * nev + i];
+    cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * B, cudaMemcpyHostToDevice, ctx->stream);
     BCols vc;
     memset(&vc, 0, sizeof(vc));
     vc.p[0] = xv;
-    k_batch_update<true><<<grid_n(ctx, (int64_t)colB), 256, 0, ctx->stream>>>(vc, 1, (const double2*)d_coef, w, dim, B);
+    k_batch_update<<<grid_n(ctx, (int64_t)colB), 256, 0, ctx->stream>>>(vc, 1, d_coef, w, dim, B);
     ctx->kernels++;
-    std::vector<const double2*> none;
-    if ((rc = batch_dots(bt, B, none, w, true, true, out)) != ED_OK) goto cleanup;
+    std::vector<const double*> none;
+    if ((rc = batch_dots(bt, B, none, w, true, out)) != ED_OK) goto cleanup;
     std::vector<double> r2(out.begin(), out.begin() + B);
-    if ((rc = batch_dots(bt, B, none, xv, true, true, out)) != ED_OK) goto cleanup;
+    if ((rc = batch_dots(bt, B, none, xv, true, out)) != ED_OK) goto cleanup;
     for (int b = 0; b < B; ++b)
       bt->errs[(size_t)b * nev + i] =
           std::sqrt(r2[b]) / std::max(std::fabs(bt->evals[(size_t)b * nev + i]) * std::sqrt(out[b]), 1e-300);
