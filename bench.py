@@ -566,7 +566,8 @@ def run_ours(args):
         'e2e': e2e, 'gpu_launches': launches,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
                      'traffic': traffic,
-                     'kernel': 'matrix-free H.v: k_hv_lin (two-table rank) + k_quantize64 + k_max_exponent',
+                     'kernel': 'matrix-free H.v: two-table-rank kernel (k_hv_jit* when hv_variant is jit*, else '
+                               'k_hv_lin) + k_quantize64_r + k_max_exponent_r',
                      'hv_variant': {'plain': H.hv_variant(False), 'fused_dot': H.hv_variant(True)},
                      'traffic_note': traffic_note, 'peak_kind': peak_kind,
                      'bytes_per_row': bytes_row, 'bytes_per_row_complex_input': bytes_row_complex,

@@ -264,31 +264,53 @@ struct BCols {
   const double* p[64];
 };
 
-// partial[(item * B + b) * nblk + blk]; items 0..nv-1 = V_i^T w, item nv = ||w||^2
+// partial[(item * B + b) * nblk + blk]; items 0..nv-1 = V_i^T w, item nv = ||w||^2.
+// A block takes a contiguous range of rows; its 256 threads are Bp column
+// lanes (consecutive b: coalesced) times 256 / Bp row lanes, and the row
+// lanes are summed in shared memory in a fixed order at the end.
+#define BD_MAXV 16
 __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const double* __restrict__ w, int64_t dim,
                                                     int B, int with_norm, double* __restrict__ partial, int nblk) {
-  // each block: rows [r0, r1), one thread per column b (loop over b chunks)
+  __shared__ double sh[256 * (BD_MAXV + 1)];
+  const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
+  const int S = 256 / Bp;  // row lanes
+  const int lane_b = threadIdx.x % Bp, lane_r = threadIdx.x / Bp;
   const int64_t rows_per = (dim + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * rows_per, r1 = min(dim, r0 + rows_per);
-  for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    double acc[16];
-    double nrm = 0.0;
-    for (int i0 = 0; i0 < max(nv, 1); i0 += 16) {
-      const int ni = max(0, min(16, nv - i0));
+  for (int b0 = 0; b0 < B; b0 += Bp) {
+    const int b = b0 + lane_b;
+    const bool act = lane_r < S && b < B;
+    for (int i0 = 0; i0 < max(nv, 1); i0 += BD_MAXV) {
+      const int ni = max(0, min(BD_MAXV, nv - i0));
+      const bool norm = with_norm && i0 == 0;
+      double acc[BD_MAXV + 1];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) acc[i] = 0.0;
-      for (int64_t r = r0; r < r1; ++r) {
-        const double wv = w[(size_t)r * B + b];
+      for (int i = 0; i <= BD_MAXV; ++i) acc[i] = 0.0;
+      if (act) {
+        for (int64_t r = r0 + lane_r; r < r1; r += S) {
+          const size_t k = (size_t)r * B + b;
+          const double wv = w[k];
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-          if (i < ni) acc[i] = fma(V.p[i0 + i][(size_t)r * B + b], wv, acc[i]);
-        if (with_norm && i0 == 0) nrm = fma(wv, wv, nrm);
+          for (int i = 0; i < BD_MAXV; ++i)
+            if (i < ni) acc[i] = fma(V.p[i0 + i][k], wv, acc[i]);
+          if (norm) acc[BD_MAXV] = fma(wv, wv, acc[BD_MAXV]);
+        }
       }
+      __syncthreads();  // sh free
 #pragma unroll
-      for (int i = 0; i < 16; ++i)
-        if (i < ni) partial[((size_t)(i0 + i) * B + b) * nblk + blockIdx.x] = acc[i];
+      for (int i = 0; i <= BD_MAXV; ++i) sh[i * 256 + threadIdx.x] = acc[i];
+      __syncthreads();
+      if (lane_r == 0 && b < B) {
+        for (int i = 0; i <= BD_MAXV; ++i) {
+          if (i < ni || (i == BD_MAXV && norm)) {
+            double t = 0.0;
+            for (int q = 0; q < S; ++q) t += sh[i * 256 + q * Bp + lane_b];
+            const int item = i < BD_MAXV ? i0 + i : nv;
+            partial[((size_t)item * B + b) * nblk + blockIdx.x] = t;
+          }
+        }
+      }
     }
-    if (with_norm) partial[((size_t)nv * B + b) * nblk + blockIdx.x] = nrm;
   }
 }
 
@@ -420,14 +442,13 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
                       std::vector<double>& out) {
   ed_ctx* ctx = bt->h->ctx;
   const int nv = (int)V.size();
-  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 2));
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 4));
   const int64_t items = (int64_t)(nv + 1) * B;
   ED_TRY(batch_reduce_buf(bt, (size_t)items * nblk + (size_t)items));
   BCols vc;
   memset(&vc, 0, sizeof(vc));
   for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
-  const int threads = std::min(256, ((B + 31) / 32) * 32);
-  k_batch_dots<<<nblk, threads, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
+  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
   k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);

@@ -4,6 +4,7 @@
 #include "ed_internal.h"
 #include "ed_device.cuh"
 #include <algorithm>
+#include <cmath>
 
 #define ED_RED_THREADS 256
 #define ED_GROUP 8
@@ -601,6 +602,64 @@ __global__ void __launch_bounds__(256) k_restart_r(const ColPtrsR cp, int m, con
   }
 }
 
+// The same combination in exact integer arithmetic.  Every column is a unit
+// vector and Y is orthogonal, so |v|, |Y| <= 1: both become 62-bit fixed
+// point (v converted in registers, Y on the host), each product is formed
+// exactly in 128 bits (__mul64hi and the low word), the sums are exact (by
+// Cauchy-Schwarz |sum_i v_i Y_ic| <= sqrt(m) < 2^2.5, far inside 128 bits),
+// and each output is rounded once.  On GB300 the integer pipes run far
+// faster than FP64 FMA, which bounds k_restart_r.  A non-finite input entry
+// makes its row's outputs NaN, as the FP64 form would.
+__device__ __forceinline__ long long ed_fx62(double v, bool& bad) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  if (e == 0x7FF) { bad = true; return 0; }
+  if (e == 0) return 0;  // |v| < 2^-1022
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = e - 1013;  // v * 2^62 = mant * 2^(e - 1023 - 52 + 62)
+  unsigned long long a;
+  if (sh >= 0) a = mant << sh;  // |v| <= 1: sh <= 10, a <= 2^62
+  else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);
+  else a = 0;
+  return (bits >> 63) ? -(long long)a : (long long)a;
+}
+
+__global__ void __launch_bounds__(256) k_restart_fx(const ColPtrsR cp, int m, const long long* __restrict__ Yq, int c0,
+                                                    int nc, const ColPtrs outp, int64_t n) {
+  __shared__ long long shY[128 * 8];  // m x 8 coefficients of this group
+  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) shY[k] = Yq[(size_t)(k / 8) * 8 + (k % 8)];
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    unsigned long long lo[8];
+    long long hi[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { lo[c] = 0ull; hi[c] = 0ll; }
+    bool bad = false;
+    for (int i = 0; i < m; ++i) {
+      const long long v = ed_fx62(cp.p[i][r], bad);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const long long y = shY[i * 8 + c];
+        const unsigned long long pl = (unsigned long long)v * (unsigned long long)y;
+        const long long ph = __mul64hi(v, y);
+        const unsigned long long s = lo[c] + pl;
+        hi[c] += ph + (s < pl ? 1 : 0);
+        lo[c] = s;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (c < nc) {
+        // (hi * 2^64 + lo) * 2^-124
+        double d = fma((double)hi[c], 0x1p-60, (double)lo[c] * 0x1p-124);
+        if (bad) d = __longlong_as_double(0x7FF8000000000000ll);
+        ((double*)outp.p[c0 + c])[r] = d;
+      }
+    }
+  }
+}
+
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
                          double* const* out, int64_t n) {
   if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
@@ -608,16 +667,29 @@ int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const do
   ColPtrs op;
   for (int i = 0; i < 128; ++i) op.p[i] = nullptr;
   for (int i = 0; i < l && i < 128; ++i) op.p[i] = (const double2*)out[i];
-  ED_TRY(ed_ensure_reduce(ctx, (size_t)m * ldY + 16));
-  double* dY = ctx->d_red;
-  ED_CUDA(cudaMemcpyAsync(dY, Y, sizeof(double) * (size_t)m * ldY, cudaMemcpyHostToDevice, ctx->stream));
-  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 4));
-  size_t smem = sizeof(double) * (size_t)m * 8;
-  for (int c0 = 0; c0 < l; c0 += 8) {
-    int nc = std::min(8, l - c0);
-    k_restart_r<<<g, 256, smem, ctx->stream>>>(cp, m, dY, ldY, c0, nc, op, n);
+  // coefficients as 62-bit fixed point, [group][i][8]
+  const int ngroups = (l + 7) / 8;
+  std::vector<long long> yq((size_t)ngroups * m * 8, 0);
+  for (int gi = 0; gi < ngroups; ++gi)
+    for (int i = 0; i < m; ++i)
+      for (int c = 0; c < 8; ++c) {
+        const int col = gi * 8 + c;
+        if (col < l) yq[((size_t)gi * m + i) * 8 + c] = std::llround(std::ldexp(Y[(size_t)i * ldY + col], 62));
+      }
+  ED_TRY(ed_ensure_reduce(ctx, yq.size() + 16));
+  long long* dY = (long long*)ctx->d_red;
+  ED_CUDA(cudaMemcpyAsync(dY, yq.data(), sizeof(long long) * yq.size(), cudaMemcpyHostToDevice, ctx->stream));
+  int per_sm = 0;
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_fx, 256, 0));
+  if (per_sm < 1) per_sm = 1;
+  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
+  for (int gi = 0; gi < ngroups; ++gi) {
+    const int nc = std::min(8, l - gi * 8);
+    k_restart_fx<<<g, 256, 0, ctx->stream>>>(cp, m, dY + (size_t)gi * m * 8, gi * 8, nc, op, n);
     ED_CHECK_LAUNCH(ctx);
   }
+  // the host coefficients must outlive the copy
+  ED_CUDA(cudaStreamSynchronize(ctx->stream));
   return ED_OK;
 }
 
