@@ -47,6 +47,23 @@ def _rank_info():
     return ws, rk, lr
 
 
+def shard_units(n, rank, world):
+    """Round-robin partition of n independent units (disorder seeds) over the
+    ranks: each rank solves its own seeds, no data-path collective."""
+    return list(range(rank, n, world))
+
+
+def dist_reduce(value, ws, op='max'):
+    """MAX or SUM of a host scalar over the ranks (gloo; identity when ws == 1)."""
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == 'max' else dist.ReduceOp.SUM)
+    return float(t[0])
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
@@ -140,7 +157,9 @@ class CpuSample:
         self.nnz = self.M.build(3)
         n = self.M.dim
         self.x = oracle.start_vector(1, n)
-        self.V = np.ascontiguousarray(np.stack([oracle.start_vector(10 + i, n) for i in range(12)]))
+        # an orthonormal basis, so repeated CGS passes on w stay bounded
+        q, _ = np.linalg.qr(np.stack([oracle.start_vector(10 + i, n) for i in range(12)]).T)
+        self.V = np.ascontiguousarray(q.T)
         self.w = oracle.start_vector(2, n)
         nn, nnn = oracle.bond_pairs(self.lt, N, lx, ly)
         self.nnz_row_f = 1 + kbar(N, mag + N // 2, list(map(tuple, nn)) + (list(map(tuple, nnn)) if J2 else []))
@@ -273,9 +292,15 @@ def run_disorder(args):
     build()
     import lsquantumed_gb300 as ed
     N, J1, J2, W, nev, tol = 20, 1.0, 0.2, 2.0, 2, 1e-9
+    ws, rk, lr = _rank_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    torch.cuda.set_device(lr)
     nseeds = args.seeds
-    env = ed.Environment(nspins=N)
-    fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in range(nseeds)])
+    mine = shard_units(nseeds, rk, ws)  # this rank's seeds (weak scaling: every rank a share)
+    env = ed.Environment(nspins=N, device=lr)
+    fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in mine])
     sectors = (0, 1, 2)
     hams = {}
     for mag in sectors:
@@ -290,6 +315,8 @@ def run_disorder(args):
         bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
         del bt
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     k0 = env.kernel_count()
     t0 = time.perf_counter()
     max_err, its, bad = 0.0, [], 0
@@ -303,11 +330,15 @@ def run_disorder(args):
         batch_evals[mag] = r['evals']
         del bt
     torch.cuda.synchronize()
-    t_batch = time.perf_counter() - t0
+    t_batch = dist_reduce(time.perf_counter() - t0, ws, 'max')
     launches = env.kernel_count() - k0
+    max_err = dist_reduce(max_err, ws, 'max')
+    bad = int(dist_reduce(bad, ws, 'sum'))
     nsolve = nseeds * len(sectors)
+    if rk != 0:
+        return 0
     # plain: one solve at a time on a subset
-    nplain = min(args.plain_sample, nseeds)
+    nplain = min(args.plain_sample, len(mine))
     t0 = time.perf_counter()
     agree = True
     for mag in sectors:
@@ -327,7 +358,8 @@ def run_disorder(args):
     torch.cuda.synchronize()
     t_plain = (time.perf_counter() - t0) / (nplain * len(sectors))
     line = {'metric': METRIC, 'workload': 'c3', 'value': nsolve / t_batch, 'unit': 'samples/s',
-            'higher_is_better': True, 'n_gpus': 1, 'steps': 1, 'warmup': args.warmup,
+            'higher_is_better': True, 'n_gpus': ws, 'steps': 1, 'warmup': args.warmup,
+            'scaling': 'strong',  # the 1,536 solves are split over the ranks by seed
             'batched': {'samples_per_s': nsolve / t_batch, 'seconds': t_batch, 'solves': nsolve,
                         'restarts_per_sector': its, 'max_rel_residual': max_err, 'unconverged': bad,
                         'gpu_launches': launches},
@@ -482,11 +514,7 @@ def run_ours(args):
         del psi0
     outputs = workload_outputs(ed, env, b, lat, wl, eps, evals) if wl in ('c1', 'c2') else None
     ed.Solver.SolverClean(eps)
-    ms_step = ms / args.steps
-    if ws > 1:
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t[0])
+    ms_step = dist_reduce(ms / args.steps, ws, 'max')
 
     # roofline of the dominant kernel (H.v): algorithmic bytes per launch
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
