@@ -22,7 +22,7 @@ SOURCES = ['ed_capi.cu', 'ed_basis.cu', 'ed_hamiltonian.cu', 'ed_linalg.cu', 'ed
            'ed_batch.cu', 'ed_adjoint.cu', 'ed_hv_lin.cu',
            'ed_spectrum.cu', 'ed_hv_jit.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
+FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2', '-Xcompiler', '-fopenmp',
          '--expt-relaxed-constexpr', '-I' + os.path.join(ROOT, 'include')]
 
 
@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
     objs = [os.path.join(BUILD, s.replace('.cu', '.o')) for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + '.tmp%d' % os.getpid()
-        cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-cudart', 'static', '-ldl']
+        cmd = [cc] + ARCH + ['-shared', '-o', tmp] + objs + ['-cudart', 'static', '-ldl', '-lgomp']
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

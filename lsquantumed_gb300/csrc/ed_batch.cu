@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
                                                   const int* __restrict__ gmax_p, int sbits, void* __restrict__ y_,
                                                   int64_t dim, int B, const uint16_t* __restrict__ t0,
                                                   const uint32_t* __restrict__ t1, int w0, const BatchBonds bb,
-                                                  double c0, double c1) {
+                                                  double c0, double c1, double* __restrict__ partial) {
   const double2* __restrict__ x = (const double2*)xv_;
   const longlong2* __restrict__ xq = (const longlong2*)xq_;
   const double* __restrict__ xr = (const double*)xv_;
@@ -178,7 +178,12 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
   extern __shared__ uint32_t sm[];
   uint16_t* t0s = (uint16_t*)sm;                       // 2^w0 entries
   uint32_t* tgt = sm + ((1 << w0) + 1) / 2;            // [BH_ROWS][nb]
+  // with partial (real storage only): per-realisation x^T y and ||y||^2 of
+  // this CTA's rows, [2][B] doubles after the targets (8-byte aligned)
+  double* dacc = (double*)(sm + ((((1 << w0) + 1) / 2 + BH_ROWS * bb.nb + 1) & ~1));
   for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
+  if (RS && partial)
+    for (int i = threadIdx.x; i < 2 * B; i += blockDim.x) dacc[i] = 0.0;
   const int e_unit = *gmax_p - 1022 - sbits;
   const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
   const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
@@ -248,9 +253,23 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
         double yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
         double yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
         if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
-        if (RS) ((double*)y_)[k] = yr;
-        else ((double2*)y_)[k] = make_double2(yr, yi);
+        if (RS) {
+          ((double*)y_)[k] = yr;
+          if (partial) {  // column b belongs to this thread in every tile: no race
+            dacc[b] = fma(xv.x, yr, dacc[b]);
+            dacc[B + b] = fma(yr, yr, dacc[B + b]);
+          }
+        } else {
+          ((double2*)y_)[k] = make_double2(yr, yi);
+        }
       }
+    }
+  }
+  if (RS && partial) {
+    // partial[(item * B + b) * gridDim.x + blk], item 0 = x^T y, 1 = ||y||^2
+    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+      partial[(size_t)b * gridDim.x + blockIdx.x] = dacc[b];
+      partial[((size_t)B + b) * gridDim.x + blockIdx.x] = dacc[B + b];
     }
   }
 }
@@ -269,8 +288,12 @@ struct BCols {
 // lanes (consecutive b: coalesced) times 256 / Bp row lanes, and the row
 // lanes are summed in shared memory in a fixed order at the end.
 #define BD_MAXV 16
-__global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const double* __restrict__ w, int64_t dim,
-                                                    int B, int with_norm, double* __restrict__ partial, int nblk) {
+// With vj: first w <- w - a_b vj - bet_b vjm1 (coef = [a][B], [bet][B]),
+// written back, in the same pass (the local Lanczos projection).
+__global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, double* __restrict__ w, int64_t dim,
+                                                    int B, int with_norm, double* __restrict__ partial, int nblk,
+                                                    const double* __restrict__ vj, const double* __restrict__ vjm1,
+                                                    const double* __restrict__ coef) {
   __shared__ double sh[256 * (BD_MAXV + 1)];
   const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
   const int S = 256 / Bp;  // row lanes
@@ -287,9 +310,16 @@ __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, const
 #pragma unroll
       for (int i = 0; i <= BD_MAXV; ++i) acc[i] = 0.0;
       if (act) {
+        const bool local = vj && i0 == 0;
+        const double ca = local ? coef[b] : 0.0, cb = local ? coef[B + b] : 0.0;
         for (int64_t r = r0 + lane_r; r < r1; r += S) {
           const size_t k = (size_t)r * B + b;
-          const double wv = w[k];
+          double wv = w[k];
+          if (local) {
+            wv = fma(-ca, vj[k], wv);
+            if (vjm1) wv = fma(-cb, vjm1[k], wv);
+            w[k] = wv;
+          }
 #pragma unroll
           for (int i = 0; i < BD_MAXV; ++i)
             if (i < ni) acc[i] = fma(V.p[i0 + i][k], wv, acc[i]);
@@ -334,6 +364,41 @@ __global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, con
 #pragma unroll 4
     for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
     w[k] = wv;
+  }
+}
+
+// The same update with the new ||w[:, b]||^2 per realisation in the same pass:
+// partial[b * nblk + blk] (blocks over row ranges, lanes as in k_batch_dots).
+__global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv, const double* __restrict__ h,
+                                                           double* __restrict__ w, int64_t dim, int B,
+                                                           double* __restrict__ partial, int nblk) {
+  __shared__ double sh[256];
+  const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
+  const int S = 256 / Bp;
+  const int lane_b = threadIdx.x % Bp, lane_r = threadIdx.x / Bp;
+  const int64_t rows_per = (dim + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per, r1 = min(dim, r0 + rows_per);
+  for (int b0 = 0; b0 < B; b0 += Bp) {
+    const int b = b0 + lane_b;
+    double nrm = 0.0;
+    if (lane_r < S && b < B) {
+      for (int64_t r = r0 + lane_r; r < r1; r += S) {
+        const size_t k = (size_t)r * B + b;
+        double wv = w[k];
+#pragma unroll 4
+        for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
+        w[k] = wv;
+        nrm = fma(wv, wv, nrm);
+      }
+    }
+    __syncthreads();
+    sh[threadIdx.x] = nrm;
+    __syncthreads();
+    if (lane_r == 0 && b < B) {
+      double t = 0.0;
+      for (int q = 0; q < S; ++q) t += sh[q * Bp + lane_b];
+      partial[(size_t)b * nblk + blockIdx.x] = t;
+    }
   }
 }
 
@@ -438,8 +503,9 @@ static int batch_reduce_buf(ed_batch* bt, size_t doubles) {
 
 // dots of nv real columns against w, per realisation; out (host) [item][B]:
 // item i < nv = V_i^T w, item nv = ||w||^2.
-static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, const double* w, bool norm,
-                      std::vector<double>& out) {
+static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, double* w, bool norm,
+                      std::vector<double>& out, const double* vj = nullptr, const double* vjm1 = nullptr,
+                      const double* coef = nullptr) {
   ed_ctx* ctx = bt->h->ctx;
   const int nv = (int)V.size();
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 4));
@@ -448,7 +514,7 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
   BCols vc;
   memset(&vc, 0, sizeof(vc));
   for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
-  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk);
+  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk, vj, vjm1, coef);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
   k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
@@ -462,7 +528,8 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
 // y = H_b x for the B (active) realisation columns of x, whose diagonals are
 // the columns of diag ([dim][B]).  rs: x, y are real storage double[dim][B]
 // (the solve), else complex128 blocks (ed_batch_apply).
-static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void* y, bool rs) {
+static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void* y, bool rs,
+                    std::vector<double>* dot = nullptr) {
   ed_ham* h = bt->h;
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
@@ -492,7 +559,9 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
     bb.type[bb.nb] = (uint8_t)(h->bs.type[q] & 1);
     ++bb.nb;
   }
-  const size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)BH_ROWS * std::max(bb.nb, 1));
+  size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)BH_ROWS * std::max(bb.nb, 1));
+  if (dot) smem = ((smem + 7) & ~(size_t)7) + sizeof(double) * 2 * (size_t)B + 8;
+  if (smem > 96 * 1024) return ed_fail(ED_ENOTSUP, "batch too wide for the batched H.v");
   static bool attr = false;
   if (!attr) {
     ED_CUDA(cudaFuncSetAttribute(k_batch_hv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
@@ -506,15 +575,25 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   if (per_sm < 1) per_sm = 1;
   const int64_t tiles = (bt->dim + BH_ROWS - 1) / BH_ROWS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
+  if (dot) ED_TRY(batch_reduce_buf(bt, (size_t)2 * B * grid + (size_t)2 * B));
   if (rs)
     k_batch_hv<true><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim,
                                                            B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
-                                                           h->bs.chalf[1]);
+                                                           h->bs.chalf[1], dot ? bt->d_red : nullptr);
   else
     k_batch_hv<false><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y,
                                                             bt->dim, B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb,
-                                                            h->bs.chalf[0], h->bs.chalf[1]);
+                                                            h->bs.chalf[0], h->bs.chalf[1], nullptr);
   ED_CHECK_LAUNCH(ctx);
+  if (dot) {
+    const int64_t items = 2 * (int64_t)B;
+    double* res = bt->d_red + (size_t)items * grid;
+    k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res);
+    ED_CHECK_LAUNCH(ctx);
+    ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));
+    dot->assign(bt->h_red, bt->h_red + items);
+  }
   return ED_OK;
 }
 
@@ -673,11 +752,12 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     ++its;
     const int64_t colA = dim * (int64_t)A;
     for (int j = k; j < m; ++j) {
-      if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true)) != ED_OK) goto cleanup;
+      // H.v with the local projection coefficient a_b = v_j^T w (and ||w||^2)
+      // reduced in the same pass
+      if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true, &out)) != ED_OK) goto cleanup;
       bt->nhv++;
-      // local projection coefficients: a_b = v_j^H w, beta_{j-1}
-      std::vector<const double*> vj(1, col[j]);
-      if ((rc = batch_dots(bt, A, vj, w, true, out)) != ED_OK) goto cleanup;
+      const double* local_vj = nullptr;
+      const double* local_vjm1 = nullptr;
       {
         std::vector<double> hc((size_t)2 * A);
         const bool three = j > k && j > 0;
@@ -687,31 +767,40 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
           hc[b] = a;
           hc[(size_t)A + b] = three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0;
         }
-        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * 2 * A, cudaMemcpyHostToDevice, ctx->stream);
-        BCols vc;
-        memset(&vc, 0, sizeof(vc));
-        vc.p[0] = col[j];
-        vc.p[1] = three ? col[j - 1] : col[j];
-        k_batch_update<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, three ? 2 : 1, d_coef, w, dim, A);
-        ctx->kernels++;
+        // the local coefficients go to the upper half of d_coef; the first
+        // CGS pass applies them in its own pass over w
+        cudaMemcpyAsync(d_coef + (size_t)64 * A, hc.data(), sizeof(double) * 2 * A, cudaMemcpyHostToDevice,
+                        ctx->stream);
+        local_vj = col[j];
+        local_vjm1 = three ? col[j - 1] : nullptr;
       }
       // full CGS pass (+ DGKS refinement when any realisation needs it)
       std::vector<const double*> vs(col.begin(), col.begin() + j + 1);
       std::vector<double> prevn(A, 0.0);
       for (int pass = 0; pass < 2; ++pass) {
-        if ((rc = batch_dots(bt, A, vs, w, true, out)) != ED_OK) goto cleanup;
+        if ((rc = batch_dots(bt, A, vs, w, true, out, pass == 0 ? local_vj : nullptr, local_vjm1,
+                             d_coef + (size_t)64 * A)) != ED_OK)
+          goto cleanup;
         std::vector<double> hc(out.begin(), out.begin() + (size_t)(j + 1) * A);
         for (int b = 0; b < A; ++b) prevn[b] = std::sqrt(out[(size_t)(j + 1) * A + b]);
         cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
         for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
-        k_batch_update<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A);
-        ctx->kernels++;
+        // update and the new norms in one pass
+        {
+          const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
+          if ((rc = batch_reduce_buf(bt, (size_t)A * nblk + (size_t)A)) != ED_OK) goto cleanup;
+          k_batch_update_norm<<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
+          ctx->kernels++;
+          double* res = bt->d_red + (size_t)A * nblk;
+          k_batch_reduce<<<grid_n(ctx, A, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, A, res);
+          ctx->kernels++;
+          ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)A, cudaMemcpyDeviceToHost, ctx->stream));
+          ED_CUDA(cudaStreamSynchronize(ctx->stream));
+          out.assign(bt->h_red, bt->h_red + A);
+        }
         for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b];
-        // norms after the update
-        std::vector<const double*> none;
-        if ((rc = batch_dots(bt, A, none, w, true, out)) != ED_OK) goto cleanup;
         bool again = false;
         for (int b = 0; b < A; ++b) {
           const double nw = std::sqrt(out[b]);
@@ -731,40 +820,43 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       ctx->kernels++;
     }
     // projected problems, convergence and restart, per active realisation
-    std::vector<int> conv_slots, keep_slots;
+    // (independent small eigenproblems: one host thread each)
+    std::vector<int> conv_slots, keep_slots, is_conv(A, 0);
     Yall.assign((size_t)A * m * l_keep, 0.0);
+#pragma omp parallel for schedule(dynamic, 4)
     for (int b = 0; b < A; ++b) {
-      T.assign((size_t)m * m, 0.0);
+      std::vector<double> Tb((size_t)m * m, 0.0), thb, Yb;
       const double* al = &alpha[(size_t)b * (m + 1)];
       const double* be = &beta[(size_t)b * (m + 1)];
       const double* ar = &arrow[(size_t)b * (m + 1)];
       for (int i = 0; i < k; ++i) {
-        T[(size_t)i * m + i] = al[i];
-        T[(size_t)i * m + k] = T[(size_t)k * m + i] = ar[i];
+        Tb[(size_t)i * m + i] = al[i];
+        Tb[(size_t)i * m + k] = Tb[(size_t)k * m + i] = ar[i];
       }
       for (int jj = k; jj < m; ++jj) {
-        T[(size_t)jj * m + jj] = al[jj];
-        if (jj + 1 < m) T[(size_t)jj * m + jj + 1] = T[(size_t)(jj + 1) * m + jj] = be[jj];
+        Tb[(size_t)jj * m + jj] = al[jj];
+        if (jj + 1 < m) Tb[(size_t)jj * m + jj + 1] = Tb[(size_t)(jj + 1) * m + jj] = be[jj];
       }
-      ed_jacobi_eig(m, T, theta, Y);
+      ed_jacobi_eig(m, Tb, thb, Yb);
       const double bm = be[m - 1];
       int nc = 0;
       for (int i = 0; i < m; ++i) {
-        const double res = std::fabs(bm * Y[(size_t)(m - 1) * m + i]);
-        if (res / std::max(std::fabs(theta[i]), 1e-300) < tol) ++nc; else break;
+        const double res = std::fabs(bm * Yb[(size_t)(m - 1) * m + i]);
+        if (res / std::max(std::fabs(thb[i]), 1e-300) < tol) ++nc; else break;
       }
       for (int i = 0; i < m; ++i)
-        for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = Y[(size_t)i * m + c];
+        for (int c = 0; c < l_keep; ++c) Yall[((size_t)b * m + i) * l_keep + c] = Yb[(size_t)i * m + c];
       const int o = act[b];
       nconv[o] = nc;
-      for (int i = 0; i < nev; ++i) bt->evals[(size_t)o * nev + i] = theta[i];
-      if (nc >= nev || its >= max_it) conv_slots.push_back(b); else keep_slots.push_back(b);
+      for (int i = 0; i < nev; ++i) bt->evals[(size_t)o * nev + i] = thb[i];
+      is_conv[b] = (nc >= nev || its >= max_it) ? 1 : 0;
       // kept Ritz values and arrow couplings for the next cycle
       for (int i = 0; i < l_keep; ++i) {
-        alpha[(size_t)b * (m + 1) + i] = theta[i];
-        arrow[(size_t)b * (m + 1) + i] = bm * Y[(size_t)(m - 1) * m + i];
+        alpha[(size_t)b * (m + 1) + i] = thb[i];
+        arrow[(size_t)b * (m + 1) + i] = bm * Yb[(size_t)(m - 1) * m + i];
       }
     }
+    for (int b = 0; b < A; ++b) (is_conv[b] ? conv_slots : keep_slots).push_back(b);
     // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
     std::vector<double*> outc(freel.begin(), freel.begin() + l_keep);
     {
