@@ -344,12 +344,17 @@ __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, doubl
   }
 }
 
+// out[item] = sum_k partial[item * nblk + k]: one warp per item, lanes over k
+// (coalesced), a fixed shuffle tree (the same order every run).
 __global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int64_t items, double* __restrict__ out) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += stride) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t it = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
     double a = 0.0;
-    for (int k = 0; k < nblk; ++k) a += partial[(size_t)it * nblk + k];
-    out[it] = a;
+    for (int k = lane; k < nblk; k += 32) a += partial[(size_t)it * nblk + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) out[it] = a;
   }
 }
 
@@ -517,7 +522,7 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
   k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk, vj, vjm1, coef);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
-  k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
+  k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
   ED_CHECK_LAUNCH(ctx);
   ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -588,7 +593,7 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   if (dot) {
     const int64_t items = 2 * (int64_t)B;
     double* res = bt->d_red + (size_t)items * grid;
-    k_batch_reduce<<<grid_n(ctx, items, 4), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res);
+    k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res);
     ED_CHECK_LAUNCH(ctx);
     ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
     ED_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -794,7 +799,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
           k_batch_update_norm<<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
           ctx->kernels++;
           double* res = bt->d_red + (size_t)A * nblk;
-          k_batch_reduce<<<grid_n(ctx, A, 4), 256, 0, ctx->stream>>>(bt->d_red, nblk, A, res);
+          k_batch_reduce<<<grid_n(ctx, (int64_t)A * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, A, res);
           ctx->kernels++;
           ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)A, cudaMemcpyDeviceToHost, ctx->stream));
           ED_CUDA(cudaStreamSynchronize(ctx->stream));
