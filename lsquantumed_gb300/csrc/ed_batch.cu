@@ -736,7 +736,6 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   for (int b = 0; b < B; ++b) act[b] = b;
   bt->evals.assign((size_t)B * nev, 0.0);
   bt->errs.assign((size_t)B * nev, 0.0);
-  std::vector<double> theta, Y, T;
   std::vector<double> Yall;
   int k = 0, its = 0, A = B;
   bt->nhv = 0;

@@ -701,48 +701,10 @@ int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits) {
   return ED_OK;
 }
 
-template <int K>
-static int launch_hv_fx64_k(ed_ham* h, const double2* x, double2* y) {
-  ed_ctx* ctx = h->ctx;
-  const ed_basis* b = h->basis;
-  ED_TRY(ensure_fixed_buffers(h));
-  int head = 0;
-  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
-  const int sbits = 62 - head;
-  ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 2 * sizeof(int), ctx->stream));
-  const int g = grid_cap(ctx, b->dim, 256, 8);
-  k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1, nullptr);
-  ED_CHECK_LAUNCH(ctx);
-  k_quantize64<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, sbits, h->d_xq, nullptr);
-  ED_CHECK_LAUNCH(ctx);
-  size_t smem = (size_t)b->rt.total * sizeof(uint32_t);
-  static bool attr_set[5] = {false};
-  if (!attr_set[K]) {
-    ED_CUDA(cudaFuncSetAttribute(k_hv_fx64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(56 * 1024)));
-    attr_set[K] = true;
-  }
-  int per_sm = 0;
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_fx64<K>, 256, smem));
-  if (per_sm < 1) per_sm = 1;
-  k_hv_fx64<K><<<grid_cap(ctx, b->dim, 256, per_sm), 256, smem, ctx->stream>>>(
-      b->d_states, h->d_diag, x, h->d_xq, h->d_gmax, sbits, y, b->dim, b->rt, h->segs, h->bs.chalf[0],
-      h->bs.chalf[1]);
-  ED_CHECK_LAUNCH(ctx);
-  return ED_OK;
-}
-
 static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
   if (h->mode == ED_HAM_CSR && h->d_rowptr) return ed_launch_csr_spmv(h, x, y);
   const bool pb = h->bs.per_bond != 0;
   if (ed_lin_supported(h)) return ed_launch_hv_lin(h, x, y, false, nullptr, false);
-  if (!pb && h->hv_kernel == 2) {
-    switch (h->basis->rt.K) {
-      case 1: return launch_hv_fx64_k<1>(h, x, y);
-      case 2: return launch_hv_fx64_k<2>(h, x, y);
-      case 3: return launch_hv_fx64_k<3>(h, x, y);
-      default: return launch_hv_fx64_k<4>(h, x, y);
-    }
-  }
   if (!pb && h->hv_kernel == 1) {
     switch (h->basis->rt.K) {
       case 1: return launch_hv_fixed_k<1>(h, x, y);

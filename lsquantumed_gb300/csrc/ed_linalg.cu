@@ -577,39 +577,15 @@ int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64
   return ED_OK;
 }
 
-// out_c = sum_i V_i * Y[i*ldY + c], c in [c0, c0+nc), nc <= 8.
-__global__ void __launch_bounds__(256) k_restart_r(const ColPtrsR cp, int m, const double* __restrict__ Y, int ldY,
-                                                   int c0, int nc, const ColPtrs outp, int64_t n) {
-  extern __shared__ double shY[];  // m x 8
-  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) {
-    int i = k / 8, c = k % 8;
-    shY[k] = (c < nc) ? Y[(size_t)i * ldY + c0 + c] : 0.0;
-  }
-  __syncthreads();
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    double ar[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) ar[c] = 0.0;
-    for (int i = 0; i < m; ++i) {
-      const double v = cp.p[i][r];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) ar[c] = fma(v, shY[i * 8 + c], ar[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (c < nc) ((double*)outp.p[c0 + c])[r] = ar[c];
-  }
-}
-
-// The same combination in exact integer arithmetic.  Every column is a unit
-// vector and Y is orthogonal, so |v|, |Y| <= 1: both become 62-bit fixed
+// out_c = sum_i V_i * Y[i*ldY + c] for real storage, in exact integer
+// arithmetic.  Every column is a unit vector and Y is orthogonal, so
+// |v|, |Y| <= 1: both become 62-bit fixed
 // point (v converted in registers, Y on the host), each product is formed
 // exactly in 128 bits (__mul64hi and the low word), the sums are exact (by
 // Cauchy-Schwarz |sum_i v_i Y_ic| <= sqrt(m) < 2^2.5, far inside 128 bits),
-// and each output is rounded once.  On GB300 the integer pipes run far
-// faster than FP64 FMA, which bounds k_restart_r.  A non-finite input entry
-// makes its row's outputs NaN, as the FP64 form would.
+// and each output is rounded once (the FP64 form, k_restart, does 16 x 8
+// rounded FMAs per element and takes about as long on GB300).  A non-finite
+// input entry makes its row's outputs NaN, as the FP64 form would.
 __device__ __forceinline__ long long ed_fx62(double v, bool& bad) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int e = (int)((bits >> 52) & 0x7FF);
