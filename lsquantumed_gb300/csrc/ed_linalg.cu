@@ -577,15 +577,18 @@ int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64
   return ED_OK;
 }
 
-// out_c = sum_i V_i * Y[i*ldY + c] for real storage, in exact integer
-// arithmetic.  Every column is a unit vector and Y is orthogonal, so
-// |v|, |Y| <= 1: both become 62-bit fixed
-// point (v converted in registers, Y on the host), each product is formed
-// exactly in 128 bits (__mul64hi and the low word), the sums are exact (by
-// Cauchy-Schwarz |sum_i v_i Y_ic| <= sqrt(m) < 2^2.5, far inside 128 bits),
-// and each output is rounded once (the FP64 form, k_restart, does 16 x 8
-// rounded FMAs per element and takes about as long on GB300).  A non-finite
-// input entry makes its row's outputs NaN, as the FP64 form would.
+// out_c = sum_i V_i * Y[i*ldY + c] for real storage.  GB300 runs FP64 FMA
+// at a small fraction of its other rates, and the combination is bound by it
+// (16 x 8 FMAs per element: 32 ms at N=30).  So the eight outputs of a group
+// are split between two arithmetic units that work side by side: columns
+// 0..3 in FP64 FMA, columns 4..7 in exact integer arithmetic.  For those,
+// every column is a unit vector and Y is orthogonal, so |v|, |Y| <= 1: both
+// become 62-bit fixed point (v in registers, Y on the host), each product is
+// exact in 128 bits (__mul64hi and the low word), each sum is exact (by
+// Cauchy-Schwarz it stays below sqrt(m), far inside 128 bits) and each output
+// is rounded once.  Measured at N=30: 23 ms against 32 ms for all-FP64 and
+// 32 ms for all-integer.  A non-finite input makes its row's integer
+// outputs NaN, as the FP64 ones become.
 __device__ __forceinline__ long long ed_fx62(double v, bool& bad) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int e = (int)((bits >> 52) & 0x7FF);
@@ -600,23 +603,36 @@ __device__ __forceinline__ long long ed_fx62(double v, bool& bad) {
   return (bits >> 63) ? -(long long)a : (long long)a;
 }
 
-__global__ void __launch_bounds__(256) k_restart_fx(const ColPtrsR cp, int m, const long long* __restrict__ Yq, int c0,
-                                                    int nc, const ColPtrs outp, int64_t n) {
-  __shared__ long long shY[128 * 8];  // m x 8 coefficients of this group
-  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) shY[k] = Yq[(size_t)(k / 8) * 8 + (k % 8)];
+#define RS_NF 4  // outputs per group formed in FP64; the other 8 - RS_NF in integers
+
+__global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, const double* __restrict__ Yd,
+                                                     const long long* __restrict__ Yq, int c0, int nc,
+                                                     const ColPtrs outp, int64_t n) {
+  __shared__ double shY[128 * 8];     // m x 8 coefficients of this group (FP64 columns)
+  __shared__ long long shQ[128 * 8];  // the same, 62-bit fixed point (integer columns)
+  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) {
+    shY[k] = Yd[k];
+    shQ[k] = Yq[k];
+  }
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    unsigned long long lo[8];
-    long long hi[8];
+    double a[RS_NF];
+    unsigned long long lo[8 - RS_NF];
+    long long hi[8 - RS_NF];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) { lo[c] = 0ull; hi[c] = 0ll; }
+    for (int c = 0; c < RS_NF; ++c) a[c] = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8 - RS_NF; ++c) { lo[c] = 0ull; hi[c] = 0ll; }
     bool bad = false;
     for (int i = 0; i < m; ++i) {
-      const long long v = ed_fx62(cp.p[i][r], bad);
+      const double vd = cp.p[i][r];
+      const long long v = ed_fx62(vd, bad);
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const long long y = shY[i * 8 + c];
+      for (int c = 0; c < RS_NF; ++c) a[c] = fma(vd, shY[i * 8 + c], a[c]);
+#pragma unroll
+      for (int c = 0; c < 8 - RS_NF; ++c) {
+        const long long y = shQ[i * 8 + RS_NF + c];
         const unsigned long long pl = (unsigned long long)v * (unsigned long long)y;
         const long long ph = __mul64hi(v, y);
         const unsigned long long s = lo[c] + pl;
@@ -625,12 +641,15 @@ __global__ void __launch_bounds__(256) k_restart_fx(const ColPtrsR cp, int m, co
       }
     }
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if (c < nc) {
+    for (int c = 0; c < RS_NF; ++c)
+      if (c < nc) ((double*)outp.p[c0 + c])[r] = a[c];
+#pragma unroll
+    for (int c = 0; c < 8 - RS_NF; ++c) {
+      if (RS_NF + c < nc) {
         // (hi * 2^64 + lo) * 2^-124
         double d = fma((double)hi[c], 0x1p-60, (double)lo[c] * 0x1p-124);
         if (bad) d = __longlong_as_double(0x7FF8000000000000ll);
-        ((double*)outp.p[c0 + c])[r] = d;
+        ((double*)outp.p[c0 + RS_NF + c])[r] = d;
       }
     }
   }
@@ -643,28 +662,35 @@ int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const do
   ColPtrs op;
   for (int i = 0; i < 128; ++i) op.p[i] = nullptr;
   for (int i = 0; i < l && i < 128; ++i) op.p[i] = (const double2*)out[i];
-  // coefficients as 62-bit fixed point, [group][i][8]
+  // coefficients per group of 8 outputs, [group][i][8]: FP64 and 62-bit fixed point
   const int ngroups = (l + 7) / 8;
-  std::vector<long long> yq((size_t)ngroups * m * 8, 0);
+  const size_t per = (size_t)m * 8;
+  std::vector<double> yd(ngroups * per, 0.0);
+  std::vector<long long> yq(ngroups * per, 0);
   for (int gi = 0; gi < ngroups; ++gi)
     for (int i = 0; i < m; ++i)
       for (int c = 0; c < 8; ++c) {
         const int col = gi * 8 + c;
-        if (col < l) yq[((size_t)gi * m + i) * 8 + c] = std::llround(std::ldexp(Y[(size_t)i * ldY + col], 62));
+        if (col >= l) continue;
+        const double y = Y[(size_t)i * ldY + col];
+        yd[(gi * m + i) * 8 + c] = y;
+        yq[(gi * m + i) * 8 + c] = std::llround(std::ldexp(y, 62));
       }
-  ED_TRY(ed_ensure_reduce(ctx, yq.size() + 16));
-  long long* dY = (long long*)ctx->d_red;
-  ED_CUDA(cudaMemcpyAsync(dY, yq.data(), sizeof(long long) * yq.size(), cudaMemcpyHostToDevice, ctx->stream));
+  ED_TRY(ed_ensure_reduce(ctx, 2 * ngroups * per + 16));
+  double* dYd = ctx->d_red;
+  long long* dYq = (long long*)(ctx->d_red + ngroups * per);
+  ED_CUDA(cudaMemcpyAsync(dYd, yd.data(), sizeof(double) * yd.size(), cudaMemcpyHostToDevice, ctx->stream));
+  ED_CUDA(cudaMemcpyAsync(dYq, yq.data(), sizeof(long long) * yq.size(), cudaMemcpyHostToDevice, ctx->stream));
   int per_sm = 0;
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_fx, 256, 0));
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_mix, 256, 0));
   if (per_sm < 1) per_sm = 1;
   int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
   for (int gi = 0; gi < ngroups; ++gi) {
     const int nc = std::min(8, l - gi * 8);
-    k_restart_fx<<<g, 256, 0, ctx->stream>>>(cp, m, dY + (size_t)gi * m * 8, gi * 8, nc, op, n);
+    k_restart_mix<<<g, 256, 0, ctx->stream>>>(cp, m, dYd + gi * per, dYq + gi * per, gi * 8, nc, op, n);
     ED_CHECK_LAUNCH(ctx);
   }
-  // the host coefficients must outlive the copy
+  // the host coefficients must outlive the copies
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   return ED_OK;
 }
