@@ -211,13 +211,13 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
   std::vector<double> c(j + 1);
   double w2 = 0.0, n2 = 0.0;
   ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
-                       beta_prev, c.data(), &w2, *norig));
+                       beta_prev, c.data(), &w2));
   double n0 = std::sqrt(w2);
   h[j] += a;
   if (three_term) h[j - 1] += beta_prev;
   for (int pass = 0; pass < 2; ++pass) {
     if (pass == 1)
-      ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr, *nw));
+      ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
     ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2));
     for (int i = 0; i <= j; ++i) h[i] += c[i];
     *nw = std::sqrt(n2);

@@ -213,10 +213,8 @@ int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double t
                       double* x2_host);
 int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);
 // Real storage (real-mode solves keep only the real parts of the basis).
-// wbound > 0: ||w|| (a bound on max|w|) before the local step; the odd
-// columns are then dotted in exact integer arithmetic beside FP64 FMAs.
 int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
-                  const double* vjm1, double b, double* h_host, double* wnorm2_host, double wbound = 0.0);
+                  const double* vjm1, double b, double* h_host, double* wnorm2_host);
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
                 double* wnorm2_host);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);

@@ -454,58 +454,14 @@ static ColPtrsR make_cols_r(const double* const* cols, int nv) {
 // partial[item * nblk + blk]: items v0..v0+ng-1 = V_i^T w; item v0+ng = ||w||^2
 // (with_norm).  LOCAL: first w <- w - a vj - b vjm1 (vjm1 may be null),
 // written back.
-// Fixed point for the integer halves of the FP64-bound kernels below:
-// round(v * 2^sh) as int64 (the caller guarantees |v| * 2^sh < 2^62); bad is
-// set for a non-finite v.
-__device__ __forceinline__ long long ed_fx(double v, int sh_total, bool& bad) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const int e = (int)((bits >> 52) & 0x7FF);
-  if (e == 0x7FF) { bad = true; return 0; }
-  if (e == 0) return 0;
-  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-  const int sh = e - 1075 + sh_total;  // v * 2^sh_total = mant * 2^(e - 1075 + sh_total)
-  unsigned long long q;
-  if (sh >= 0) q = mant << sh;
-  else if (sh > -63) q = (mant + (1ull << (-sh - 1))) >> (-sh);
-  else q = 0;
-  return (bits >> 63) ? -(long long)q : (long long)q;
-}
-
-// 128-bit exact multiply-accumulate of two int64.
-__device__ __forceinline__ void ed_mac128(long long x, long long y, unsigned long long& lo, long long& hi) {
-  const unsigned long long pl = (unsigned long long)x * (unsigned long long)y;
-  const long long ph = __mul64hi(x, y);
-  const unsigned long long s = lo + pl;
-  hi += ph + (s < pl ? 1 : 0);
-  lo = s;
-}
-
-__device__ __forceinline__ double ed_i128_to_double(long long hi, unsigned long long lo) {
-  return fma((double)hi, 0x1p64, (double)lo);
-}
-
-// partial[item * nblk + blk]: items v0..v0+ng-1 = V_i^T w; item v0+ng = ||w||^2
-// (with_norm).  LOCAL: first w <- w - a vj - b vjm1 (vjm1 may be null),
-// written back.  MIX: the odd columns are dotted in exact integer arithmetic
-// beside the FP64 FMAs of the even ones (GB300's FP64 FMA rate bounds this
-// kernel; its integer pipes are a second, independent unit).  v (a unit
-// vector) is 62-bit fixed point, w is fixed point against 2^wexp >= max|w|
-// (60 bits), each product is exact in 128 bits, and every 16 rows the exact
-// partial sum is rounded once into FP64.
-template <int G, bool LOCAL, bool MIX>
+template <int G, bool LOCAL>
 __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot_r(const ColPtrsR cp, int v0, int ng, double* __restrict__ w,
                                                                int64_t n, const double* __restrict__ vj, double a,
                                                                const double* __restrict__ vjm1, double b, int with_norm,
-                                                               double* __restrict__ partial, int nblk, int wexp) {
+                                                               double* __restrict__ partial, int nblk) {
   double acc[G + 1];
 #pragma unroll
   for (int k = 0; k <= G; ++k) acc[k] = 0.0;
-  unsigned long long lo[G / 2];
-  long long hi[G / 2];
-#pragma unroll
-  for (int k = 0; k < G / 2; ++k) { lo[k] = 0ull; hi[k] = 0ll; }
-  bool bad = false;
-  int since = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
     double wv = w[r];
@@ -514,39 +470,10 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot_r(const ColPtrsR cp
       if (vjm1) wv = fma(-b, vjm1[r], wv);
       w[r] = wv;
     }
-    if (MIX) {
-      const long long wq = ed_fx(wv, 60 - wexp, bad);
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        if (g < ng) {
-          const double v = cp.p[v0 + g][r];
-          if (g & 1) ed_mac128(ed_fx(v, 62, bad), wq, lo[g / 2], hi[g / 2]);
-          else acc[g] = fma(v, wv, acc[g]);
-        }
-      }
-      if (++since == 16) {  // 16 products of at most 2^122 each: flush before 2^127
-        since = 0;
-#pragma unroll
-        for (int k = 0; k < G / 2; ++k) {
-          acc[2 * k + 1] += ed_i128_to_double(hi[k], lo[k]);
-          lo[k] = 0ull;
-          hi[k] = 0ll;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int g = 0; g < G; ++g)
-        if (g < ng) acc[g] = fma(cp.p[v0 + g][r], wv, acc[g]);
-    }
+    for (int g = 0; g < G; ++g)
+      if (g < ng) acc[g] = fma(cp.p[v0 + g][r], wv, acc[g]);
     if (with_norm) acc[G] = fma(wv, wv, acc[G]);
-  }
-  if (MIX) {
-    const double unit = ldexp(1.0, wexp - 122);  // one unit of v * w in fixed point
-#pragma unroll
-    for (int k = 0; k < G / 2; ++k) {
-      acc[2 * k + 1] = (acc[2 * k + 1] + ed_i128_to_double(hi[k], lo[k])) * unit;
-      if (bad) acc[2 * k + 1] = __longlong_as_double(0x7FF8000000000000ll);
-    }
   }
   __shared__ double sh[(G + 1) * 32];
   ed_block_reduce<G + 1>(acc, sh);
@@ -562,36 +489,23 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot_r(const ColPtrsR cp
 // when vj is given: w <- w - a vj - b vjm1 first, in the same pass as the
 // first group of dots).
 int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
-                  const double* vjm1, double b, double* h_host, double* wnorm2_host, double wbound) {
+                  const double* vjm1, double b, double* h_host, double* wnorm2_host) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
   const int items = nv + 1;
   ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + items));
   ColPtrsR cp = make_cols_r(cols, nv);
-  // the integer half needs a bound on max|w| after the local step
-  const bool mix = wbound > 0.0 && std::isfinite(wbound);
-  const int wexp = mix ? std::ilogb(wbound + std::fabs(a) + std::fabs(b)) + 2 : 0;
   const int ngroups = std::max(1, (nv + ED_GROUP_R - 1) / ED_GROUP_R);
   for (int gidx = 0; gidx < ngroups; ++gidx) {
     const int v0 = gidx * ED_GROUP_R;
     const int ng = std::max(0, std::min(ED_GROUP_R, nv - v0));
     const int last = gidx == ngroups - 1;
-    const bool loc = gidx == 0 && vj;
-    const double* pj = loc ? vj : nullptr;
-    const double* pjm1 = loc ? vjm1 : nullptr;
-    const double aa = loc ? a : 0.0, bb = loc ? b : 0.0;
-    if (loc && mix)
-      k_multidot_r<ED_GROUP_R, true, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(
-          cp, v0, ng, w, n, pj, aa, pjm1, bb, last, ctx->d_red, nblk, wexp);
-    else if (loc)
-      k_multidot_r<ED_GROUP_R, true, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(
-          cp, v0, ng, w, n, pj, aa, pjm1, bb, last, ctx->d_red, nblk, 0);
-    else if (mix)
-      k_multidot_r<ED_GROUP_R, false, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(
-          cp, v0, ng, w, n, nullptr, 0.0, nullptr, 0.0, last, ctx->d_red, nblk, wexp);
+    if (gidx == 0 && vj)
+      k_multidot_r<ED_GROUP_R, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, vj, a, vjm1, b, last,
+                                                                              ctx->d_red, nblk);
     else
-      k_multidot_r<ED_GROUP_R, false, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(
-          cp, v0, ng, w, n, nullptr, 0.0, nullptr, 0.0, last, ctx->d_red, nblk, 0);
+      k_multidot_r<ED_GROUP_R, false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, nullptr, 0.0, nullptr,
+                                                                               0.0, last, ctx->d_red, nblk);
     ED_CHECK_LAUNCH(ctx);
   }
   std::vector<double> out(items);
@@ -601,44 +515,34 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
   return ED_OK;
 }
 
-// w <- w - sum_i V_i h_i; partial ||w||^2.  MIX: the odd columns go through
-// exact integer arithmetic beside the FP64 FMAs of the even ones (as in
-// k_multidot_r): v as 62-bit fixed point, h_i against 2^hexp >= max|h_odd|
-// (60 bits, hq precomputed), their sum exact in 128 bits (at most 16 odd
-// columns: below 2^125) and rounded once before it is subtracted.
-template <bool MIX>
+// w <- w - sum_i V_i h_i; partial ||w||^2.  Two rows per thread, columns
+// unrolled by four.
 __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, int nv, const double* __restrict__ h,
-                                                             const long long* __restrict__ hq, int hexp,
                                                              double* __restrict__ w, int64_t n,
                                                              double* __restrict__ partial) {
   __shared__ double sh_h[128];
-  __shared__ long long sh_q[128];
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    sh_h[i] = h[i];
-    if (MIX) sh_q[i] = hq[i];
-  }
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) sh_h[i] = h[i];
   __syncthreads();
-  const double unit = MIX ? ldexp(1.0, hexp - 122) : 0.0;
   double acc[1] = {0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    double wv = w[r];
-    if (MIX) {
-      unsigned long long lo = 0ull;
-      long long hi = 0ll;
-      bool bad = false;
-      for (int i = 0; i < nv; i += 2) {
-        wv = fma(-cp.p[i][r], sh_h[i], wv);
-        if (i + 1 < nv) ed_mac128(ed_fx(cp.p[i + 1][r], 62, bad), sh_q[i + 1], lo, hi);
-      }
-      wv = fma(-ed_i128_to_double(hi, lo), unit, wv);
-      if (bad) wv = __longlong_as_double(0x7FF8000000000000ll);
-    } else {
+  for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < n; r0 += 2 * stride) {
+    const int64_t r1 = r0 + stride;
+    const bool has1 = r1 < n;
+    double w0 = w[r0];
+    double w1 = has1 ? w[r1] : 0.0;
 #pragma unroll 4
-      for (int i = 0; i < nv; ++i) wv = fma(-cp.p[i][r], sh_h[i], wv);
+    for (int i = 0; i < nv; ++i) {
+      const double* col = cp.p[i];
+      const double c = sh_h[i];
+      w0 = fma(-col[r0], c, w0);
+      if (has1) w1 = fma(-col[r1], c, w1);
     }
-    w[r] = wv;
-    acc[0] = fma(wv, wv, acc[0]);
+    w[r0] = w0;
+    acc[0] = fma(w0, w0, acc[0]);
+    if (has1) {
+      w[r1] = w1;
+      acc[0] = fma(w1, w1, acc[0]);
+    }
   }
   __shared__ double shr[32];
   ed_block_reduce<1>(acc, shr);
@@ -649,25 +553,14 @@ int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_
                 double* wnorm2_host) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
-  ED_TRY(ed_ensure_reduce(ctx, (size_t)nblk + 4 + 256));
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)nblk + 4 + 128));
   double* h_dev = ctx->d_red + nblk + 2;
-  long long* q_dev = (long long*)(h_dev + 128);
-  // integer half for the odd columns when there are at most 16 of them
-  double hmax = 0.0;
-  for (int i = 1; i < nv; i += 2) hmax = std::max(hmax, std::fabs(h_host[i]));
-  const bool mix = nv >= 2 && nv <= 32 && hmax > 0.0 && std::isfinite(hmax);
-  const int hexp = mix ? std::ilogb(hmax) + 2 : 0;
-  std::vector<long long> hq(128, 0);
-  if (mix)
-    for (int i = 1; i < nv; i += 2) hq[i] = std::llround(std::ldexp(h_host[i], 60 - hexp));
   ED_CUDA(cudaMemcpyAsync(h_dev, h_host, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
-  if (mix) ED_CUDA(cudaMemcpyAsync(q_dev, hq.data(), sizeof(long long) * nv, cudaMemcpyHostToDevice, ctx->stream));
   ColPtrsR cp = make_cols_r(cols, nv);
-  if (mix) k_update_r<true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, q_dev, hexp, w, n, ctx->d_red);
-  else k_update_r<false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, nullptr, 0, w, n, ctx->d_red);
+  k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red);
   ED_CHECK_LAUNCH(ctx);
   double out;
-  ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));  // synchronises: hq may go out of scope after this
+  ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));
   if (wnorm2_host) *wnorm2_host = out;
   return ED_OK;
 }
