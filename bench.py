@@ -405,34 +405,41 @@ def run_hv_only(args):
     if args.variant != 'auto':
         H.set_hv_variant(args.variant)
     dim = b.size
-    x = torch.empty(dim, dtype=torch.complex128, device='cuda')
-    x.real.uniform_(-1, 1)
-    if args.real_input:
-        x.imag.zero_()
+    if args.real_storage:
+        x = torch.empty(dim, dtype=torch.float64, device='cuda').uniform_(-1, 1)
+        apply = H.apply_real
     else:
-        x.imag.uniform_(-1, 1)
+        x = torch.empty(dim, dtype=torch.complex128, device='cuda')
+        x.real.uniform_(-1, 1)
+        if args.real_input:
+            x.imag.zero_()
+        else:
+            x.imag.uniform_(-1, 1)
+        apply = H.apply
     x /= torch.linalg.vector_norm(x)
     y = torch.empty_like(x)
     for _ in range(args.warmup):
-        H.apply(x, out=y)
+        apply(x, out=y)
     torch.cuda.synchronize()
     env.profile(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stream = torch.cuda.current_stream()
     e0.record(stream)
     for _ in range(args.steps):
-        H.apply(x, out=y)
+        apply(x, out=y)
     e1.record(stream)
     torch.cuda.synchronize()
     n_hv, ms_hv = env.profile_read()
     env.profile(False)
     pairs = list(map(tuple, lat.nn_pairs)) + (list(map(tuple, lat.nnn_pairs)) if J2 else [])
-    real_mode = args.real_input and args.acc == 'fixed64'
-    bytes_row = hv_bytes_per_row(kbar(N, b.nspins_up, pairs), 'real_gathers' if real_mode else 'complex')
+    real_mode = (args.real_input or args.real_storage) and args.acc == 'fixed64'
+    mode = 'real_storage' if args.real_storage else ('real_gathers' if real_mode else 'complex')
+    bytes_row = hv_bytes_per_row(kbar(N, b.nspins_up, pairs), mode)
     ms = ms_hv / max(n_hv, 1)
     peak, _ = measured_peaks()
     gbs = dim * bytes_row / (ms * 1e-3) / 1e9
     print(json.dumps({'mode': 'hv-only', 'workload': wl, 'acc': args.acc, 'real_input': bool(args.real_input),
+                      'real_storage': bool(args.real_storage),
                       'dim': dim, 'launches': n_hv, 'ms_per_hv': ms,
                       'ms_per_step_events': e0.elapsed_time(e1) / args.steps, 'algorithmic_gbs': gbs,
                       'frac_of_measured_hbm': gbs / peak, 'bytes_per_row': bytes_row,
@@ -641,6 +648,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
+    ap.add_argument('--real-storage', action='store_true',
+                    help='--hv-only on real vectors in real storage (float64, as inside the solve)')
     ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')

@@ -122,6 +122,13 @@ int ed_ham_build_disorder(ed_ham* h, const double* hi_host);
 int ed_ham_apply(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev);
 /* Same with host buffers (copies in and out on the context's stream). */
 int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host);
+/* y = H x for real vectors (double[dim] on the device).  The Hamiltonian is
+ * real symmetric, so this is ed_ham_apply on x + 0i with half the storage and
+ * traffic; the result equals the real part of ed_ham_apply's bit for bit.
+ * Needs the matrix-free two-table kernel (uniform couplings, ED_ACC_FIXED64):
+ * ED_ENOTSUP otherwise.  No counterpart in the reference (PETSc vectors there
+ * are complex128). */
+int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev);
 /* y = H x (device vectors) without allocating any device memory: for
  * callers that cannot let a library call cudaMalloc, e.g. code running under
  * a framework that owns the whole device memory pool, or a loop that cannot

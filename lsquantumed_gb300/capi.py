@@ -67,6 +67,7 @@ SIGNATURES = {
     'ed_ham_build_disorder': [vp, vp],
     'ed_ham_apply': [vp, vp, vp],
     'ed_ham_apply_host': [vp, vp, vp],
+    'ed_ham_apply_real': [vp, vp, vp],
     'ed_ham_apply_noalloc': [vp, vp, vp],
     'ed_ham_build_csr': [vp, P(i64)],
     'ed_ham_set_mode': [vp, i32],

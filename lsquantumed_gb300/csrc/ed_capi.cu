@@ -447,6 +447,12 @@ int ed_ham_apply(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev) {
   return ed_launch_hv(h, (const double2*)x_dev, (double2*)y_dev);
 }
 
+int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev) {
+  if (!h || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
+  if (x_dev == y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
+  return ed_launch_hv_r(h, x_dev, y_dev);
+}
+
 int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host) {
   if (!h || !x_host || !y_host) return ed_fail(ED_EINVAL, "null argument");
   ed_ctx* ctx = h->ctx;

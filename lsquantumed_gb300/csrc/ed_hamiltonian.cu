@@ -722,8 +722,18 @@ static int launch_hv_dispatch(ed_ham* h, const double2* x, double2* y) {
 }
 
 int ed_launch_hv_r(ed_ham* h, const double* x, double* y) {
-  if (!ed_lin_supported(h)) return ed_fail(ED_ENOTSUP, "real-storage H.v needs the two-table kernel");
-  return ed_launch_hv_lin(h, x, y, false, nullptr, true);
+  if (!ed_lin_supported(h)) return ed_fail(ED_ENOTSUP, "real-storage H.v needs the two-table fixed-point kernel");
+  ed_ctx* ctx = h->ctx;
+  if (!ctx->profiling) return ed_launch_hv_lin(h, x, y, false, nullptr, true);
+  cudaEvent_t e0, e1;
+  ED_CUDA(cudaEventCreate(&e0));
+  ED_CUDA(cudaEventCreate(&e1));
+  ED_CUDA(cudaEventRecord(e0, ctx->stream));
+  int rc = ed_launch_hv_lin(h, x, y, false, nullptr, true);
+  ED_CUDA(cudaEventRecord(e1, ctx->stream));
+  ctx->prof_events.push_back(e0);
+  ctx->prof_events.push_back(e1);
+  return rc;
 }
 
 int ed_launch_hv(ed_ham* h, const double2* x, double2* y) {

@@ -123,11 +123,11 @@ __device__ __forceinline__ void gather(const L2* __restrict__ xq, u32 g, bool on
   }
 }
 
-template <bool CHECK, bool RX, bool DOT>
+template <bool CHECK, bool RX, bool DOT, bool RIO>
 __device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                      i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
-                                     double c0c, double c1c, double s1, double s2, double* dacc, bool rio) {
+                                     double c0c, double c1c, double s1, double s2, double* dacc) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const u32 s = states[r];
@@ -140,43 +140,61 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     BONDS
     const double d = diag[r];
     D2 xv;
-    if (rio) { xv.x = ((const double*)x)[r]; xv.y = 0.0; } else xv = x[r];
+    if (RIO) { xv.x = ((const double*)x)[r]; xv.y = 0.0; } else xv = x[r];
     const double s0r = (double)a0 * s1 * s2, s0i = (double)a1 * s1 * s2;
     const double s1r = (double)a2 * s1 * s2, s1i = (double)a3 * s1 * s2;
     double yr = fma(d, xv.x, fma(c0c, s0r, c1c * s1r));
     double yi = fma(d, xv.y, fma(c0c, s0i, c1c * s1i));
     if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
-    if (rio) ((double*)y)[r] = yr;
+    if (RIO) ((double*)y)[r] = yr;
     else { D2 o; o.x = yr; o.y = yi; y[r] = o; }
     if (DOT) {
-      dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
-      dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
-      dacc[2] = fma(yr, yr, fma(yi, yi, dacc[2]));
+      if (RIO) {
+        dacc[0] = fma(xv.x, yr, dacc[0]);
+        dacc[2] = fma(yr, yr, dacc[2]);
+      } else {
+        dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
+        dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
+        dacc[2] = fma(yr, yr, fma(yi, yi, dacc[2]));
+      }
     }
   }
 }
 
-template <bool DOT>
+// The checked rows (some input entry is not finite: rare) stay out of line so
+// that their register needs do not weigh on the unchecked path.
+template <bool RX, bool DOT, bool RIO>
+__device__ __noinline__ void rows_checked(const u32* __restrict__ states, const double* __restrict__ diag,
+                                          const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
+                                          i64 dim, const unsigned short* __restrict__ t0s,
+                                          const u32* __restrict__ t1, double c0c, double c1c, double s1, double s2,
+                                          double* dacc) {
+  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+}
+
+// RIO: x and y are real storage (double[dim]); the input is then real, and
+// xq holds only real parts.  Otherwise x is complex and gmax_p[2] == 0 tells
+// that it is real.
+template <bool DOT, bool RIO>
 __device__ __forceinline__ void body(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq,
                                      const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
                                      const unsigned short* __restrict__ t0, const u32* __restrict__ t1, double c0c,
-                                     double c1c, double* __restrict__ partial, int rio_flag) {
+                                     double c1c, double* __restrict__ partial) {
   extern __shared__ unsigned short t0s[];
-  const bool rio = rio_flag != 0;
   for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
   const int e_unit = gmax_p[0] - 1022 - sbits;
   const double s1 = __longlong_as_double((i64)(e_unit / 2 + 1023) << 52);
   const double s2 = __longlong_as_double((i64)(e_unit - e_unit / 2 + 1023) << 52);
   double dacc[3] = {0.0, 0.0, 0.0};
-  const bool rx = gmax_p[2] == 0;
+  const bool rx = RIO || gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) rows<true, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
-    else rows<true, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
+    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
   } else {
-    if (rx) rows<false, true, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
-    else rows<false, false, DOT>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc, rio);
+    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -197,23 +215,37 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   }
 }
 
-#define JIT_KERNEL(NAME, DOT, MINB)                                                                       \
+#define JIT_KERNEL(NAME, DOT, RIO, MINB)                                                                  \
   extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
-      const u32* t1, double c0c, double c1c, double* partial, int rio) {                                    \
-    body<DOT>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial, rio);                  \
+      const u32* t1, double c0c, double c1c, double* partial) {                                             \
+    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);                  \
   }
-// register budgets: all loads of a row in flight (2 blocks of 256 per SM), or 4 blocks per SM
-JIT_KERNEL(k_hv_jit_b2, false, 1)
-JIT_KERNEL(k_hv_jit_dot_b2, true, 1)
-JIT_KERNEL(k_hv_jit_b4, false, 4)
-JIT_KERNEL(k_hv_jit_dot_b4, true, 4)
+// register budgets: 2, 3 or 4 blocks of 256 per SM (128, 80 or 64 registers);
+// _r: real storage of x and y
+JIT_KERNEL(k_hv_jit_b2, false, false, 2)
+JIT_KERNEL(k_hv_jit_dot_b2, true, false, 2)
+JIT_KERNEL(k_hv_jit_b3, false, false, 3)
+JIT_KERNEL(k_hv_jit_dot_b3, true, false, 3)
+JIT_KERNEL(k_hv_jit_b4, false, false, 4)
+JIT_KERNEL(k_hv_jit_dot_b4, true, false, 4)
+JIT_KERNEL(k_hv_jit_b2_r, false, true, 2)
+JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 2)
+JIT_KERNEL(k_hv_jit_b3_r, false, true, 3)
+JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 3)
+JIT_KERNEL(k_hv_jit_b4_r, false, true, 4)
+JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
 )";
+
+// Register budgets of the generated kernels, by the budget index of
+// ed_jit_launch: 0, 1, 2 = two, four, three blocks of 256 per SM.
+const int kJitBudgets = 3;
+const char* const kJitBudgetSuffix[kJitBudgets] = {"b2", "b4", "b3"};
 
 struct JitModule {
   bool ok = false;
-  CUfunction fn[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [budget][dot]
-  int per_sm[2][2] = {{1, 1}, {1, 1}};
+  CUfunction fn[kJitBudgets][2][2] = {};  // [budget][dot][real storage]
+  int per_sm[kJitBudgets][2][2] = {};
 };
 
 std::map<std::tuple<int, uint64_t>, JitModule> g_modules;
@@ -346,21 +378,22 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
         cache_write(dir, path, cubin);
       }
       CUmodule m = nullptr;
-      const char* names[2][2] = {{"k_hv_jit_b2", "k_hv_jit_dot_b2"}, {"k_hv_jit_b4", "k_hv_jit_dot_b4"}};
       bool got = g_drv.load(&m, cubin.data()) == CUDA_SUCCESS;
-      for (int bg = 0; bg < 2 && got; ++bg)
-        for (int k = 0; k < 2 && got; ++k) got = g_drv.get(&jm.fn[bg][k], m, names[bg][k]) == CUDA_SUCCESS;
+      const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
+      for (int bg = 0; bg < kJitBudgets && got; ++bg)
+        for (int k = 0; k < 2 && got; ++k)
+          for (int ri = 0; ri < 2 && got; ++ri) {
+            const std::string fname = std::string(k ? "k_hv_jit_dot_" : "k_hv_jit_") + kJitBudgetSuffix[bg] +
+                                      (ri ? "_r" : "");
+            got = g_drv.get(&jm.fn[bg][k][ri], m, fname.c_str()) == CUDA_SUCCESS;
+            int ps = 0;
+            if (got && (g_drv.occupancy(&ps, jm.fn[bg][k][ri], 256, smem) != CUDA_SUCCESS || ps < 1)) ps = 1;
+            jm.per_sm[bg][k][ri] = ps;
+          }
       if (!got) {
         g_modules[key] = jm;
         return ed_fail(ED_ENOTSUP, "loading the compiled H.v module failed");
       }
-      const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
-      for (int bg = 0; bg < 2; ++bg)
-        for (int k = 0; k < 2; ++k) {
-          int ps = 0;
-          if (g_drv.occupancy(&ps, jm.fn[bg][k], 256, smem) != CUDA_SUCCESS || ps < 1) ps = 1;
-          jm.per_sm[bg][k] = ps;
-        }
       jm.ok = true;
       it = g_modules.emplace(key, jm).first;
     }
@@ -368,9 +401,10 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
     mod = &it->second;
   }
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
+  if (budget < 0 || budget >= kJitBudgets) return ed_fail(ED_EINVAL, "unknown register budget");
   int64_t g = (b->dim + 255) / 256;
-  const int bg = budget ? 1 : 0;
-  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[bg][dot ? 1 : 0]));
+  const int bg = budget, kd = dot ? 1 : 0, ri = rio ? 1 : 0;
+  g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[bg][kd][ri]));
   const int nblk = (int)g;
   if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
   const uint32_t* states = b->d_states;
@@ -382,9 +416,8 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   const uint32_t* t1 = b->d_lin_t1;
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
-  int rio_flag = rio ? 1 : 0;
-  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial, &rio_flag};
-  CUresult r = g_drv.launch(mod->fn[bg][dot ? 1 : 0], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
+  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  CUresult r = g_drv.launch(mod->fn[bg][kd][ri], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);
   if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");
   ctx->kernels++;

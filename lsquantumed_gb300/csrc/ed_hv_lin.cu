@@ -39,7 +39,7 @@ struct LinSegs {
 struct ed_lin {
   LinSegs segs{};
   int built_nb = -1;
-  int variant[2] = {-1, -1};  // launch variants (plain, with dot) chosen by lin_autotune; -1: not yet
+  int variant[4] = {-1, -1, -1, -1};  // launch variants [2 * dot + real storage] chosen by lin_autotune; -1: not yet
 };
 
 static uint64_t binom(int n, int k) {
@@ -298,10 +298,11 @@ static const LinVariant kLinVariants[] = {
 };
 static const int kNumLinVariants = (int)(sizeof(kLinVariants) / sizeof(kLinVariants[0]));
 
-// Variants kNumLinVariants and +1 are the run-time specialised kernel
-// (ed_hv_jit.cu) with two register budgets.
+// Variants kNumLinVariants + 0, 1, 2 are the run-time specialised kernel
+// (ed_hv_jit.cu) with its three register budgets.
 static const int kJitVariant = kNumLinVariants;
-static const int kNumAllVariants = kNumLinVariants + 2;
+static const int kNumAllVariants = kNumLinVariants + 3;
+static const char* const kJitNames[3] = {"jit", "jit-b4", "jit-b3"};
 static uint64_t lin_signature(const ed_ham* h);
 
 static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sbits, int* nblk_out, bool rio) {
@@ -331,7 +332,7 @@ static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sb
 // Autotuner choices, shared by every operator of the same structure (device,
 // sector, bond words): a second Hamiltonian of a lattice does not time again.
 static std::mutex g_tune_mu;
-static std::map<std::tuple<int, int, int, uint64_t, int>, int> g_tune;
+static std::map<std::tuple<int, int, int, uint64_t, int, int>, int> g_tune;
 
 static uint64_t lin_signature(const ed_ham* h) {
   uint64_t z = 1469598103934665603ull;  // FNV-1a over the segment table and words
@@ -351,10 +352,11 @@ static uint64_t lin_signature(const ed_ham* h) {
 static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, bool rio) {
   ed_lin* L = h->lin;
   ed_ctx* ctx = h->ctx;
-  int& chosen = L->variant[dot ? 1 : 0];
+  int& chosen = L->variant[2 * (dot ? 1 : 0) + (rio ? 1 : 0)];
   chosen = 0;
   if (h->basis->dim < (int64_t)1 << 20) return ED_OK;
-  const auto key = std::make_tuple(ctx->device, h->basis->nspins, h->basis->nup, lin_signature(h), dot ? 1 : 0);
+  const auto key =
+      std::make_tuple(ctx->device, h->basis->nspins, h->basis->nup, lin_signature(h), dot ? 1 : 0, rio ? 1 : 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -402,7 +404,7 @@ int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out,
   int sbits = 0;
   if (rio) ED_TRY(ed_fx64_quantize_r(h, (const double*)x, &sbits));
   else ED_TRY(ed_fx64_quantize(h, (const double2*)x, &sbits));
-  const int which = dot ? 1 : 0;
+  const int which = 2 * (dot ? 1 : 0) + (rio ? 1 : 0);
   if (h->lin->variant[which] < 0) ED_TRY(lin_autotune(h, x, y, sbits, dot, rio));
   return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out, rio);
 }
@@ -413,22 +415,25 @@ int ed_lin_set_variant(ed_ham* h, const char* name) {
   ED_TRY(lin_prepare(h));
   int v = -2;
   if (strcmp(name, "auto") == 0) v = -1;
-  else if (strcmp(name, "jit") == 0) v = kJitVariant;
-  else if (strcmp(name, "jit-b4") == 0) v = kJitVariant + 1;
-  else
-    for (int i = 0; i < kNumLinVariants; ++i)
-      if (strcmp(name, kLinVariants[i].name) == 0) v = i;
+  for (int i = 0; i < 3; ++i)
+    if (strcmp(name, kJitNames[i]) == 0) v = kJitVariant + i;
+  for (int i = 0; i < kNumLinVariants; ++i)
+    if (strcmp(name, kLinVariants[i].name) == 0) v = i;
   if (v == -2) return ed_fail(ED_EINVAL, std::string("unknown H.v variant ") + name);
-  h->lin->variant[0] = h->lin->variant[1] = v;
+  for (int& c : h->lin->variant) c = v;
   return ED_OK;
 }
 
+// The variant last chosen for (dot, real storage); where only one of the two
+// storage forms ran, that one.
 const char* ed_lin_variant_name(const ed_ham* h, int dot) {
-  const int which = dot ? 1 : 0;
-  if (!h->lin || h->lin->variant[which] < 0) return "";
-  if (h->lin->variant[which] == kJitVariant) return "jit";
-  if (h->lin->variant[which] == kJitVariant + 1) return "jit-b4";
-  return kLinVariants[h->lin->variant[which]].name;
+  if (!h->lin) return "";
+  const int base = 2 * (dot ? 1 : 0);
+  int v = h->lin->variant[base + 1];
+  if (v < 0) v = h->lin->variant[base];
+  if (v < 0) return "";
+  if (v >= kJitVariant) return kJitNames[v - kJitVariant];
+  return kLinVariants[v].name;
 }
 
 void ed_lin_invalidate(ed_lin* L) {

@@ -174,7 +174,7 @@ bool ed_lin_supported(const ed_ham* h);
 int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio);
 // The two-table H.v compiled at run time for one operator's bond words
 // (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
-// budget 0: no register limit (2 blocks of 256 per SM); 1: 4 blocks per SM.
+// budget 0, 1, 2: register budget for 2, 4 or 3 blocks of 256 per SM.
 int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
                   int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio);
 void ed_lin_invalidate(ed_lin* L);

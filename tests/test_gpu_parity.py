@@ -281,6 +281,35 @@ def test_hv_real_input(ed, envs, case):
     assert bad == cols
 
 
+@pytest.mark.parametrize('case', [
+    (1, 20, 4, 5, 0, 1.0, 1.0, 0.5, 0.5),
+    (1, 24, 4, 6, 1, 1.0, 0.7, 0.55, 0.55),
+])
+def test_hv_real_storage(ed, envs, case):
+    """Real storage (float64 vectors, the solver's real mode): every launch
+    variant gives the real part of the complex-storage H.v bit for bit, and a
+    non-finite entry reaches exactly the rows that gather it (the checked
+    path of each kernel).  The 4x6 case is above the autotuner's size
+    threshold, so 'auto' times the variants there."""
+    ltype, N, lx, ly, mag, J1, D1, J2, D2 = case
+    env, b, h, M = make_pair(ed, envs, ltype, N, lx, ly, mag, J1, D1, J2, D2)
+    xr = oracle.start_vector(9, b.size).real.copy()
+    ref = h.apply(xr.astype(np.complex128)).cpu().numpy().real
+    assert np.abs(ref - M.apply(xr.astype(np.complex128)).real).max() <= 1e-14 * np.linalg.norm(xr)
+    xbad = xr.copy()
+    xbad[7] = np.nan
+    cols = set(M.scipy()[:, 7].nonzero()[0]) | {7}
+    for v in ('auto', 'u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3'):
+        h.set_hv_variant(v)
+        y = h.apply_real(xr).cpu().numpy()
+        assert np.array_equal(y.view(np.uint64), ref.view(np.uint64)), v
+        y = h.apply_real(xbad).cpu().numpy()
+        assert set(np.nonzero(~np.isfinite(y))[0]) == cols, v
+    h.set_hv_variant('auto')
+    with pytest.raises(ed.InvalidArgument):
+        h.apply_real(xr[:-1])
+
+
 def test_hv_variants_bit_identical(ed, envs):
     """Every launch variant of the two-table H.v (static unroll / register
     budgets, and the kernel compiled at run time for this lattice's bonds)
@@ -291,7 +320,7 @@ def test_hv_variants_bit_identical(ed, envs):
     xc = oracle.start_vector(8, b.size)
     xr = xc.real.astype(np.complex128)
     ref = {}
-    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4'):
+    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3'):
         h.set_hv_variant(v)
         for name, x in (('complex', xc), ('real', xr)):
             y = h.apply(x).cpu().numpy()
