@@ -472,6 +472,7 @@ def run_ours(args):
     def one_solve():
         eps = ed.Solver.SolverInit(H, nev, ncv if ncv else ed.PETSC_DEFAULT)
         ed.Solver.EPSSetTolerances(eps, tol, 0)
+        eps.set_restart_arithmetic(args.restart)
         nconv = ed.Solver.solve(env, eps)
         return eps, nconv
 
@@ -561,6 +562,7 @@ def run_ours(args):
         H2.build_off_diag(env)
         eps2 = ed.Solver.SolverInit(H2, nev, ncv if ncv else ed.PETSC_DEFAULT)
         ed.Solver.EPSSetTolerances(eps2, tol, 0)
+        eps2.set_restart_arithmetic(args.restart)
         eps2.set_initial_vector(start_host)
         ed.Solver.solve(env, eps2)
         vals2 = []
@@ -610,6 +612,7 @@ def run_ours(args):
                      'launches_timed': n_hv},
         'hv_gbs': achieved, 'sisj_all_pairs': sisj, 'outputs': outputs,
         'solver': {'nconv': nconv, 'its': st['its'], 'nhv': st['nhv'] // 1, 'ortho_passes': st['ortho_passes'],
+                   'restart_arithmetic': args.restart,
                    'eigenvalues': evals,
                    'rel_residuals': errs},
         'clocks': clocks, 'cpu_baseline': cpu,
@@ -648,6 +651,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
+    ap.add_argument('--restart', default='auto', choices=('auto', 'fp64', 'pair'),
+                    help='restart-combination products of the real-storage solve (auto: float pairs from 2^22 states)')
     ap.add_argument('--real-storage', action='store_true',
                     help='--hv-only on real vectors in real storage (float64, as inside the solve)')
     ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')

@@ -188,6 +188,18 @@ int ed_eps_set_dimensions(ed_eps* e, int nev, int ncv, int mpd);
 int ed_eps_set_tolerances(ed_eps* e, double tol, int max_it);
 /* Seed of the deterministic start vector (re, im ~ U[-1,1) per entry). */
 int ed_eps_set_seed(ed_eps* e, uint64_t seed);
+/* Arithmetic of the restart combination V Y (the Krylov-Schur restart;
+ * BVMultInPlace in SLEPc) in a real-storage solve (a real start vector and
+ * the two-table H.v).  ED_RESTART_FP64: FP64 FMA beside exact integer
+ * products.  ED_RESTART_PAIR: float-pair products on the FP32 units (each
+ * FP64 value split into hi + lo, error below 2^-45 of |v y| per product;
+ * storage and sums stay FP64), 1.5x faster on GB300, whose FP64 unit bounds
+ * this step.  ED_RESTART_AUTO (default): pairs from 2^22 basis states up.
+ * No counterpart in the reference (FP64 throughout). */
+#define ED_RESTART_AUTO 0
+#define ED_RESTART_FP64 1
+#define ED_RESTART_PAIR 2
+int ed_eps_set_restart_arithmetic(ed_eps* e, int mode);
 /* EPSSetInitialSpace with one vector (normalised by the solver); on_device
  * selects whether v points to device or host memory.  NULL clears it. */
 int ed_eps_set_initial_vector(ed_eps* e, const ed_cplx* v, int on_device);

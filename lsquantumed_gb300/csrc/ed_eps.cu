@@ -41,6 +41,8 @@ struct ed_eps {
   double* w_r = nullptr;
   std::vector<double*> col_r;
   double2* xbuf = nullptr;            // complex128 staging of a real column for host copies
+  int restart_arith = ED_RESTART_AUTO;  // ed_eps_set_restart_arithmetic
+  bool restart_pair = false;            // float-pair restart products in this real-storage solve
 };
 
 void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, std::vector<double>& Y) {
@@ -260,6 +262,8 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
   }
   e->real_storage = true;
   e->real_coeffs = true;
+  e->restart_pair =
+      e->restart_arith == ED_RESTART_PAIR || (e->restart_arith == ED_RESTART_AUTO && n >= ((int64_t)1 << 22));
   std::vector<double*> freelist;
   e->col_r.assign(m + 1, nullptr);
   for (int i = 0; i < e->pool_cols; ++i) {
@@ -332,7 +336,7 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
     }
     std::vector<double*> outc(freelist.begin(), freelist.begin() + l);
     std::vector<const double*> inc(e->col_r.begin(), e->col_r.begin() + m);
-    ED_TRY(ed_restart_combine_r(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n));
+    ED_TRY(ed_restart_combine_r(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n, e->restart_pair));
     std::vector<double*> newcol(m + 1, nullptr);
     for (int c = 0; c < l; ++c) newcol[c] = outc[c];
     newcol[l] = e->col_r[m];
@@ -545,6 +549,14 @@ int ed_eps_set_tolerances(ed_eps* e, double tol, int max_it) {
 int ed_eps_set_seed(ed_eps* e, uint64_t seed) {
   if (!e) return ed_fail(ED_EINVAL, "null solver");
   e->seed = seed;
+  return ED_OK;
+}
+
+int ed_eps_set_restart_arithmetic(ed_eps* e, int mode) {
+  if (!e) return ed_fail(ED_EINVAL, "null solver");
+  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR)
+    return ed_fail(ED_EINVAL, "unknown restart arithmetic");
+  e->restart_arith = mode;
   return ED_OK;
 }
 

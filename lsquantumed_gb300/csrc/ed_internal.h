@@ -218,8 +218,10 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
                 double* wnorm2_host);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);
+// pair: the products in float-pair arithmetic on the FP32 units (see
+// ed_linalg.cu) instead of FP64 FMA beside exact integer products.
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
-                         double* const* out, int64_t n);
+                         double* const* out, int64_t n, bool pair = false);
 int ed_residual_norm2_r(ed_ctx* ctx, const double* hx, const double* x, double theta, int64_t n, double* r2_host,
                         double* x2_host);
 int ed_start_vector_r(ed_ctx* ctx, uint64_t seed, int64_t n, double* v);

@@ -451,6 +451,93 @@ static ColPtrsR make_cols_r(const double* const* cols, int nv) {
   return c;
 }
 
+// ---------------------------------------------------------------------------
+// Float-pair products.  GB300 issues FP64 FMA at about 2 per clock per SM and
+// FP32 FMA many times faster, and the restart combination V Y (16 x 8 FMAs
+// per basis entry) is bound by the FP64 unit.  k_restart_pair keeps storage
+// and the final sums in FP64 but forms the products on the FP32 units: each
+// FP64 value v is read as a float pair hi + lo (integer operations on its
+// bits: hi = the leading 24 significand bits, lo = the next 23 rounded,
+// |v - hi - lo| <= 2^-47 |v|), products are formed exactly to first order
+// (hi*hi exactly with an FMA, the three other terms added) and each thread
+// sums them in a float pair with an error-free two-sum (Knuth's TwoSum).  The
+// error of a product is below 2^-45 of |v y|; FP64 FMA over the 16 terms of
+// an output is bounded by 16 x 2^-53 of the same sum, so the two agree to
+// about 2^-45 relative.  Entries below 2^-126 in magnitude count as zero
+// (below 2^-103 they lose lo); entries of 2^128 or more and non-finite ones
+// give NaN.  For the Gram-Schmidt dots (one product per basis entry, so one
+// split per product) the same arithmetic measured slower than FP64 FMA
+// (6.9 against 5.5 ms at N=30), alone and split with FP64 columns, so those
+// stay FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 ed_pair(double v) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const unsigned int hw = (unsigned int)(bits >> 32), lw = (unsigned int)bits;
+  const unsigned int sign = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  // hi: float exponent e - 1023 + 127 (the 9-bit field wraps correctly in
+  // range), fraction = the top 23 fraction bits of v
+  unsigned int hb = ((__funnelshift_l(lw, hw, 3) - (896u << 23)) & 0x7FFFFFFFu) | sign;
+  // lo: fraction bits 28..6 rounded at bit 5, as (2^E + m ulp) - 2^E exactly
+  // (a carry out of m moves into the exponent, which is the right value)
+  const unsigned int m = (((lw & 0x1FFFFFFFu) >> 5) + 1u) >> 1;
+  const unsigned int base = (unsigned int)(e - 919) << 23;
+  float lo = __fsub_rn(__uint_as_float(base + m), __uint_as_float(base));
+  lo = __uint_as_float(__float_as_uint(lo) | sign);
+  if ((unsigned int)(e - 897) > 253u) hb = e > 1150 ? 0x7FC00000u : sign;
+  if ((unsigned int)(e - 920) > 230u) lo = 0.0f;
+  return make_float2(__uint_as_float(hb), lo);
+}
+
+// (s, c) += a * b for float pairs a, b.
+__device__ __forceinline__ void ed_pair_mac(float2 a, float2 b, float& s, float& c) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  e = __fmaf_rn(a.y, b.y, e);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  c = __fadd_rn(c, __fadd_rn(err, e));
+  s = t;
+}
+
+__device__ __forceinline__ double ed_pair_value(float s, float c) { return (double)s + (double)c; }
+
+// out_c = sum_i V_i Y[i][c] for 8 outputs per launch in float-pair products
+// (Yp: the group's m x 8 coefficients as float pairs).  Measured at N=30:
+// 14.9 ms per group against 32 ms in FP64 FMA, 22 ms with half the outputs
+// in exact integers, and 21.7 ms with three of eight in FP64 beside five in
+// pairs (the FP64 instructions do not overlap the FP32 work here).
+__global__ void __launch_bounds__(256) k_restart_pair(const ColPtrsR cp, int m, const float2* __restrict__ Yp, int c0,
+                                                      int nc, const ColPtrs outp, int64_t n) {
+  __shared__ float2 shY[128 * 8];
+  for (int k = threadIdx.x; k < m * 8; k += blockDim.x) shY[k] = Yp[k];
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    float s[8], c[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s[k] = c[k] = 0.0f;
+    for (int i = 0; i < m; ++i) {
+      const float2 v = ed_pair(cp.p[i][r]);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ed_pair_mac(v, shY[i * 8 + k], s[k], c[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < nc) ((double*)outp.p[c0 + k])[r] = ed_pair_value(s[k], c[k]);
+  }
+}
+
+// A double as a float pair on the host (round to nearest twice: the pair's
+// error is below 2^-48 |v|; coefficients are bounded, |v| <= 2^127).
+static float2 host_pair(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
 // partial[item * nblk + blk]: items v0..v0+ng-1 = V_i^T w; item v0+ng = ||w||^2
 // (with_norm).  LOCAL: first w <- w - a vj - b vjm1 (vjm1 may be null),
 // written back.
@@ -548,6 +635,7 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
   ed_block_reduce<1>(acc, shr);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
 }
+
 
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
                 double* wnorm2_host) {
@@ -656,15 +744,36 @@ __global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, c
 }
 
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
-                         double* const* out, int64_t n) {
+                         double* const* out, int64_t n, bool pair) {
   if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   ColPtrsR cp = make_cols_r(cols, m);
   ColPtrs op;
   for (int i = 0; i < 128; ++i) op.p[i] = nullptr;
   for (int i = 0; i < l && i < 128; ++i) op.p[i] = (const double2*)out[i];
-  // coefficients per group of 8 outputs, [group][i][8]: FP64 and 62-bit fixed point
   const int ngroups = (l + 7) / 8;
   const size_t per = (size_t)m * 8;
+  if (pair) {
+    // coefficients per group of 8 outputs, [group][i][8], as float pairs
+    std::vector<float2> yp(ngroups * per, make_float2(0.0f, 0.0f));
+    for (int gi = 0; gi < ngroups; ++gi)
+      for (int i = 0; i < m; ++i)
+        for (int c = 0; c < 8 && gi * 8 + c < l; ++c) yp[(gi * m + i) * 8 + c] = host_pair(Y[(size_t)i * ldY + gi * 8 + c]);
+    ED_TRY(ed_ensure_reduce(ctx, ngroups * per + 16));
+    float2* dYp = (float2*)ctx->d_red;
+    ED_CUDA(cudaMemcpyAsync(dYp, yp.data(), sizeof(float2) * yp.size(), cudaMemcpyHostToDevice, ctx->stream));
+    int per_sm = 0;
+    ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_pair, 256, 0));
+    if (per_sm < 1) per_sm = 1;
+    int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
+    for (int gi = 0; gi < ngroups; ++gi) {
+      k_restart_pair<<<g, 256, 0, ctx->stream>>>(cp, m, dYp + gi * per, gi * 8, std::min(8, l - gi * 8), op, n);
+      ED_CHECK_LAUNCH(ctx);
+    }
+    // the host coefficients must outlive the copies
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ED_OK;
+  }
+  // coefficients per group of 8 outputs, [group][i][8]: FP64 and 62-bit fixed point
   std::vector<double> yd(ngroups * per, 0.0);
   std::vector<long long> yq(ngroups * per, 0);
   for (int gi = 0; gi < ngroups; ++gi)

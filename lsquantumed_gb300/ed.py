@@ -405,6 +405,15 @@ class EPS:
     def set_seed(self, seed):
         call('ed_eps_set_seed', self._h, int(seed))
 
+    def set_restart_arithmetic(self, mode):
+        """Products of the restart combination V Y in a real-storage solve:
+        'fp64', 'pair' (float pairs on the FP32 units, storage and sums FP64)
+        or 'auto' (pairs from 2^22 basis states up)."""
+        m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR}.get(mode)
+        if m is None:
+            raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
+        call('ed_eps_set_restart_arithmetic', self._h, m)
+
     def set_initial_vector(self, v):
         """EPSSetInitialSpace with one vector: numpy (host) or CUDA tensor."""
         if v is None:
