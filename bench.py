@@ -323,6 +323,7 @@ def run_disorder(args):
     batch_evals = {}
     for mag in sectors:
         bt = ed.DisorderBatch(hams[mag][1], fields)
+        bt.set_restart_arithmetic(args.restart)
         r = bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
         max_err = max(max_err, float(r['errs'].max()))
         bad += int((r['nconv'] < nev).sum())
@@ -362,7 +363,7 @@ def run_disorder(args):
             'scaling': 'strong',  # the 1,536 solves are split over the ranks by seed
             'batched': {'samples_per_s': nsolve / t_batch, 'seconds': t_batch, 'solves': nsolve,
                         'restarts_per_sector': its, 'max_rel_residual': max_err, 'unconverged': bad,
-                        'gpu_launches': launches},
+                        'gpu_launches': launches, 'restart_arithmetic': args.restart},
             'plain': {'samples_per_s': 1.0 / t_plain, 'seconds_per_solve': t_plain,
                       'sample': '%d seeds x %d sectors, one solve at a time' % (nplain, len(sectors))},
             'batched_over_plain': (nsolve / t_batch) * t_plain,

@@ -234,6 +234,9 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
 /* Eigenvector i of realisation b into a contiguous device vector. */
 int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev);
 int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv);
+/* Products of the restart combination, as ed_eps_set_restart_arithmetic
+ * (ED_RESTART_AUTO: float pairs from 2^22 entries of the [dim][B] block up). */
+int ed_batch_set_restart_arithmetic(ed_batch* bt, int mode);
 
 /* ---- measurements: replace SiSj/SzSz/SpSm/SmSp::ExpectVal
  *      (src/spinOperators/correlation.cpp:38-299) --------------------------- */

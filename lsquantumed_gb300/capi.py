@@ -83,6 +83,7 @@ SIGNATURES = {
     'ed_eps_set_tolerances': [vp, dbl, i32],
     'ed_eps_set_seed': [vp, u64],
     'ed_eps_set_restart_arithmetic': [vp, i32],
+    'ed_batch_set_restart_arithmetic': [vp, i32],
     'ed_eps_set_initial_vector': [vp, vp, i32],
     'ed_eps_solve': [vp, P(i32)],
     'ed_eps_get_eigenpair': [vp, i32, P(dbl), P(dbl), vp],

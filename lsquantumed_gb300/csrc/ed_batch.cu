@@ -31,6 +31,7 @@ struct ed_batch {
   double* d_red = nullptr;
   size_t red_cap = 0;
   double* h_red = nullptr;
+  int restart_arith = ED_RESTART_AUTO;  // ed_batch_set_restart_arithmetic
 };
 
 // Per-realisation diagonal, exactly as build_disorder computes it:
@@ -415,26 +416,69 @@ __global__ void k_batch_scale(const double* __restrict__ src, double* __restrict
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k] * s[k % B];
 }
 
-// out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation).
-__global__ void __launch_bounds__(256) k_batch_restart(const BCols V, int m, const double* __restrict__ Y, int l,
-                                                       BCols out, int c0, int nc, int64_t dim, int B) {
-  const int64_t n = dim * B;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    const int b = (int)(k % B);
-    const double* Yb = Y + (size_t)b * m * l;
-    double ar[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) ar[c] = 0.0;
-    for (int i = 0; i < m; ++i) {
-      const double vx = V.p[i][k];
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (c < nc) ar[c] = fma(vx, Yb[(size_t)i * l + c0 + c], ar[c]);
+// out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation),
+// outputs c0..c0+nc-1 (nc <= 8).  A block takes a tile of TB realisations
+// (TB a power of two <= 32; thread = realisation b0 + t % TB, row offset
+// t / TB) and stages their m x 8 coefficients in shared memory, so each
+// coefficient is read from global memory once per block instead of once per
+// entry; the basis loads stay coalesced (TB consecutive entries of a row).
+// PAIR: products in float pairs on the FP32 units (ed_pair; storage and
+// final sums FP64), Y given as float pairs; else FP64 FMA.
+template <bool PAIR>
+__global__ void __launch_bounds__(256) k_batch_restart(const BCols V, int m, const void* __restrict__ Yv, int l,
+                                                       BCols out, int c0, int nc, int64_t dim, int B, int TB) {
+  extern __shared__ double shYd[];  // [TB][m * 8 + 1] (the +1 staggers the banks)
+  const int ld = m * 8 + 1;
+  const int bl = threadIdx.x % TB, rsub = threadIdx.x / TB, rpb = blockDim.x / TB;
+  const int b0 = blockIdx.x * TB;
+  for (int t = threadIdx.x; t < TB * m * 8; t += blockDim.x) {
+    const int tb = t / (m * 8), rem = t % (m * 8), i = rem / 8, q = rem % 8;
+    const int b = b0 + tb;
+    double y = 0.0;
+    if (b < B && q < nc) {
+      const size_t at = ((size_t)b * m + i) * l + c0 + q;
+      y = PAIR ? __longlong_as_double(((const long long*)Yv)[at]) : ((const double*)Yv)[at];
     }
+    shYd[tb * ld + rem] = y;
+  }
+  __syncthreads();
+  const int b = b0 + bl;
+  if (b >= B) return;
+  const double* yb = shYd + bl * ld;
+  for (int64_t row = (int64_t)blockIdx.y * rpb + rsub; row < dim; row += (int64_t)gridDim.y * rpb) {
+    const int64_t k = row * B + b;
+    if (PAIR) {
+      float s[8], c[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (c < nc) ((double*)out.p[c0 + c])[k] = ar[c];
+      for (int q = 0; q < 8; ++q) s[q] = c[q] = 0.0f;
+      for (int i = 0; i < m; ++i) {
+        const float2 v = ed_pair(V.p[i][k]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (q < nc) {
+            const unsigned long long u = (unsigned long long)__double_as_longlong(yb[i * 8 + q]);
+            ed_pair_mac(v, make_float2(__uint_as_float((unsigned int)u), __uint_as_float((unsigned int)(u >> 32))),
+                        s[q], c[q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nc) ((double*)out.p[c0 + q])[k] = ed_pair_value(s[q], c[q]);
+    } else {
+      double ar[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) ar[q] = 0.0;
+      for (int i = 0; i < m; ++i) {
+        const double vx = V.p[i][k];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (q < nc) ar[q] = fma(vx, yb[i * 8 + q], ar[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nc) ((double*)out.p[c0 + q])[k] = ar[q];
+    }
   }
 }
 
@@ -864,15 +908,42 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
     std::vector<double*> outc(freel.begin(), freel.begin() + l_keep);
     {
-      ED_CUDA(cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream));
+      // float-pair products from 2^22 block entries up (the FP64 unit bounds
+      // the FP64 form there), unless FP64 is forced
+      const bool pair = bt->restart_arith == ED_RESTART_PAIR ||
+                        (bt->restart_arith == ED_RESTART_AUTO && colA >= ((int64_t)1 << 22));
+      if (pair) {
+        // pageable source: staged by the time cudaMemcpyAsync returns
+        std::vector<float2> Yp(Yall.size());
+        for (size_t q = 0; q < Yall.size(); ++q) Yp[q] = ed_host_pair(Yall[q]);
+        ED_CUDA(cudaMemcpyAsync(dY, Yp.data(), sizeof(float2) * Yp.size(), cudaMemcpyHostToDevice, ctx->stream));
+      } else {
+        ED_CUDA(cudaMemcpyAsync(dY, Yall.data(), sizeof(double) * Yall.size(), cudaMemcpyHostToDevice, ctx->stream));
+      }
       BCols vin, vout;
       memset(&vin, 0, sizeof(vin));
       memset(&vout, 0, sizeof(vout));
       for (int i = 0; i < m; ++i) vin.p[i] = col[i];
       for (int c = 0; c < l_keep; ++c) vout.p[c] = outc[c];
+      int TB = 1;
+      while (TB < 32 && TB < A) TB *= 2;
+      const int tiles = (A + TB - 1) / TB;
+      const int rows_y = (int)std::max<int64_t>(
+          1, std::min<int64_t>((dim + 256 / TB - 1) / (256 / TB), ((int64_t)ctx->num_sms * 4 + tiles - 1) / tiles));
+      const size_t smem = sizeof(double) * (size_t)TB * (m * 8 + 1);  // <= 127 KB (m <= 62)
+      if (smem > 48 * 1024) {
+        ED_CUDA(cudaFuncSetAttribute(k_batch_restart<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ED_CUDA(cudaFuncSetAttribute(k_batch_restart<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      }
       for (int c0 = 0; c0 < l_keep; c0 += 8) {
-        k_batch_restart<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(vin, m, dY, l_keep, vout, c0,
-                                                                    std::min(8, l_keep - c0), dim, A);
+        const dim3 grid(tiles, rows_y);
+        if (pair)
+          k_batch_restart<true><<<grid, 256, smem, ctx->stream>>>(vin, m, dY, l_keep, vout, c0, std::min(8, l_keep - c0),
+                                                                  dim, A, TB);
+        else
+          k_batch_restart<false><<<grid, 256, smem, ctx->stream>>>(vin, m, dY, l_keep, vout, c0, std::min(8, l_keep - c0),
+                                                                   dim, A, TB);
+        ED_CUDA(cudaGetLastError());
         ctx->kernels++;
       }
     }
@@ -987,6 +1058,14 @@ int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev) {
   k_batch_extract<<<grid_n(ctx, bt->dim), 256, 0, ctx->stream>>>(bt->d_vecs + (size_t)i * bt->dim * bt->B, bt->dim,
                                                                 bt->B, b, (double2*)vec_dev);
   ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+int ed_batch_set_restart_arithmetic(ed_batch* bt, int mode) {
+  if (!bt) return ed_fail(ED_EINVAL, "null batch");
+  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR)
+    return ed_fail(ED_EINVAL, "unknown restart arithmetic");
+  bt->restart_arith = mode;
   return ED_OK;
 }
 

@@ -111,3 +111,51 @@ __device__ __forceinline__ void ed_load_tables(uint32_t* stab, const RankTables&
   for (int i = threadIdx.x; i < rt.total; i += blockDim.x) stab[i] = rt.tab[i];
   __syncthreads();
 }
+
+// Float pairs: an FP64 value v read as hi + lo (two floats) so that products
+// can be formed on the FP32 units.  hi = the leading 24 significand bits of v
+// (truncated), lo = the next 23 (rounded): |v - hi - lo| <= 2^-47 |v|.  Built
+// with integer operations on the bits only.  |v| < 2^-126 gives 0 (below
+// 2^-103 lo is 0); |v| >= 2^128 and non-finite v give NaN.
+__device__ __forceinline__ float2 ed_pair(double v) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const unsigned int hw = (unsigned int)(bits >> 32), lw = (unsigned int)bits;
+  const unsigned int sign = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  // hi: float exponent e - 1023 + 127 (the 9-bit field wraps correctly in
+  // range), fraction = the top 23 fraction bits of v
+  unsigned int hb = ((__funnelshift_l(lw, hw, 3) - (896u << 23)) & 0x7FFFFFFFu) | sign;
+  // lo: fraction bits 28..6 rounded at bit 5, as (2^E + m ulp) - 2^E exactly
+  // (a carry out of m moves into the exponent, which is the right value)
+  const unsigned int m = (((lw & 0x1FFFFFFFu) >> 5) + 1u) >> 1;
+  const unsigned int base = (unsigned int)(e - 919) << 23;
+  float lo = __fsub_rn(__uint_as_float(base + m), __uint_as_float(base));
+  lo = __uint_as_float(__float_as_uint(lo) | sign);
+  if ((unsigned int)(e - 897) > 253u) hb = e > 1150 ? 0x7FC00000u : sign;
+  if ((unsigned int)(e - 920) > 230u) lo = 0.0f;
+  return make_float2(__uint_as_float(hb), lo);
+}
+
+// (s, c) += a * b for float pairs a, b: the product exact to first order (hi*hi
+// exactly with an FMA, the other three terms added; error below 2^-45 |a b|
+// with the splitting), summed into the pair (s, c) by Knuth's TwoSum.
+__device__ __forceinline__ void ed_pair_mac(float2 a, float2 b, float& s, float& c) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  e = __fmaf_rn(a.y, b.y, e);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  c = __fadd_rn(c, __fadd_rn(err, e));
+  s = t;
+}
+
+__device__ __forceinline__ double ed_pair_value(float s, float c) { return (double)s + (double)c; }
+
+// The same split on the host, rounding twice: error below 2^-48 |v| (|v| < 2^127).
+static inline float2 ed_host_pair(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}

@@ -470,40 +470,6 @@ static ColPtrsR make_cols_r(const double* const* cols, int nv) {
 // (6.9 against 5.5 ms at N=30), alone and split with FP64 columns, so those
 // stay FP64.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 ed_pair(double v) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const unsigned int hw = (unsigned int)(bits >> 32), lw = (unsigned int)bits;
-  const unsigned int sign = hw & 0x80000000u;
-  const int e = (int)((hw >> 20) & 0x7FFu);
-  // hi: float exponent e - 1023 + 127 (the 9-bit field wraps correctly in
-  // range), fraction = the top 23 fraction bits of v
-  unsigned int hb = ((__funnelshift_l(lw, hw, 3) - (896u << 23)) & 0x7FFFFFFFu) | sign;
-  // lo: fraction bits 28..6 rounded at bit 5, as (2^E + m ulp) - 2^E exactly
-  // (a carry out of m moves into the exponent, which is the right value)
-  const unsigned int m = (((lw & 0x1FFFFFFFu) >> 5) + 1u) >> 1;
-  const unsigned int base = (unsigned int)(e - 919) << 23;
-  float lo = __fsub_rn(__uint_as_float(base + m), __uint_as_float(base));
-  lo = __uint_as_float(__float_as_uint(lo) | sign);
-  if ((unsigned int)(e - 897) > 253u) hb = e > 1150 ? 0x7FC00000u : sign;
-  if ((unsigned int)(e - 920) > 230u) lo = 0.0f;
-  return make_float2(__uint_as_float(hb), lo);
-}
-
-// (s, c) += a * b for float pairs a, b.
-__device__ __forceinline__ void ed_pair_mac(float2 a, float2 b, float& s, float& c) {
-  const float p = __fmul_rn(a.x, b.x);
-  float e = __fmaf_rn(a.x, b.x, -p);
-  e = __fmaf_rn(a.x, b.y, e);
-  e = __fmaf_rn(a.y, b.x, e);
-  e = __fmaf_rn(a.y, b.y, e);
-  const float t = __fadd_rn(s, p);
-  const float z = __fsub_rn(t, s);
-  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
-  c = __fadd_rn(c, __fadd_rn(err, e));
-  s = t;
-}
-
-__device__ __forceinline__ double ed_pair_value(float s, float c) { return (double)s + (double)c; }
 
 // out_c = sum_i V_i Y[i][c] for 8 outputs per launch in float-pair products
 // (Yp: the group's m x 8 coefficients as float pairs).  Measured at N=30:
@@ -529,13 +495,6 @@ __global__ void __launch_bounds__(256) k_restart_pair(const ColPtrsR cp, int m, 
     for (int k = 0; k < 8; ++k)
       if (k < nc) ((double*)outp.p[c0 + k])[r] = ed_pair_value(s[k], c[k]);
   }
-}
-
-// A double as a float pair on the host (round to nearest twice: the pair's
-// error is below 2^-48 |v|; coefficients are bounded, |v| <= 2^127).
-static float2 host_pair(double v) {
-  const float hi = (float)v;
-  return make_float2(hi, (float)(v - (double)hi));
 }
 
 // partial[item * nblk + blk]: items v0..v0+ng-1 = V_i^T w; item v0+ng = ||w||^2
@@ -757,7 +716,7 @@ int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const do
     std::vector<float2> yp(ngroups * per, make_float2(0.0f, 0.0f));
     for (int gi = 0; gi < ngroups; ++gi)
       for (int i = 0; i < m; ++i)
-        for (int c = 0; c < 8 && gi * 8 + c < l; ++c) yp[(gi * m + i) * 8 + c] = host_pair(Y[(size_t)i * ldY + gi * 8 + c]);
+        for (int c = 0; c < 8 && gi * 8 + c < l; ++c) yp[(gi * m + i) * 8 + c] = ed_host_pair(Y[(size_t)i * ldY + gi * 8 + c]);
     ED_TRY(ed_ensure_reduce(ctx, ngroups * per + 16));
     float2* dYp = (float2*)ctx->d_red;
     ED_CUDA(cudaMemcpyAsync(dYp, yp.data(), sizeof(float2) * yp.size(), cudaMemcpyHostToDevice, ctx->stream));

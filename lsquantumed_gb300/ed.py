@@ -534,6 +534,14 @@ class DisorderBatch:
         call('ed_batch_diag_host', self._h, _p(out))
         return out
 
+    def set_restart_arithmetic(self, mode):
+        """Products of the restart combination: 'fp64', 'pair' or 'auto' (as
+        EPS.set_restart_arithmetic; pairs from 2^22 entries of the block up)."""
+        m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR}.get(mode)
+        if m is None:
+            raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
+        call('ed_batch_set_restart_arithmetic', self._h, m)
+
     def solve(self, nev=1, ncv=0, tol=1e-8, max_it=0, seed=0):
         ev = np.zeros((self.B, nev))
         er = np.zeros((self.B, nev))

@@ -79,6 +79,27 @@ def test_batch_solve_matches_plain_and_dense(ed):
         assert np.linalg.norm(r) <= 1e-8 * abs(res['evals'][k][0])
 
 
+@pytest.mark.parametrize('restart', ['fp64', 'pair'])
+def test_batch_restart_arithmetic(ed, restart):
+    """Both restart arithmetics (FP64 with exact integers; float pairs, the
+    default for large blocks) give the dense spectrum within 1e-10 relative
+    and residuals within tol, on a block with realisations converging at
+    different restarts."""
+    N, mag, B, nev = 12, 1, 9, 2
+    env, b, h, fields = _setup(ed, N, mag, B, seed0=40)
+    bt = ed.DisorderBatch(h, fields)
+    bt.set_restart_arithmetic(restart)
+    res = bt.solve(nev=nev, ncv=12, tol=1e-10, seed=3)
+    assert np.all(res['nconv'] >= nev) and np.all(res['errs'] <= 1e-10)
+    for k in range(B):
+        M = Model(0, N, 1, N, mag, 1.0, 1.0, 0.2, 0.2)
+        M.build(3, fields[k])
+        ev = np.linalg.eigvalsh(M.dense())
+        assert np.allclose(res['evals'][k], ev[:nev], rtol=1e-10, atol=0), (k, res['evals'][k], ev[:nev])
+    with pytest.raises(ed.InvalidArgument):
+        bt.set_restart_arithmetic('fp32')
+
+
 def test_batch_rejects_bad_input(ed):
     env, b, h, fields = _setup(ed, 8, 0, 2)
     with pytest.raises(ValueError):
