@@ -289,6 +289,7 @@ struct BCols {
 // lanes (consecutive b: coalesced) times 256 / Bp row lanes, and the row
 // lanes are summed in shared memory in a fixed order at the end.
 #define BD_MAXV 16
+#define BU_REG 16  // k_batch_update_norm keeps up to this many coefficients in registers
 // With vj: first w <- w - a_b vj - bet_b vjm1 (coef = [a][B], [bet][B]),
 // written back, in the same pass (the local Lanczos projection).
 __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, double* __restrict__ w, int64_t dim,
@@ -375,6 +376,7 @@ __global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, con
 
 // The same update with the new ||w[:, b]||^2 per realisation in the same pass:
 // partial[b * nblk + blk] (blocks over row ranges, lanes as in k_batch_dots).
+template <bool REG>
 __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv, const double* __restrict__ h,
                                                            double* __restrict__ w, int64_t dim, int B,
                                                            double* __restrict__ partial, int nblk) {
@@ -388,13 +390,40 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
     const int b = b0 + lane_b;
     double nrm = 0.0;
     if (lane_r < S && b < B) {
-      for (int64_t r = r0 + lane_r; r < r1; r += S) {
-        const size_t k = (size_t)r * B + b;
-        double wv = w[k];
+      if (REG) {
+        // nv <= BU_REG: this realisation's coefficients in registers, two
+        // rows per pass (two independent FMA chains)
+        double hr[BU_REG];
+#pragma unroll
+        for (int i = 0; i < BU_REG; ++i) hr[i] = i < nv ? h[(size_t)i * B + b] : 0.0;
+        for (int64_t r = r0 + lane_r; r < r1; r += 2 * S) {
+          const int64_t rb = r + S;
+          const bool has1 = rb < r1;
+          const size_t k0 = (size_t)r * B + b, k1 = (size_t)rb * B + b;
+          double w0 = w[k0], w1 = has1 ? w[k1] : 0.0;
+#pragma unroll
+          for (int i = 0; i < BU_REG; ++i) {
+            if (i < nv) {
+              w0 = fma(-V.p[i][k0], hr[i], w0);
+              if (has1) w1 = fma(-V.p[i][k1], hr[i], w1);
+            }
+          }
+          w[k0] = w0;
+          nrm = fma(w0, w0, nrm);
+          if (has1) {
+            w[k1] = w1;
+            nrm = fma(w1, w1, nrm);
+          }
+        }
+      } else {
+        for (int64_t r = r0 + lane_r; r < r1; r += S) {
+          const size_t k = (size_t)r * B + b;
+          double wv = w[k];
 #pragma unroll 4
-        for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
-        w[k] = wv;
-        nrm = fma(wv, wv, nrm);
+          for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
+          w[k] = wv;
+          nrm = fma(wv, wv, nrm);
+        }
       }
     }
     __syncthreads();
@@ -839,7 +868,10 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
         {
           const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
           if ((rc = batch_reduce_buf(bt, (size_t)A * nblk + (size_t)A)) != ED_OK) goto cleanup;
-          k_batch_update_norm<<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
+          if (j + 1 <= BU_REG)
+            k_batch_update_norm<true><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
+          else
+            k_batch_update_norm<false><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
           ctx->kernels++;
           double* res = bt->d_red + (size_t)A * nblk;
           k_batch_reduce<<<grid_n(ctx, (int64_t)A * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, A, res);
