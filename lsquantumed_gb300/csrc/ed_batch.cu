@@ -32,6 +32,10 @@ struct ed_batch {
   size_t red_cap = 0;
   double* h_red = nullptr;
   int restart_arith = ED_RESTART_AUTO;  // ed_batch_set_restart_arithmetic
+  // d_xq / d_gmax already hold the fixed-point copy of this [dim][xq_b] block
+  // (k_batch_scale_quantize); the next batched H.v of it uses them once
+  const void* xq_src = nullptr;
+  int xq_b = 0;
 };
 
 // Per-realisation diagonal, exactly as build_disorder computes it:
@@ -123,28 +127,31 @@ __global__ void k_batch_maxexp_r(const double* __restrict__ x, int64_t n, int* _
   if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(gmax, m);
 }
 
+__device__ __forceinline__ long long batch_fx64_entry(double v, int emax, int sbits) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  long long m = 0;
+  if (e == 0x7FF) {
+    m = (long long)0x8000000000000000ull;
+  } else if (e != 0) {
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    const int sh = e - emax + sbits - 53;
+    unsigned long long a;
+    if (sh >= 0) a = mant << sh;
+    else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);
+    else a = 0;
+    m = (long long)a;
+    if (bits >> 63) m = -m;
+  }
+  return m;
+}
+
 __global__ void k_batch_quantize_r(const double* __restrict__ x, int64_t n, const int* __restrict__ gmax_p, int sbits,
                                    long long* __restrict__ xq) {
   const int emax = *gmax_p;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x[r]);
-    const int e = (int)((bits >> 52) & 0x7FF);
-    long long m = 0;
-    if (e == 0x7FF) {
-      m = (long long)0x8000000000000000ull;
-    } else if (e != 0) {
-      const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-      const int sh = e - emax + sbits - 53;
-      unsigned long long a;
-      if (sh >= 0) a = mant << sh;
-      else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);
-      else a = 0;
-      m = (long long)a;
-      if (bits >> 63) m = -m;
-    }
-    xq[r] = m;
-  }
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+    xq[r] = batch_fx64_entry(x[r], emax, sbits);
 }
 
 // Batched H.v over a [dim][B] block.  A CTA takes a tile of BH_ROWS rows:
@@ -348,14 +355,23 @@ __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, doubl
 
 // out[item] = sum_k partial[item * nblk + k]: one warp per item, lanes over k
 // (coalesced), a fixed shuffle tree (the same order every run).
-__global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int64_t items, double* __restrict__ out) {
+// Items below nsum are summed over the blocks, the others maximised.
+__global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int64_t items, double* __restrict__ out,
+                               int64_t nsum) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t it = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
+    const bool mx = it >= nsum;
     double a = 0.0;
-    for (int k = lane; k < nblk; k += 32) a += partial[(size_t)it * nblk + k];
+    for (int k = lane; k < nblk; k += 32) {
+      const double v = partial[(size_t)it * nblk + k];
+      a = mx ? fmax(a, v) : a + v;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v = __shfl_down_sync(0xffffffffu, a, o);
+      a = mx ? fmax(a, v) : a + v;
+    }
     if (lane == 0) out[it] = a;
   }
 }
@@ -376,11 +392,12 @@ __global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, con
 
 // The same update with the new ||w[:, b]||^2 per realisation in the same pass:
 // partial[b * nblk + blk] (blocks over row ranges, lanes as in k_batch_dots).
+// partial[(B + b) * nblk + blk]: max_r |w[r, b]| over the block's rows.
 template <bool REG>
 __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv, const double* __restrict__ h,
                                                            double* __restrict__ w, int64_t dim, int B,
                                                            double* __restrict__ partial, int nblk) {
-  __shared__ double sh[256];
+  __shared__ double sh[256], shm[256];
   const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
   const int S = 256 / Bp;
   const int lane_b = threadIdx.x % Bp, lane_r = threadIdx.x / Bp;
@@ -389,6 +406,7 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
   for (int b0 = 0; b0 < B; b0 += Bp) {
     const int b = b0 + lane_b;
     double nrm = 0.0;
+    unsigned long long amax = 0ull;  // bits of max |w[r, b]|
     if (lane_r < S && b < B) {
       if (REG) {
         // nv <= BU_REG: this realisation's coefficients in registers, two
@@ -410,9 +428,11 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
           }
           w[k0] = w0;
           nrm = fma(w0, w0, nrm);
+          amax = ed_absmax_bits(amax, w0);
           if (has1) {
             w[k1] = w1;
             nrm = fma(w1, w1, nrm);
+            amax = ed_absmax_bits(amax, w1);
           }
         }
       } else {
@@ -423,16 +443,22 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
           for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
           w[k] = wv;
           nrm = fma(wv, wv, nrm);
+          amax = ed_absmax_bits(amax, wv);
         }
       }
     }
     __syncthreads();
     sh[threadIdx.x] = nrm;
+    shm[threadIdx.x] = __longlong_as_double((long long)amax);
     __syncthreads();
     if (lane_r == 0 && b < B) {
-      double t = 0.0;
-      for (int q = 0; q < S; ++q) t += sh[q * Bp + lane_b];
+      double t = 0.0, mx = 0.0;
+      for (int q = 0; q < S; ++q) {
+        t += sh[q * Bp + lane_b];
+        mx = fmax(mx, shm[q * Bp + lane_b]);
+      }
       partial[(size_t)b * nblk + blockIdx.x] = t;
+      partial[(size_t)(B + b) * nblk + blockIdx.x] = mx;
     }
   }
 }
@@ -443,6 +469,22 @@ __global__ void k_batch_scale(const double* __restrict__ src, double* __restrict
   const int64_t n = dim * B;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k] * s[k % B];
+}
+
+// The same scaling and, in the same pass, the fixed-point copy of dst for the
+// next batched H.v (k_batch_quantize_r's values) with the largest exponent
+// emax found on the host from the per-realisation maxima.
+__global__ void k_batch_scale_quantize(const double* __restrict__ src, double* __restrict__ dst,
+                                       const double* __restrict__ s, int64_t dim, int B, int emax, int sbits,
+                                       long long* __restrict__ xq, int* __restrict__ gmax) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) gmax[0] = emax;
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const double v = src[k] * s[k % B];
+    dst[k] = v;
+    xq[k] = batch_fx64_entry(v, emax, sbits);
+  }
 }
 
 // out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation),
@@ -595,12 +637,22 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
   k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk, vj, vjm1, coef);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
-  k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res);
+  k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res, items);
   ED_CHECK_LAUNCH(ctx);
   ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   out.assign(bt->h_red, bt->h_red + items);
   return ED_OK;
+}
+
+// Scale of the fixed-point H.v input (depends on the bond counts only).
+static int batch_sbits(const ed_batch* bt) {
+  const ed_ham* h = bt->h;
+  int cnt[2] = {0, 0};
+  for (int q = 0; q < h->bs.nb; ++q) cnt[h->bs.type[q] & 1]++;
+  int head = 0;
+  while ((1 << head) < std::max(cnt[0], cnt[1]) + 1) ++head;
+  return 62 - head;
 }
 
 // y = H_b x for the B (active) realisation columns of x, whose diagonals are
@@ -612,23 +664,26 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const int64_t n = bt->dim * B;
-  int cnt[2] = {0, 0};
-  for (int q = 0; q < h->bs.nb; ++q) cnt[h->bs.type[q] & 1]++;
-  int head = 0;
-  while ((1 << head) < std::max(cnt[0], cnt[1]) + 1) ++head;
-  const int sbits = 62 - head;
-  ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
-  if (rs) {
+  const int sbits = batch_sbits(bt);
+  if (rs && bt->xq_src == x && bt->xq_b == B) {
+    // made with x by k_batch_scale_quantize: use it once
+    bt->xq_src = nullptr;
+  } else if (rs) {
+    bt->xq_src = nullptr;
+    ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
     k_batch_maxexp_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax);
     ED_CHECK_LAUNCH(ctx);
     k_batch_quantize_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, sbits,
                                                                  (long long*)bt->d_xq);
+    ED_CHECK_LAUNCH(ctx);
   } else {
+    bt->xq_src = nullptr;
+    ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
     k_batch_maxexp<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double2*)x, n, bt->d_gmax);
     ED_CHECK_LAUNCH(ctx);
     k_batch_quantize<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double2*)x, n, bt->d_gmax, sbits, bt->d_xq);
+    ED_CHECK_LAUNCH(ctx);
   }
-  ED_CHECK_LAUNCH(ctx);
   BatchBonds bb;
   memset(&bb, 0, sizeof(bb));
   for (int q = 0; q < h->bs.nb; ++q) {
@@ -666,7 +721,7 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   if (dot) {
     const int64_t items = 2 * (int64_t)B;
     double* res = bt->d_red + (size_t)items * grid;
-    k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res);
+    k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res, items);
     ED_CHECK_LAUNCH(ctx);
     ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
     ED_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -803,7 +858,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
   int cur = 0;  // dg[cur] holds the active realisations' diagonals
   int rc = ED_OK;
-  std::vector<double> out;
+  std::vector<double> out, wmax;
   std::vector<double> alpha((size_t)B * (m + 1)), beta((size_t)B * (m + 1)), arrow((size_t)B * (m + 1));
   std::vector<int> act(B), nconv(B, 0);
   for (int b = 0; b < B; ++b) act[b] = b;
@@ -867,18 +922,22 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
         // update and the new norms in one pass
         {
           const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
-          if ((rc = batch_reduce_buf(bt, (size_t)A * nblk + (size_t)A)) != ED_OK) goto cleanup;
+          // items: A norms, then A maxima
+          if ((rc = batch_reduce_buf(bt, (size_t)2 * A * nblk + 2 * (size_t)A)) != ED_OK) goto cleanup;
           if (j + 1 <= BU_REG)
             k_batch_update_norm<true><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
           else
             k_batch_update_norm<false><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
           ctx->kernels++;
-          double* res = bt->d_red + (size_t)A * nblk;
-          k_batch_reduce<<<grid_n(ctx, (int64_t)A * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, A, res);
+          double* res = bt->d_red + (size_t)2 * A * nblk;
+          k_batch_reduce<<<grid_n(ctx, (int64_t)A * 64, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, 2 * (int64_t)A,
+                                                                                    res, A);
           ctx->kernels++;
-          ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)A, cudaMemcpyDeviceToHost, ctx->stream));
+          ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * 2 * (size_t)A, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
           ED_CUDA(cudaStreamSynchronize(ctx->stream));
           out.assign(bt->h_red, bt->h_red + A);
+          wmax.assign(bt->h_red + A, bt->h_red + 2 * A);
         }
         for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b];
         bool again = false;
@@ -889,14 +948,31 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
         }
         if (!again) break;
       }
-      // normalise into col[j+1]
+      // normalise into col[j+1]; its fixed-point copy for the next H.v in
+      // the same pass: the largest exponent of the scaled block is the largest
+      // of fl(max_r |w[r, b]| * s_b) over b (rounding is monotonic)
       std::vector<double> sc(A);
+      int emax = 0;
+      bool finite = true;
       for (int b = 0; b < A; ++b) {
         const double nb = beta[(size_t)b * (m + 1) + j];
         sc[b] = nb > 1e-300 ? 1.0 / nb : 0.0;
+        const double mb = wmax[b] * sc[b];
+        if (!std::isfinite(mb)) { finite = false; continue; }
+        uint64_t bits;
+        memcpy(&bits, &mb, sizeof(bits));
+        emax = std::max(emax, (int)((bits >> 52) & 0x7FF));
       }
       cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
-      k_batch_scale<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A);
+      if (finite) {
+        k_batch_scale_quantize<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A, emax,
+                                                                           batch_sbits(bt), (long long*)bt->d_xq,
+                                                                           bt->d_gmax);
+        bt->xq_src = col[j + 1];
+        bt->xq_b = A;
+      } else {
+        k_batch_scale<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A);
+      }
       ctx->kernels++;
     }
     // projected problems, convergence and restart, per active realisation

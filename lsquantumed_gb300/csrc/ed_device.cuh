@@ -106,6 +106,28 @@ __device__ __forceinline__ void ed_block_reduce(double (&v)[NV], double* sh) {
   }
 }
 
+// Running max of |v| kept as the bit pattern of a non-negative double (whose
+// order is that of the unsigned integer): integer instructions only, since
+// FP64 min/max issue on GB300's slow FP64 unit.
+__device__ __forceinline__ unsigned long long ed_absmax_bits(unsigned long long m, double v) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+  return a > m ? a : m;
+}
+
+// Block maximum of v (>= 0) into thread 0's v; sh holds 32 doubles.
+__device__ __forceinline__ void ed_block_max(double& v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < nw ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  }
+}
+
 // Load the rank tables into shared memory (block-cooperative).
 __device__ __forceinline__ void ed_load_tables(uint32_t* stab, const RankTables& rt) {
   for (int i = threadIdx.x; i < rt.total; i += blockDim.x) stab[i] = rt.tab[i];

@@ -202,8 +202,9 @@ static int orthogonalize(ed_eps* e, int j, std::vector<double2>& h, double* nw, 
 // traffic of every projection, update and restart.  The steps are those of
 // orthogonalize_lanczos / eps_solve_impl; only the storage differs.
 // ---------------------------------------------------------------------------
+// *wmax: max_r |w_r| after the last pass.
 static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, double a, double y2,
-                                   std::vector<double>& h, double* nw, double* norig) {
+                                   std::vector<double>& h, double* nw, double* norig, double* wmax) {
   ed_ctx* ctx = e->h->ctx;
   const int64_t n = e->h->basis->dim;
   std::vector<const double*> cols(e->col_r.begin(), e->col_r.begin() + j + 1);
@@ -220,7 +221,7 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
   for (int pass = 0; pass < 2; ++pass) {
     if (pass == 1)
       ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
-    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2));
+    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, wmax));
     for (int i = 0; i <= j; ++i) h[i] += c[i];
     *nw = std::sqrt(n2);
     e->ortho_passes++;
@@ -291,8 +292,8 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
       double pre_y2 = 0.0;
       ED_TRY(ed_launch_hv_dot_any(H, e->col_r[j], e->w_r, true, &pre_a, &pre_y2));
       e->nhv++;
-      double nw, norig;
-      ED_TRY(orthogonalize_lanczos_r(e, j, k, j > 0 ? beta[j - 1] : 0.0, pre_a.x, pre_y2, h, &nw, &norig));
+      double nw, norig, wmax;
+      ED_TRY(orthogonalize_lanczos_r(e, j, k, j > 0 ? beta[j - 1] : 0.0, pre_a.x, pre_y2, h, &nw, &norig, &wmax));
       alpha[j] = h[j];
       if (nw <= 1e-13 * norig) {
         // invariant subspace: continue with a (real) random vector orthogonal to V
@@ -306,7 +307,12 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
           ED_CUDA(cudaMemsetAsync(e->col_r[j + 1], 0, sizeof(double) * (size_t)n, ctx->stream));
         }
       } else {
-        ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw, n));
+        // the next H.v's input is this vector: its fixed-point copy is made in
+        // the same pass (bit-identical to quantizing it afterwards)
+        if (std::isfinite(wmax) && std::isfinite(nw))
+          ED_TRY(ed_scale_quantize_r(H, e->w_r, e->col_r[j + 1], 1.0 / nw, wmax));
+        else
+          ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw, n));
         beta[j] = nw;
       }
     }

@@ -17,6 +17,7 @@
 #include "ed_device.cuh"
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -600,6 +601,7 @@ static int launch_hv_fixed_k(ed_ham* h, const double2* x, double2* y) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   ED_TRY(ensure_fixed_buffers(h));
+  h->xq_src = nullptr;
   ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, sizeof(int), ctx->stream));
   k_quantize<<<grid_cap(ctx, b->dim, 256, 8), 256, 0, ctx->stream>>>(x, b->dim, h->d_xq, h->d_xe, h->d_gmax);
   ED_CHECK_LAUNCH(ctx);
@@ -644,38 +646,84 @@ __global__ void __launch_bounds__(256) k_max_exponent_r(const double* __restrict
   }
 }
 
+// One entry in 64-bit fixed point: v * 2^(sbits - 1 - (emax - 1023)) rounded,
+// or the non-finite sentinel.
+__device__ __forceinline__ long long ed_fx64_entry(double v, int emax, int sbits) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((bits >> 52) & 0x7FF);
+  long long m = 0;
+  if (e == 0x7FF) {
+    m = (long long)0x8000000000000000ull;  // non-finite sentinel
+  } else if (e != 0) {
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    const int sh = e - emax + sbits - 53;
+    unsigned long long a;
+    if (sh >= 0) a = mant << sh;
+    else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);  // round half up in magnitude
+    else a = 0;
+    m = (long long)a;
+    if (bits >> 63) m = -m;
+  }
+  return m;
+}
+
 __global__ void __launch_bounds__(256) k_quantize64_r(const double* __restrict__ x, int64_t dim,
                                                       const int* __restrict__ gmax_p, int sbits,
                                                       long long* __restrict__ xq) {
   const int emax = *gmax_p;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x[r]);
-    const int e = (int)((bits >> 52) & 0x7FF);
-    long long m = 0;
-    if (e == 0x7FF) {
-      m = (long long)0x8000000000000000ull;  // non-finite sentinel
-    } else if (e != 0) {
-      const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-      const int sh = e - emax + sbits - 53;
-      unsigned long long a;
-      if (sh >= 0) a = mant << sh;
-      else if (sh > -63) a = (mant + (1ull << (-sh - 1))) >> (-sh);  // round half up in magnitude
-      else a = 0;
-      m = (long long)a;
-      if (bits >> 63) m = -m;
-    }
-    xq[r] = m;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride)
+    xq[r] = ed_fx64_entry(x[r], emax, sbits);
+}
+
+// dst = src * s and its fixed-point copy with the largest exponent emax
+// (found on the host); the flags of gmax as k_max_exponent_r leaves them for
+// a finite real input.
+__global__ void __launch_bounds__(256) k_scale_quantize_r(const double* __restrict__ src, double* __restrict__ dst,
+                                                          double s, int64_t dim, int emax, int sbits,
+                                                          long long* __restrict__ xq, int* __restrict__ gmax) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    gmax[0] = emax;
+    gmax[1] = 0;
+    gmax[2] = 0;
   }
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const double v = src[r] * s;
+    dst[r] = v;
+    xq[r] = ed_fx64_entry(v, emax, sbits);
+  }
+}
+
+int ed_fx64_sbits(const ed_ham* h) {
+  int head = 0;
+  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
+  return 62 - head;
+}
+
+int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax) {
+  ed_ctx* ctx = h->ctx;
+  const ed_basis* b = h->basis;
+  const double m = src_absmax * s;
+  if (!std::isfinite(m) || !(s > 0.0)) return ed_fail(ED_EINVAL, "scale-quantize needs a finite input and s > 0");
+  ED_TRY(ensure_fixed_buffers(h));
+  uint64_t mb;
+  std::memcpy(&mb, &m, sizeof(mb));
+  const int emax = (int)((mb >> 52) & 0x7FF);
+  const int g = grid_cap(ctx, b->dim, 256, 8);
+  k_scale_quantize_r<<<g, 256, 0, ctx->stream>>>(src, dst, s, b->dim, emax, ed_fx64_sbits(h), (long long*)h->d_xq,
+                                                  h->d_gmax);
+  ED_CHECK_LAUNCH(ctx);
+  h->xq_src = dst;
+  return ED_OK;
 }
 
 int ed_fx64_quantize_r(ed_ham* h, const double* x, int* sbits) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   ED_TRY(ensure_fixed_buffers(h));
-  int head = 0;
-  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
-  *sbits = 62 - head;
+  h->xq_src = nullptr;
+  *sbits = ed_fx64_sbits(h);
   ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 3 * sizeof(int), ctx->stream));
   const int g = grid_cap(ctx, b->dim, 256, 8);
   k_max_exponent_r<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1);
@@ -689,9 +737,8 @@ int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   ED_TRY(ensure_fixed_buffers(h));
-  int head = 0;
-  while ((1 << head) < max_type_count(h->bs) + 1) ++head;
-  *sbits = 62 - head;
+  h->xq_src = nullptr;
+  *sbits = ed_fx64_sbits(h);
   ED_CUDA(cudaMemsetAsync(h->d_gmax, 0, 3 * sizeof(int), ctx->stream));
   const int g = grid_cap(ctx, b->dim, 256, 8);
   k_max_exponent<<<g, 256, 0, ctx->stream>>>(x, b->dim, h->d_gmax, h->d_gmax + 1, h->d_gmax + 2);

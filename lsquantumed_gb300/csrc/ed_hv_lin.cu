@@ -402,8 +402,15 @@ static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, 
 int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio) {
   ED_TRY(lin_prepare(h));
   int sbits = 0;
-  if (rio) ED_TRY(ed_fx64_quantize_r(h, (const double*)x, &sbits));
-  else ED_TRY(ed_fx64_quantize(h, (const double2*)x, &sbits));
+  if (rio && h->xq_src == x) {
+    // the fixed-point copy of x was made with it (ed_scale_quantize_r): use it once
+    sbits = ed_fx64_sbits(h);
+    h->xq_src = nullptr;
+  } else if (rio) {
+    ED_TRY(ed_fx64_quantize_r(h, (const double*)x, &sbits));
+  } else {
+    ED_TRY(ed_fx64_quantize(h, (const double2*)x, &sbits));
+  }
   const int which = 2 * (dot ? 1 : 0) + (rio ? 1 : 0);
   if (h->lin->variant[which] < 0) ED_TRY(lin_autotune(h, x, y, sbits, dot, rio));
   return lin_launch(h, h->lin->variant[which], x, y, dot, sbits, nblk_out, rio);

@@ -140,6 +140,9 @@ struct ed_ham {
   longlong2* d_xq = nullptr;      // 62-bit mantissas, (re, im) per state
   uint16_t* d_xe = nullptr;       // biased exponent per 32-state block
   int* d_gmax = nullptr;          // largest block exponent
+  // d_xq / d_gmax already hold the fixed-point copy of this real vector
+  // (ed_scale_quantize_r); the next two-table H.v of it uses them once
+  const void* xq_src = nullptr;
   int hv_kernel = 2;              // 0: FP64, 1: exact 128-bit, 2: 64-bit fixed point
   BondSegments segs{};
   ed_lin* lin = nullptr;          // tables and bond words of the two-table kernel
@@ -169,6 +172,14 @@ int ed_launch_hv_r(ed_ham* h, const double* x, double* y);
 // zero only the real parts are stored (int64[dim]).  *sbits = the scale.
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
 int ed_fx64_quantize_r(ed_ham* h, const double* x, int* sbits);
+// dst = src * s (real storage) and, in the same pass, dst's fixed-point copy
+// for the next H.v of dst (h->xq_src = dst).  src_absmax = max_r |src_r|
+// (finite): the largest exponent among fl(src_r * s) is that of
+// fl(src_absmax * s), since rounding is monotonic, so the copy equals what
+// ed_fx64_quantize_r would make of dst, bit for bit.
+int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax);
+// sbits of h's fixed-point H.v input (depends on the bond counts only).
+int ed_fx64_sbits(const ed_ham* h);
 bool ed_lin_supported(const ed_ham* h);
 // rio: x and y are real storage (double[dim]) instead of complex128.
 int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio);
@@ -192,7 +203,8 @@ void ed_ham_unique_masks(const ed_ham* h, std::vector<uint32_t>& masks, std::vec
 int ed_ensure_reduce(ed_ctx* ctx, size_t doubles);
 // Sum `items` rows of nblk per-block partials in ctx->d_red (fixed order),
 // copy to host_out and synchronise the stream.
-int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out);
+// The last nmax items are maximised over the blocks instead of summed.
+int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out, int nmax = 0);
 int ed_start_vector(ed_ctx* ctx, uint64_t seed, int64_t n, double2* v, bool real_only = false);
 // *real = every imaginary part of v is zero.
 int ed_is_real(ed_ctx* ctx, const double2* v, int64_t n, bool* real);
@@ -215,8 +227,9 @@ int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);
 // Real storage (real-mode solves keep only the real parts of the basis).
 int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
                   const double* vjm1, double b, double* h_host, double* wnorm2_host);
+// wmax_host (nullable): max_r |w_r| after the update.
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
-                double* wnorm2_host);
+                double* wnorm2_host, double* wmax_host = nullptr);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);
 // pair: the products in float-pair arithmetic on the FP32 units (see
 // ed_linalg.cu) instead of FP64 FMA beside exact integer products.

@@ -73,23 +73,28 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_multidot(const ColPtrs cp, i
 }
 
 // Second stage: out[item] = sum_b partial[item*nblk + b] (fixed order).
-__global__ void k_reduce_items(const double* __restrict__ partial, int nblk, double* __restrict__ out) {
+// Items below nsum are summed over the blocks, the others maximised.
+__global__ void k_reduce_items(const double* __restrict__ partial, int nblk, double* __restrict__ out, int nsum) {
   __shared__ double sh[256];
   const int item = blockIdx.x;
+  const bool mx = item >= nsum;
   double a = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) a += partial[(size_t)item * nblk + b];
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    const double v = partial[(size_t)item * nblk + b];
+    a = mx ? fmax(a, v) : a + v;
+  }
   sh[threadIdx.x] = a;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    if (threadIdx.x < s) sh[threadIdx.x] = mx ? fmax(sh[threadIdx.x], sh[threadIdx.x + s]) : sh[threadIdx.x] + sh[threadIdx.x + s];
     __syncthreads();
   }
   if (threadIdx.x == 0) out[item] = sh[0];
 }
 
-int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out) {
+int ed_finish_reduce(ed_ctx* ctx, int items, int nblk, double* host_out, int nmax) {
   double* out_dev = ctx->d_red + (size_t)items * nblk;
-  k_reduce_items<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, out_dev);
+  k_reduce_items<<<items, 256, 0, ctx->stream>>>(ctx->d_red, nblk, out_dev, items - nmax);
   ED_CHECK_LAUNCH(ctx);
   ED_CUDA(cudaMemcpyAsync(ctx->h_red, out_dev, sizeof(double) * items, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -565,11 +570,12 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
 // unrolled by four.
 __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, int nv, const double* __restrict__ h,
                                                              double* __restrict__ w, int64_t n,
-                                                             double* __restrict__ partial) {
+                                                             double* __restrict__ partial, int with_max) {
   __shared__ double sh_h[128];
   for (int i = threadIdx.x; i < nv; i += blockDim.x) sh_h[i] = h[i];
   __syncthreads();
   double acc[1] = {0.0};
+  unsigned long long amax = 0ull;  // bits of max |w|
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < n; r0 += 2 * stride) {
     const int64_t r1 = r0 + stride;
@@ -585,30 +591,40 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
     }
     w[r0] = w0;
     acc[0] = fma(w0, w0, acc[0]);
+    if (with_max) amax = ed_absmax_bits(amax, w0);
     if (has1) {
       w[r1] = w1;
       acc[0] = fma(w1, w1, acc[0]);
+      if (with_max) amax = ed_absmax_bits(amax, w1);
     }
   }
   __shared__ double shr[32];
   ed_block_reduce<1>(acc, shr);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
+  if (with_max) {
+    __syncthreads();  // shr reused
+    double am = __longlong_as_double((long long)amax);
+    ed_block_max(am, shr);
+    if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = am;
+  }
 }
 
 
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
-                double* wnorm2_host) {
+                double* wnorm2_host, double* wmax_host) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
   const int nblk = red_blocks(ctx, n);
-  ED_TRY(ed_ensure_reduce(ctx, (size_t)nblk + 4 + 128));
-  double* h_dev = ctx->d_red + nblk + 2;
+  const int items = wmax_host ? 2 : 1;
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + 4 + 128));
+  double* h_dev = ctx->d_red + (size_t)items * nblk + 2;
   ED_CUDA(cudaMemcpyAsync(h_dev, h_host, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
   ColPtrsR cp = make_cols_r(cols, nv);
-  k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red);
+  k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, wmax_host ? 1 : 0);
   ED_CHECK_LAUNCH(ctx);
-  double out;
-  ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));
-  if (wnorm2_host) *wnorm2_host = out;
+  double out[2];
+  ED_TRY(ed_finish_reduce(ctx, items, nblk, out, items - 1));
+  if (wnorm2_host) *wnorm2_host = out[0];
+  if (wmax_host) *wmax_host = out[1];
   return ED_OK;
 }
 
