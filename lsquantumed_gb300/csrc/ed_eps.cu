@@ -15,6 +15,7 @@
 #include "ed_internal.h"
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 struct ed_eps {
@@ -40,7 +41,6 @@ struct ed_eps {
   double* pool_r = nullptr;
   double* w_r = nullptr;
   std::vector<double*> col_r;
-  double2* xbuf = nullptr;            // complex128 staging of a real column for host copies
   int restart_arith = ED_RESTART_AUTO;  // ed_eps_set_restart_arithmetic
   bool restart_pair = false;            // float-pair restart products in this real-storage solve
 };
@@ -100,12 +100,10 @@ static void eps_free(ed_eps* e) {
   if (e->w) cudaFree(e->w);
   if (e->pool_r) cudaFree(e->pool_r);
   if (e->w_r) cudaFree(e->w_r);
-  if (e->xbuf) cudaFree(e->xbuf);
   e->pool = nullptr;
   e->w = nullptr;
   e->pool_r = nullptr;
   e->w_r = nullptr;
-  e->xbuf = nullptr;
   e->col.clear();
   e->col_r.clear();
   e->real_storage = false;
@@ -609,16 +607,29 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host) {
   if (i < 0 || i >= e->nrep) return ed_fail(ED_EINVAL, "eigenpair index out of range");
   ed_ctx* ctx = e->h->ctx;
   const int64_t n = e->h->basis->dim;
-  const double2* src = e->real_storage ? nullptr : e->col[i];
   if (e->real_storage) {
-    if (!e->xbuf && cudaMalloc(&e->xbuf, sizeof(double2) * (size_t)n) != cudaSuccess) {
-      cudaGetLastError();
-      return ed_fail(ED_ENOMEM, "no room to stage the eigenvector");
+    // expand to complex128 in halves through a basis column that holds no
+    // Ritz vector (col_r[m], n doubles = n/2 complex entries): no allocation
+    const int m = (int)e->col_r.size() - 1;
+    if (n < 2) {  // one state: a column cannot hold one complex entry
+      double v = 0.0;
+      ED_CUDA(cudaMemcpyAsync(&v, e->col_r[i], sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      ED_CUDA(cudaStreamSynchronize(ctx->stream));
+      std::memcpy(vec_host, &v, sizeof(double));
+      std::memset((char*)vec_host + sizeof(double), 0, sizeof(double));
+      return ED_OK;
     }
-    ED_TRY(ed_real_to_complex(ctx, e->col_r[i], e->xbuf, n));
-    src = e->xbuf;
+    double2* stage = (double2*)e->col_r[m];
+    const int64_t half = n / 2;
+    for (int64_t r0 = 0; r0 < n; r0 += half) {
+      const int64_t c = std::min(half, n - r0);
+      ED_TRY(ed_real_to_complex(ctx, e->col_r[i] + r0, stage, c));
+      ED_CUDA(cudaMemcpyAsync(vec_host + r0, stage, sizeof(double2) * (size_t)c, cudaMemcpyDeviceToHost, ctx->stream));
+      ED_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return ED_OK;
   }
-  ED_CUDA(cudaMemcpyAsync(vec_host, src, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+  ED_CUDA(cudaMemcpyAsync(vec_host, e->col[i], sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   return ED_OK;
 }

@@ -420,6 +420,24 @@ def test_real_storage_matches_complex_path(ed, envs):
     assert max(err_r) <= 1e-11
 
 
+@pytest.mark.parametrize('case', [(18, 7), (8, 4), (16, 0)])
+def test_host_eigenvector_real_storage(ed, envs, case):
+    """solution_host of a real-storage solve (staged in halves through a spare
+    basis column) equals the device eigenvector bit for bit, for an odd
+    dimension (C(18,16) = 153), the one-state sector and an even one."""
+    N, mag = case
+    env, b, h, M = make_pair(ed, envs, 0, N, 1, N, mag, 1.0, 1.0, 0.3, 0.3)
+    nev = 1 if b.size == 1 else 2
+    eps, nconv, ev, errs = solve(ed, env, h, nev, tol=1e-10, ncv=min(16, b.size))
+    assert nconv >= nev
+    for i in range(nev):
+        dev = ed.Solver.solution(eps, i)[1].cpu().numpy()
+        host = ed.Solver.solution_host(eps, i)
+        assert np.array_equal(host.view(np.uint64), dev.view(np.uint64)), (case, i)
+        assert np.all(host.imag == 0.0)
+    ed.Solver.SolverClean(eps)
+
+
 def test_restart_pair_arithmetic(ed, envs, golden):
     """Float-pair products in the restart combination (forced here; the
     default from 2^22 basis states up): every golden solver case at 1e-12 as
