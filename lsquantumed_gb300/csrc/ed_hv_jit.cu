@@ -105,6 +105,7 @@ typedef unsigned long long u64;
 struct alignas(16) D2 { double x, y; };
 struct alignas(16) L2 { i64 x, y; };
 #define NAN_Q ((i64)0x8000000000000000ull)
+#define T0B(off) ((u32)*(const unsigned short*)((const char*)t0s + (off)))
 )";
 
 const char* kKernels = R"(
@@ -134,6 +135,7 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 c0 = s & LOWMASK, c1 = s >> W0;
     const u32 rr = (u32)r;
     const u32 rb0 = rr - (u32)t0s[c0];
+    const u32 c0b = c0 << 1;  // byte offset of T0[c0]; T0[c0 ^ m] is at c0b ^ (m << 1)
     const u32 rb1 = rr - t1[c1];
     i64 a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     bool bad = false;
@@ -311,13 +313,13 @@ std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
   o << "{ ";
   if (cls == 0) {
     o << "const u32 t = c0 & " << hex(m0) << "; const bool on = (t != 0u) & (t != " << hex(m0)
-      << "); const u32 g = rb0 + (u32)t0s[c0 ^ " << hex(m0) << "]; ";
+      << "); const u32 g = rb0 + T0B(c0b ^ " << hex(m0 << 1) << "); ";
   } else if (cls == 1) {
     o << "const u32 t = c1 & " << hex(m1) << "; const bool on = (t != 0u) & (t != " << hex(m1)
       << "); const u32 g = rb1 + t1[c1 ^ " << hex(m1) << "]; ";
   } else {
-    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = (u32)t0s[c0 ^ "
-      << hex(m0) << "] + t1[c1 ^ " << hex(m1) << "]; ";
+    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = T0B(c0b ^ "
+      << hex(m0 << 1) << ") + t1[c1 ^ " << hex(m1) << "]; ";
   }
   o << "gather<CHECK, RX>(xq, g, on, " << ar << ", " << ai << ", bad); }\n    ";
   return o.str();
