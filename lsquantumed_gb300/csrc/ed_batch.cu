@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
   for (int b0 = 0; b0 < B; b0 += Bp) {
     const int b = b0 + lane_b;
     double nrm = 0.0;
-    unsigned long long amax = 0ull;  // bits of max |w[r, b]|
+    unsigned int amax = 0u;  // high word of max |w[r, b]|
     if (lane_r < S && b < B) {
       if (REG) {
         // nv <= BU_REG: this realisation's coefficients in registers, two
@@ -428,11 +428,11 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
           }
           w[k0] = w0;
           nrm = fma(w0, w0, nrm);
-          amax = ed_absmax_bits(amax, w0);
+          amax = ed_absmax_hi(amax, w0);
           if (has1) {
             w[k1] = w1;
             nrm = fma(w1, w1, nrm);
-            amax = ed_absmax_bits(amax, w1);
+            amax = ed_absmax_hi(amax, w1);
           }
         }
       } else {
@@ -443,13 +443,13 @@ __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv
           for (int i = 0; i < nv; ++i) wv = fma(-V.p[i][k], h[(size_t)i * B + b], wv);
           w[k] = wv;
           nrm = fma(wv, wv, nrm);
-          amax = ed_absmax_bits(amax, wv);
+          amax = ed_absmax_hi(amax, wv);
         }
       }
     }
     __syncthreads();
     sh[threadIdx.x] = nrm;
-    shm[threadIdx.x] = __longlong_as_double((long long)amax);
+    shm[threadIdx.x] = ed_absmax_hi_value(amax);
     __syncthreads();
     if (lane_r == 0 && b < B) {
       double t = 0.0, mx = 0.0;
@@ -950,18 +950,18 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       }
       // normalise into col[j+1]; its fixed-point copy for the next H.v in
       // the same pass: the largest exponent of the scaled block is the largest
-      // of fl(max_r |w[r, b]| * s_b) over b (rounding is monotonic)
+      // of fl(max_r |w[r, b]| * s_b) over b (rounding is monotonic); where
+      // one is not determined by the high words, scale only
       std::vector<double> sc(A);
       int emax = 0;
       bool finite = true;
       for (int b = 0; b < A; ++b) {
         const double nb = beta[(size_t)b * (m + 1) + j];
         sc[b] = nb > 1e-300 ? 1.0 / nb : 0.0;
-        const double mb = wmax[b] * sc[b];
-        if (!std::isfinite(mb)) { finite = false; continue; }
-        uint64_t bits;
-        memcpy(&bits, &mb, sizeof(bits));
-        emax = std::max(emax, (int)((bits >> 52) & 0x7FF));
+        if (sc[b] == 0.0) continue;  // a zero column stays zero
+        const int eb = ed_fx64_emax_scaled(wmax[b], sc[b]);
+        if (eb < 0) { finite = false; continue; }
+        emax = std::max(emax, eb);
       }
       cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
       if (finite) {

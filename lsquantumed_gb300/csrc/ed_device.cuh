@@ -106,12 +106,18 @@ __device__ __forceinline__ void ed_block_reduce(double (&v)[NV], double* sh) {
   }
 }
 
-// Running max of |v| kept as the bit pattern of a non-negative double (whose
-// order is that of the unsigned integer): integer instructions only, since
-// FP64 min/max issue on GB300's slow FP64 unit.
-__device__ __forceinline__ unsigned long long ed_absmax_bits(unsigned long long m, double v) {
-  const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-  return a > m ? a : m;
+// Running max of the high 32 bits of |v| (sign, exponent and the top 20
+// fraction bits; for non-negative doubles their order is that of the
+// integers): two integer instructions per value, since FP64 min/max issue on
+// GB300's slow FP64 unit and a 64-bit compare costs more.  The result, as the
+// double whose low word is zero, is a lower bound of max |v| with the same
+// high 32 bits.
+__device__ __forceinline__ unsigned int ed_absmax_hi(unsigned int m, double v) {
+  return max(m, (unsigned int)(__double_as_longlong(v) >> 32) & 0x7FFFFFFFu);
+}
+
+__device__ __forceinline__ double ed_absmax_hi_value(unsigned int m) {
+  return __longlong_as_double((long long)((unsigned long long)m << 32));
 }
 
 // Block maximum of v (>= 0) into thread 0's v; sh holds 32 doubles.

@@ -200,7 +200,7 @@ static int orthogonalize(ed_eps* e, int j, std::vector<double2>& h, double* nw, 
 // traffic of every projection, update and restart.  The steps are those of
 // orthogonalize_lanczos / eps_solve_impl; only the storage differs.
 // ---------------------------------------------------------------------------
-// *wmax: max_r |w_r| after the last pass.
+// *wmax: max_r |w_r| after the last pass, low 32 bits cleared.
 static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, double a, double y2,
                                    std::vector<double>& h, double* nw, double* norig, double* wmax) {
   ed_ctx* ctx = e->h->ctx;
@@ -307,10 +307,9 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
       } else {
         // the next H.v's input is this vector: its fixed-point copy is made in
         // the same pass (bit-identical to quantizing it afterwards)
-        if (std::isfinite(wmax) && std::isfinite(nw))
-          ED_TRY(ed_scale_quantize_r(H, e->w_r, e->col_r[j + 1], 1.0 / nw, wmax));
-        else
-          ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw, n));
+        const int rq = ed_scale_quantize_r(H, e->w_r, e->col_r[j + 1], 1.0 / nw, wmax);
+        if (rq == ED_ENOTSUP) ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw, n));
+        else if (rq != ED_OK) return rq;
         beta[j] = nw;
       }
     }

@@ -701,15 +701,27 @@ int ed_fx64_sbits(const ed_ham* h) {
   return 62 - head;
 }
 
-int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax) {
+int ed_fx64_emax_scaled(double absmax_hi, double s) {
+  uint64_t lb;
+  std::memcpy(&lb, &absmax_hi, sizeof(lb));
+  const uint64_t ub = lb | 0xFFFFFFFFull;
+  double u;
+  std::memcpy(&u, &ub, sizeof(u));
+  const double ml = absmax_hi * s, mu = u * s;
+  if (!std::isfinite(ml) || !std::isfinite(mu) || !(s > 0.0)) return -1;
+  uint64_t bl, bu;
+  std::memcpy(&bl, &ml, sizeof(bl));
+  std::memcpy(&bu, &mu, sizeof(bu));
+  const int el = (int)((bl >> 52) & 0x7FF), eu = (int)((bu >> 52) & 0x7FF);
+  return el == eu ? el : -1;
+}
+
+int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax_hi) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
-  const double m = src_absmax * s;
-  if (!std::isfinite(m) || !(s > 0.0)) return ed_fail(ED_EINVAL, "scale-quantize needs a finite input and s > 0");
+  const int emax = ed_fx64_emax_scaled(src_absmax_hi, s);
+  if (emax < 0) return ED_ENOTSUP;  // not determined: the caller scales and the H.v quantizes
   ED_TRY(ensure_fixed_buffers(h));
-  uint64_t mb;
-  std::memcpy(&mb, &m, sizeof(mb));
-  const int emax = (int)((mb >> 52) & 0x7FF);
   const int g = grid_cap(ctx, b->dim, 256, 8);
   k_scale_quantize_r<<<g, 256, 0, ctx->stream>>>(src, dst, s, b->dim, emax, ed_fx64_sbits(h), (long long*)h->d_xq,
                                                   h->d_gmax);

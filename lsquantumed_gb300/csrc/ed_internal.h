@@ -172,12 +172,17 @@ int ed_launch_hv_r(ed_ham* h, const double* x, double* y);
 // zero only the real parts are stored (int64[dim]).  *sbits = the scale.
 int ed_fx64_quantize(ed_ham* h, const double2* x, int* sbits);
 int ed_fx64_quantize_r(ed_ham* h, const double* x, int* sbits);
+// Largest biased exponent among fl(v_r * s), given absmax_hi = max_r |v_r|
+// with its low 32 bits cleared (the device tracks the high words only).  The
+// true maximum lies between absmax_hi and absmax_hi with the low word all
+// ones, and rounding is monotonic, so the exponent is known when both bounds
+// give the same one; -1 otherwise (or when not finite, or s <= 0).
+int ed_fx64_emax_scaled(double absmax_hi, double s);
 // dst = src * s (real storage) and, in the same pass, dst's fixed-point copy
-// for the next H.v of dst (h->xq_src = dst).  src_absmax = max_r |src_r|
-// (finite): the largest exponent among fl(src_r * s) is that of
-// fl(src_absmax * s), since rounding is monotonic, so the copy equals what
-// ed_fx64_quantize_r would make of dst, bit for bit.
-int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax);
+// for the next H.v of dst (h->xq_src = dst), bit-identical to what
+// ed_fx64_quantize_r would make of dst.  src_absmax_hi as above.  Returns
+// ED_ENOTSUP without launching anything when the exponent is not determined.
+int ed_scale_quantize_r(ed_ham* h, const double* src, double* dst, double s, double src_absmax_hi);
 // sbits of h's fixed-point H.v input (depends on the bond counts only).
 int ed_fx64_sbits(const ed_ham* h);
 bool ed_lin_supported(const ed_ham* h);
@@ -227,7 +232,8 @@ int ed_copy(ed_ctx* ctx, const double2* src, double2* dst, int64_t n);
 // Real storage (real-mode solves keep only the real parts of the basis).
 int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
                   const double* vjm1, double b, double* h_host, double* wnorm2_host);
-// wmax_host (nullable): max_r |w_r| after the update.
+// wmax_host (nullable): max_r |w_r| after the update with its low 32 bits
+// cleared (see ed_fx64_emax_scaled).
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
                 double* wnorm2_host, double* wmax_host = nullptr);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);

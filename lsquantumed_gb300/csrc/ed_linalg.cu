@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
   for (int i = threadIdx.x; i < nv; i += blockDim.x) sh_h[i] = h[i];
   __syncthreads();
   double acc[1] = {0.0};
-  unsigned long long amax = 0ull;  // bits of max |w|
+  unsigned int amax = 0u;  // high word of max |w|
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r0 < n; r0 += 2 * stride) {
     const int64_t r1 = r0 + stride;
@@ -591,11 +591,11 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
     }
     w[r0] = w0;
     acc[0] = fma(w0, w0, acc[0]);
-    if (with_max) amax = ed_absmax_bits(amax, w0);
+    if (with_max) amax = ed_absmax_hi(amax, w0);
     if (has1) {
       w[r1] = w1;
       acc[0] = fma(w1, w1, acc[0]);
-      if (with_max) amax = ed_absmax_bits(amax, w1);
+      if (with_max) amax = ed_absmax_hi(amax, w1);
     }
   }
   __shared__ double shr[32];
@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
   if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
   if (with_max) {
     __syncthreads();  // shr reused
-    double am = __longlong_as_double((long long)amax);
+    double am = ed_absmax_hi_value(amax);
     ed_block_max(am, shr);
     if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = am;
   }
