@@ -210,10 +210,13 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
   *norig = std::sqrt(y2);
   const bool three_term = j > k && j > 0;
   std::vector<double> c(j + 1);
-  double w2 = 0.0, n2 = 0.0;
+  double n2 = 0.0;
+  // no norm in the projection pass (one FP64 FMA per row less on the FP64
+  // bound kernel): the norm before the update is sqrt(||w_after||^2 + sum c_i^2)
+  // (Pythagoras against the orthonormal basis), formed after the update
   ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
-                       beta_prev, c.data(), &w2));
-  double n0 = std::sqrt(w2);
+                       beta_prev, c.data(), nullptr));
+  double n0 = -1.0;
   h[j] += a;
   if (three_term) h[j - 1] += beta_prev;
   for (int pass = 0; pass < 2; ++pass) {
@@ -222,6 +225,11 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
     ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, wmax));
     for (int i = 0; i <= j; ++i) h[i] += c[i];
     *nw = std::sqrt(n2);
+    if (n0 < 0.0) {
+      double s2 = n2;
+      for (int i = 0; i <= j; ++i) s2 += c[i] * c[i];
+      n0 = std::sqrt(s2);
+    }
     e->ortho_passes++;
     if (*nw >= 0.7071067811865476 * n0) break;
     n0 = *nw;

@@ -550,7 +550,7 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
   for (int gidx = 0; gidx < ngroups; ++gidx) {
     const int v0 = gidx * ED_GROUP_R;
     const int ng = std::max(0, std::min(ED_GROUP_R, nv - v0));
-    const int last = gidx == ngroups - 1;
+    const int last = gidx == ngroups - 1 && wnorm2_host != nullptr;  // the norm costs one FP64 FMA per row
     if (gidx == 0 && vj)
       k_multidot_r<ED_GROUP_R, true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, v0, ng, w, n, vj, a, vjm1, b, last,
                                                                               ctx->d_red, nblk);
