@@ -908,13 +908,16 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       }
       // full CGS pass (+ DGKS refinement when any realisation needs it)
       std::vector<const double*> vs(col.begin(), col.begin() + j + 1);
-      std::vector<double> prevn(A, 0.0);
+      // norms before each pass for the DGKS test: no norm in the dot pass (one
+      // FP64 FMA per entry less); before the first pass it is
+      // sqrt(||w_after||^2 + sum_i c_i^2) (Pythagoras), before the second the
+      // norm after the first
+      std::vector<double> prevn(A, -1.0);
       for (int pass = 0; pass < 2; ++pass) {
-        if ((rc = batch_dots(bt, A, vs, w, true, out, pass == 0 ? local_vj : nullptr, local_vjm1,
+        if ((rc = batch_dots(bt, A, vs, w, false, out, pass == 0 ? local_vj : nullptr, local_vjm1,
                              d_coef + (size_t)64 * A)) != ED_OK)
           goto cleanup;
         std::vector<double> hc(out.begin(), out.begin() + (size_t)(j + 1) * A);
-        for (int b = 0; b < A; ++b) prevn[b] = std::sqrt(out[(size_t)(j + 1) * A + b]);
         cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
         BCols vc;
         memset(&vc, 0, sizeof(vc));
@@ -944,7 +947,13 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
         for (int b = 0; b < A; ++b) {
           const double nw = std::sqrt(out[b]);
           beta[(size_t)b * (m + 1) + j] = nw;
+          if (prevn[b] < 0.0) {
+            double s2 = out[b];
+            for (int i = 0; i <= j; ++i) s2 += hc[(size_t)i * A + b] * hc[(size_t)i * A + b];
+            prevn[b] = std::sqrt(s2);
+          }
           if (nw < 0.7071067811865476 * prevn[b]) again = true;
+          prevn[b] = nw;
         }
         if (!again) break;
       }
