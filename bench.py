@@ -604,8 +604,10 @@ def run_ours(args):
         'e2e': e2e, 'gpu_launches': launches,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
                      'traffic': traffic,
-                     'kernel': 'matrix-free H.v: two-table-rank kernel (k_hv_jit* when hv_variant is jit*, else '
-                               'k_hv_lin) + k_quantize64_r + k_max_exponent_r',
+                     'kernel': 'matrix-free H.v in real storage: two-table-rank kernel (k_hv_jit*_r when '
+                               'hv_variant is jit*, else k_hv_lin); its fixed-point input comes from the '
+                               'preceding scaling pass (k_scale_quantize_r), else k_max_exponent_r + '
+                               'k_quantize64_r inside the timed launch',
                      'hv_variant': {'plain': H.hv_variant(False), 'fused_dot': H.hv_variant(True)},
                      'traffic_note': traffic_note, 'peak_kind': peak_kind,
                      'bytes_per_row': bytes_row, 'bytes_per_row_complex_input': bytes_row_complex,
