@@ -180,7 +180,10 @@ int ed_ham_set_hv_variant(ed_ham* h, const char* name);
 
 /* ---- eigensolver: replaces Solver:: (src/solver.cpp:7-68) ----------------- */
 /* SolverInit(eps, H, nev, ncv, mpd): Hermitian, Krylov-Schur, smallest real.
- * ncv/mpd <= 0 mean PETSC_DECIDE (ncv = max(2 nev, nev + 15), capped at n). */
+ * ncv/mpd <= 0 mean PETSC_DECIDE (ncv = max(2 nev, nev + 15), capped at n).
+ * The solver refers to h until ed_eps_destroy: destroy it first (as an EPS
+ * is cleaned before the Mat it solves in the reference's drivers); the same
+ * holds for a batch (ed_batch_destroy before ed_ham_destroy). */
 int ed_eps_create(ed_ham* h, int nev, int ncv, int mpd, ed_eps** out);
 /* EPSSetDimensions */
 int ed_eps_set_dimensions(ed_eps* e, int nev, int ncv, int mpd);

@@ -1158,6 +1158,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
 cleanup:
   cudaStreamSynchronize(ctx->stream);
+  bt->xq_src = nullptr;  // made with a column of the pool freed here
   cudaFree(pool);
   cudaFree(w);
   cudaFree(dg[0]);

@@ -96,6 +96,8 @@ void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, st
 }
 
 static void eps_free(ed_eps* e) {
+  // a fixed-point copy made with one of these columns must not outlive them
+  if (e->h && e->pool_r && e->h->xq_src) e->h->xq_src = nullptr;
   if (e->pool) cudaFree(e->pool);
   if (e->w) cudaFree(e->w);
   if (e->pool_r) cudaFree(e->pool_r);
