@@ -6,7 +6,10 @@ error bounds the code and the header state:
   2^-47 |v|;
 - one pair product (hi*hi exactly by FMA, the three other terms added in
   FP32) is within 2^-45 |v w| of the exact product;
-- values below 2^-126 give 0 and non-finite values NaN.
+- values below 2^-126 give 0 and non-finite values NaN;
+- the largest exponent of a scaled vector taken from the high 32 bits of
+  its largest magnitude (ed_fx64_emax_scaled) is exact wherever it is
+  reported.
 
 The FP32 operations are emulated in float64, where every FP32 product is
 exact; exact references use fractions.  No GPU needed.
@@ -95,3 +98,42 @@ def test_host_pair_matches_bound():
         lo = np.float32(y - float(hi))
         err = abs(Fraction(float(y)) - Fraction(float(hi)) - Fraction(float(lo)))
         assert err <= abs(Fraction(float(y))) * Fraction(1, 2 ** 48)
+
+
+def emax_scaled(absmax_hi, s):
+    """ed_fx64_emax_scaled: the largest biased exponent among fl(v_r * s) from
+    max |v_r| with its low 32 bits cleared, or -1 when the bounds disagree."""
+    lb = np.array([absmax_hi]).view(np.uint64)[0]
+    u = np.array([lb | np.uint64(0xFFFFFFFF)], dtype=np.uint64).view(np.float64)[0]
+    ml, mu = absmax_hi * s, u * s
+    if not (np.isfinite(ml) and np.isfinite(mu) and s > 0):
+        return -1
+    el = int(np.array([ml]).view(np.uint64)[0] >> np.uint64(52)) & 0x7FF
+    eu = int(np.array([mu]).view(np.uint64)[0] >> np.uint64(52)) & 0x7FF
+    return el if el == eu else -1
+
+
+def test_emax_from_high_words():
+    """The one-pass scaling of the solver takes the largest exponent of the
+    scaled vector from the high 32 bits of max |w|: where both bounds agree
+    it equals the exponent k_max_exponent_r finds on fl(w * s), and they
+    disagree only when fl(max |w| * s) sits within 2^-20 of a power of two."""
+    rng = np.random.default_rng(5)
+    undetermined = 0
+    for trial in range(3000):
+        w = rng.standard_normal(64) * np.exp2(rng.integers(-30, 30))
+        s = 1.0 / np.linalg.norm(w) if trial % 3 else float(np.exp2(rng.integers(-5, 5)))
+        bits = np.abs(w).view(np.uint64) >> np.uint64(32)
+        hi = (bits.max() << np.uint64(32)).astype(np.uint64).view(np.float64)
+        got = emax_scaled(float(hi), s)
+        want = int(((np.abs(w) * s).view(np.uint64) >> np.uint64(52)).max() & np.uint64(0x7FF))
+        if got < 0:
+            undetermined += 1
+        else:
+            assert got == want, (trial, got, want)
+    # undetermined needs fl(max |w| * s) within about 2^-20 of a power of two
+    assert undetermined <= 3
+    # a value just below a power of two whose low word decides the binade
+    v = np.array([np.nextafter(2.0, 0.0)])
+    hiv = float((v.view(np.uint64) >> np.uint64(32) << np.uint64(32)).view(np.float64)[0])
+    assert emax_scaled(hiv, 1.0 + 2.0 ** -40) == -1
