@@ -15,7 +15,9 @@ int ed_fail(int code, const std::string& msg) {
   return code;
 }
 int ed_cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
-  g_err = std::string("CUDA error: ") + cudaGetErrorString(e) + " in " + what + " (" + file + ":" + std::to_string(line) + ")";
+  const char* base = strrchr(file, '/');  // the source file's name, not the build machine's path
+  base = base ? base + 1 : file;
+  g_err = std::string("CUDA error: ") + cudaGetErrorString(e) + " in " + what + " (" + base + ":" + std::to_string(line) + ")";
   return e == cudaErrorMemoryAllocation ? ED_ENOMEM : ED_ECUDA;
 }
 

@@ -112,3 +112,38 @@ def test_environment_requires_gpu():
     import lsquantumed_gb300 as ed
     with pytest.raises(RuntimeError):
         ed.Environment(nspins=8)
+
+
+def _driver(lib, *args):
+    import subprocess
+    from lsquantumed_gb300.build import DRIVER
+    assert os.path.exists(DRIVER)
+    return subprocess.run([DRIVER, *args], capture_output=True, text=True, timeout=120)
+
+
+@pytest.mark.parametrize('args,msg', [
+    (('-n', '7'), 'The total number of spins has to be EVEN.'),
+    (('-n', '-4'), 'The total number of spins has to be POSITIVE.'),
+    (('-n', '8', '-eps_type', 'lanczos'), 'only -eps_type krylovschur is provided'),
+    (('-n',), 'missing value for -n'),
+])
+def test_driver_rejects_bad_input(lib, args, msg):
+    """The drop-in driver validates its flags as the reference's parser and
+    Environment do (include/tools/parse_args.hpp:34-66, environment.cpp:31-35)
+    before it touches a GPU: exit status 1 and the reference's message."""
+    r = _driver(lib, *args)
+    assert r.returncode == 1
+    assert msg in r.stderr
+
+
+def test_driver_without_gpu_fails_cleanly(lib):
+    """With valid flags and no GPU the driver stops with an error (no CPU
+    fallback) and prints no eigenvalue line."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('GPU present')
+    r = _driver(lib, '-n', '8', '-ltype', 'chain1D', '-j1', '1', '-d1', '1', '-legacy_unused', '1')
+    assert r.returncode == 1
+    assert 'warning: unused option -legacy_unused' in r.stderr
+    assert 'error: CUDA error' in r.stderr and '(ed_capi.cu:' in r.stderr
+    assert '||Ax-kx||' not in r.stdout
