@@ -1,0 +1,53 @@
+"""CPU checks of the benchmark's byte accounting: k-bar (mean off-diagonal
+entries per row) for every workload from the reference's bond tables, and the
+algorithmic bytes per H.v row that roofline.achieved is computed from."""
+import importlib.util
+import os
+
+import pytest
+
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope='module')
+def bench():
+    spec = importlib.util.spec_from_file_location('bench_under_test', os.path.join(ROOT, 'bench.py'))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _pairs(ltype, N, lx, ly, with_nnn):
+    nn, nnn = oracle.bond_pairs(ltype, N, lx, ly)
+    pairs = [tuple(p) for p in nn]
+    if with_nnn:
+        pairs += [tuple(p) for p in nnn]
+    return pairs
+
+
+@pytest.mark.parametrize('case,B', [
+    ((oracle.SQUARE2D, 30, 6, 5, True), 120),   # N=30 6x5 J1-J2: k-bar 62.07
+    ((oracle.SQUARE2D, 20, 4, 5, True), 80),    # 4x5 J1-J2: 42.1
+    ((oracle.CHAIN1D, 16, 1, 16, False), 16),   # chain N=16: 8.53
+    ((oracle.CHAIN1D, 20, 1, 20, True), 40),    # chain N=20 J1-J2 (disorder sweep): 21.05
+    ((oracle.SQUARE2D, 16, 4, 4, True), 64),    # 4x4 J1-J2: 34.1
+    ((oracle.SQUARE2D, 24, 4, 6, True), 96),    # 4x6 J1-J2: 50.1
+])
+def test_kbar_from_reference_bonds(bench, case, B):
+    """k-bar = B N / (2 (N - 1)) at Sz=0 for B distinct bonds."""
+    ltype, N, lx, ly, nnn = case
+    kb = bench.kbar(N, N // 2, _pairs(ltype, N, lx, ly, nnn))
+    assert abs(kb - B * N / (2 * (N - 1))) < 1e-12, kb
+
+
+def test_bytes_per_row(bench):
+    kb = bench.kbar(30, 15, _pairs(oracle.SQUARE2D, 30, 6, 5, True))
+    # real storage (the solve): 8 x_s + 8 k-bar + 8 y_s + 4 state + 8 diagonal
+    assert abs(bench.hv_bytes_per_row(kb, 'real_storage') - (28 + 8 * kb)) < 1e-9
+    assert abs(bench.hv_bytes_per_row(kb, 'real_storage') - 524.55) < 0.01
+    # complex128 vectors and 16-byte gathers
+    assert abs(bench.hv_bytes_per_row(kb, 'complex') - 1037.1) < 0.05
+    # one launch at N=30 moves 81.4 GB of algorithmic bytes
+    assert abs(bench.hv_bytes_per_row(kb, 'real_storage') * 155117520 / 1e9 - 81.4) < 0.05
