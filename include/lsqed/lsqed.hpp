@@ -11,6 +11,7 @@
 #include <complex>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -43,6 +44,27 @@ inline void throw_on(int rc) {
 // ---------------------------------------------------------------------------
 // Environment (include/environment.hpp:20-53)
 // ---------------------------------------------------------------------------
+// The solver options of the command line, as PETSc's options database holds
+// them for EPSSetFromOptions (src/solver.cpp:21): -eps_tol and -eps_max_it
+// apply to every solver SolverInit creates, the DSF one included.
+struct SolverOptions {
+  double eps_tol = 0.0;  // 0: the library default (1e-8)
+  int eps_max_it = 0;    // 0: the library default
+};
+inline SolverOptions& solver_options() {
+  static SolverOptions o;
+  return o;
+}
+inline void parse_solver_options(int argc, char** argv) {
+  if (!argv) return;
+  for (int i = 1; i + 1 < argc; ++i) {
+    std::string k = argv[i];
+    for (auto& ch : k) ch = (char)((ch >= 'A' && ch <= 'Z') ? ch - 'A' + 'a' : ch);
+    if (k == "-eps_tol") solver_options().eps_tol = std::atof(argv[i + 1]);
+    else if (k == "-eps_max_it") solver_options().eps_max_it = std::atoi(argv[i + 1]);
+  }
+}
+
 class Environment {
  public:
   PetscInt nspins = 0;
@@ -50,11 +72,15 @@ class Environment {
   bool disorder_flg = false;
   ed_ctx* ctx = nullptr;
 
-  Environment(int /*argc*/, char** /*argv*/, const char* /*help*/ = nullptr) { throw_on(ed_ctx_create(0, nullptr, &ctx)); }
-  Environment(int /*argc*/, char** /*argv*/, PetscInt m_nspins, const char* /*help*/ = nullptr) {
+  Environment(int argc, char** argv, const char* /*help*/ = nullptr) {
+    parse_solver_options(argc, argv);
+    throw_on(ed_ctx_create(0, nullptr, &ctx));
+  }
+  Environment(int argc, char** argv, PetscInt m_nspins, const char* /*help*/ = nullptr) {
     if (m_nspins % 2 != 0) throw std::invalid_argument("The total number of spins has to be EVEN.");
     if (m_nspins <= 0) throw std::invalid_argument("The total number of spins has to be POSITIVE.");
     nspins = m_nspins;
+    parse_solver_options(argc, argv);
     throw_on(ed_ctx_create(0, nullptr, &ctx));
   }
   ~Environment() { ed_ctx_destroy(ctx); }
@@ -189,7 +215,10 @@ namespace Solver {
 template <typename L>
 inline PetscErrorCode SolverInit(EPS& solver, Hamiltonian<L>& h, PetscInt nev, PetscInt ncv = PETSC_DEFAULT,
                                  PetscInt mpd = PETSC_DEFAULT) {
-  return ed_eps_create(h.hamilt, (int)nev, (int)ncv, (int)mpd, &solver.e);
+  PetscErrorCode rc = ed_eps_create(h.hamilt, (int)nev, (int)ncv, (int)mpd, &solver.e);
+  const SolverOptions& o = solver_options();  // EPSSetFromOptions
+  if (rc == ED_OK && (o.eps_tol > 0.0 || o.eps_max_it > 0)) rc = ed_eps_set_tolerances(solver.e, o.eps_tol, o.eps_max_it);
+  return rc;
 }
 inline PetscErrorCode EPSSetDimensions(EPS& solver, PetscInt nev, PetscInt ncv, PetscInt mpd) {
   return ed_eps_set_dimensions(solver.e, (int)nev, (int)ncv, (int)mpd);
@@ -315,6 +344,75 @@ template <typename L>
 inline PetscScalar SquaredSubLattMagSTR(Environment& env, Basis& b, Striped<L>& sl, Vec& state) {
   PetscScalar e = sublattice_sum(b, {&sl.get_sl(0), &sl.get_sl(1), &sl.get_sl(2), &sl.get_sl(3)}, state);
   return e * 4.0 / PetscScalar((double)env.nspins) / PetscScalar(env.nspins + 4.0);
+}
+
+// DSF_data (include/phys.hpp:25-39): the same fields.
+template <typename L>
+struct DSF_data {
+  DSF_data() {}
+  Basis* b0 = nullptr;            // basis of the state's sector
+  Basis* b1 = nullptr;            // basis of the sector SQ maps to (b0 for Sqz)
+  L* lat = nullptr;
+  Hamiltonian<L>* h0 = nullptr;   // its couplings go to the file header
+  Hamiltonian<L>* h1 = nullptr;   // solved for nev eigenpairs
+  PetscInt nev = 10, ncv = PETSC_DEFAULT, mpd = PETSC_DEFAULT;
+  bool disorder = false;
+  PetscReal* hi = nullptr;        // nspins fields, written to the header when disorder
+  const char* path = "./";
+};
+}  // namespace Phys
+
+// Operator tags of DynStructFactor: S^z_i within the sector
+// (spinOPft.tmpl_func.hpp:28-60) and S^+_i from sector m to m+1
+// (spinOPft.tmpl_func.hpp:77-143).
+struct Sqz { static constexpr int op = 0; };
+struct Sqp { static constexpr int op = 1; };
+
+namespace Phys {
+// DynStructFactor<L, SQ> (include/phys.tmpl_func.hpp:87-215): nev lowest
+// eigenpairs of h1 (SLEPc's default tolerance, as the reference sets none),
+// c_{i,n} = <n| SQ_i |state> for every site, and the file
+// <path>/dsf_d<dis_iter>.dat in the reference's layout.
+template <typename L, typename SQ>
+inline PetscErrorCode DynStructFactor(Environment& env, DSF_data<L>& data, PetscScalar gs, Vec& state,
+                                      PetscInt dis_iter = 0) {
+  EPS solver;
+  PetscErrorCode rc = Solver::SolverInit(solver, *data.h1, data.nev, data.ncv, data.mpd);
+  if (rc != ED_OK) return rc;
+  PetscInt nconv = 0;
+  const int nev = (int)data.nev;
+  const size_t dim1 = (size_t)data.b1->size;
+  Vec vecs(env, (PetscInt)(dim1 * (size_t)nev));
+  std::vector<double> ev((size_t)nev);
+  rc = Solver::solve(env, solver, nconv);
+  for (int n = 0; n < nev && rc == ED_OK; ++n) {
+    double er = 0.0;
+    rc = ed_eps_get_eigenpair(solver.e, n, &ev[(size_t)n], &er, vecs.d + (size_t)n * dim1);
+  }
+  std::vector<ed_cplx> c((size_t)env.nspins * (size_t)nev);
+  if (rc == ED_OK) rc = ed_dsf_coefficients(data.b0->h, data.b1->h, SQ::op, state.d, vecs.d, nev, c.data());
+  Solver::SolverClean(solver);
+  if (rc != ED_OK) return rc;
+  const std::string fn = std::string(data.path) + "/dsf_d" + std::to_string((long)dis_iter) + ".dat";
+  FILE* fp = std::fopen(fn.c_str(), "w");
+  if (!fp) throw std::runtime_error("Cannot open file");
+  std::fprintf(fp, "#------------------------------- Parameters -------------------------------------\n");
+  std::fprintf(fp, "#%7s:   %ld  \n", " nspins", (long)env.nspins);
+  std::fprintf(fp, "#%7s:   %ld  \n", " nev", (long)data.nev);
+  std::fprintf(fp, "#%7s:   %.16f  \n", " GS", gs.real());
+  std::fprintf(fp, "#%7s:   %.5f  %4s:   %.5f  %4s:   %.5f  %4s:   %.5f\n", "J1", data.h0->hamilt_J1(), "D1",
+               data.h0->hamilt_D1(), "J2", data.h0->hamilt_J2(), "D2", data.h0->hamilt_D2());
+  if (data.disorder)
+    for (PetscInt i = 0; i < env.nspins; ++i) std::fprintf(fp, "# hi[%4ld]: %.16f\n", (long)i, data.hi[i]);
+  std::fprintf(fp, "#--------------------------------------------------------------------------------\n#\n#\n");
+  std::fprintf(fp, "#----- Energy -----  ------ Factor -----\n");
+  for (PetscInt s = 0; s < env.nspins; ++s) {
+    std::fprintf(fp, "# spin: %ld\n", (long)s);
+    for (int n = 0; n < nev; ++n)
+      std::fprintf(fp, "%.13e  %.13e\n", ev[(size_t)n] - gs.real(), c[(size_t)s * (size_t)nev + (size_t)n].re);
+  }
+  std::fclose(fp);
+  return ED_OK;
 }
 }  // namespace Phys
 

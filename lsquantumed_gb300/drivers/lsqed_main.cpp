@@ -117,42 +117,20 @@ static int run(Environment& env, L& lat, const Args& a) {
       std::printf("magSTR: %.10f\n", magSTR / (double)a.rep);
     }
     if (a.dsf_nev > 0) {
-      // Phys::DynStructFactor<L, Sqz> (phys.tmpl_func.hpp:87-215)
-      EPS dsf;
-      throw_on(Solver::SolverInit(dsf, h, a.dsf_nev));
-      throw_on(Solver::EPSSetTolerances(dsf, a.tol, a.max_it));
-      PetscInt nc = 0;
-      throw_on(Solver::solve(env, dsf, nc));
-      if (nc < a.dsf_nev) throw std::runtime_error("DSF eigensolve did not converge");
-      Vec vecs(env, b.size * a.dsf_nev);
-      std::vector<double> ev((size_t)a.dsf_nev);
-      for (int n = 0; n < a.dsf_nev; ++n) {
-        double e, er;
-        throw_on(ed_eps_get_eigenpair(dsf.e, n, &e, &er, vecs.d + (size_t)n * (size_t)b.size));
-        ev[(size_t)n] = e;
-      }
-      std::vector<ed_cplx> c((size_t)(a.n * a.dsf_nev));
-      throw_on(ed_dsf_coefficients(b.h, b.h, 0, state.d, vecs.d, a.dsf_nev, c.data()));
-      Solver::SolverClean(dsf);
-      std::string fn = a.path + "/dsf_d" + std::to_string((long)repet) + ".dat";
-      FILE* fp = std::fopen(fn.c_str(), "w");
-      if (!fp) throw std::runtime_error("Cannot open file");
-      std::fprintf(fp, "#------------------------------- Parameters -------------------------------------\n");
-      std::fprintf(fp, "#%7s:   %ld  \n", " nspins", (long)a.n);
-      std::fprintf(fp, "#%7s:   %d  \n", " nev", a.dsf_nev);
-      std::fprintf(fp, "#%7s:   %.16f  \n", " GS", eig.real());
-      std::fprintf(fp, "#%7s:   %.5f  %4s:   %.5f  %4s:   %.5f  %4s:   %.5f\n", "J1", a.J1, "D1", a.D1, "J2", a.J2, "D2",
-                   a.D2);
-      if (a.disorder)
-        for (PetscInt i = 0; i < a.n; ++i) std::fprintf(fp, "# hi[%4ld]: %.16f\n", (long)i, hi[(size_t)i]);
-      std::fprintf(fp, "#--------------------------------------------------------------------------------\n#\n#\n");
-      std::fprintf(fp, "#----- Energy -----  ------ Factor -----\n");
-      for (PetscInt s = 0; s < a.n; ++s) {
-        std::fprintf(fp, "# spin: %ld\n", (long)s);
-        for (int n = 0; n < a.dsf_nev; ++n)
-          std::fprintf(fp, "%.13e  %.13e\n", ev[(size_t)n] - eig.real(), c[(size_t)(s * a.dsf_nev + n)].re);
-      }
-      std::fclose(fp);
+      // examples/main.cpp:89-98: the DSF of the ground state within the sector
+      Phys::DSF_data<L> dsf_data;
+      dsf_data.b0 = &b;
+      dsf_data.b1 = &b;
+      dsf_data.lat = &lat;
+      dsf_data.h0 = &h;
+      dsf_data.h1 = &h;
+      dsf_data.nev = a.dsf_nev;
+      dsf_data.ncv = PETSC_DECIDE;
+      dsf_data.mpd = PETSC_DECIDE;
+      dsf_data.disorder = a.disorder;
+      dsf_data.hi = a.disorder ? hi.data() : nullptr;
+      dsf_data.path = a.path.c_str();
+      throw_on(Phys::DynStructFactor<L, Sqz>(env, dsf_data, eig, state, repet));
     }
   }
   return 0;

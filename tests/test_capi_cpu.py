@@ -147,3 +147,15 @@ def test_driver_without_gpu_fails_cleanly(lib):
     assert 'warning: unused option -legacy_unused' in r.stderr
     assert 'error: CUDA error' in r.stderr and '(ed_capi.cu:' in r.stderr
     assert '||Ax-kx||' not in r.stdout
+
+
+def test_shim_compiles_for_every_lattice():
+    """include/lsqed/lsqed.hpp instantiates with all of the reference's
+    interface (Basis, Hamiltonian<L>, Solver::, the four correlations, AF /
+    Striped order parameters, DSF_data and DynStructFactor<L, Sqz|Sqp>) for
+    every lattice, without warnings."""
+    import subprocess
+    src = os.path.join(ROOT, 'tests', 'cpp', 'shim_instantiate.cpp')
+    r = subprocess.run(['g++', '-std=c++17', '-Wall', '-Wextra', '-Werror', '-fsyntax-only',
+                        '-I' + os.path.join(ROOT, 'include'), src], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
