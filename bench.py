@@ -280,6 +280,25 @@ def workload_outputs(ed, env, b, lat, wl, eps, evals):
     return out
 
 
+def c3_cpu_sample(fields, sectors, N, J1, J2, nev, tol):
+    """The oracle's CPU eigensolve (explicit CSR in the reference layout,
+    Krylov-Schur, all host threads) of the chain with each field realisation
+    in each sector, as one disorder-sweep sample each: (samples/s, threads,
+    {sector: [lowest nev eigenvalues per realisation]})."""
+    import oracle
+    t0 = time.perf_counter()
+    evals = {}
+    for mag in sectors:
+        evals[mag] = []
+        for hi in fields:
+            M = oracle.Model(oracle.CHAIN1D, N, 1, N, mag, J1, 1.0, J2, J2)
+            M.build(3, hi)
+            r = M.eps_solve(nev=nev, ncv=16, tol=tol, seed=0, vectors=False)
+            evals[mag].append(r['evals'][:nev])
+    dt = time.perf_counter() - t0
+    return len(sectors) * len(fields) / dt, oracle.get_threads(), evals
+
+
 def run_disorder(args):
     """C3: disorder sweep, chain N=20 (J1=1, J2=0.2, Delta=1), h_i ~ U[-2, 2]
     from mt19937_64(seed) for seed = 0..511 (RandomDisorder::hi_init with
@@ -358,6 +377,20 @@ def run_disorder(args):
             ed.Solver.SolverClean(eps)
     torch.cuda.synchronize()
     t_plain = (time.perf_counter() - t0) / (nplain * len(sectors))
+    # CPU baseline: the oracle port on a bounded subset of the same solves
+    cpu = None
+    if not args.no_cpu:
+        try:
+            k = max(1, min(args.cpu_seeds, len(mine)))
+            sps, cores, cev = c3_cpu_sample(fields[:k], sectors, N, J1, J2, nev, tol)
+            cagree = all(abs(cev[mag][i][q] - batch_evals[mag][i][q]) <= 1e-8 * abs(cev[mag][i][q])
+                         for mag in sectors for i in range(k) for q in range(nev))
+            cpu = {'value': sps, 'unit': 'samples/s', 'cores': cores, 'kind': 'port',
+                   'sample': '%d seeds x %d sectors: full CPU eigensolves (explicit CSR build + Krylov-Schur, '
+                             'nev=2, tol 1e-9), the rate extrapolated to the sweep' % (k, len(sectors)),
+                   'eigenvalues_agree_1e-8': bool(cagree)}
+        except Exception as ex:  # reported, never fatal
+            cpu = {'value': None, 'unit': 'samples/s', 'cores': None, 'kind': 'port', 'sample': 'failed: %s' % ex}
     line = {'metric': METRIC, 'workload': 'c3', 'value': nsolve / t_batch, 'unit': 'samples/s',
             'higher_is_better': True, 'n_gpus': ws, 'steps': 1, 'warmup': args.warmup,
             'scaling': 'strong',  # the 1,536 solves are split over the ranks by seed
@@ -367,6 +400,7 @@ def run_disorder(args):
             'plain': {'samples_per_s': 1.0 / t_plain, 'seconds_per_solve': t_plain,
                       'sample': '%d seeds x %d sectors, one solve at a time' % (nplain, len(sectors))},
             'batched_over_plain': (nsolve / t_batch) * t_plain,
+            'cpu_baseline': cpu,
             'eigenvalues_agree_1e-8': bool(agree), 'dtype': 'f64', 'data': 'synthetic',
             'dtype_note': 'FP64 real storage of the Krylov basis (the complex128 solve of the reference with its '
                           'exactly-zero imaginary parts dropped); H.v sums in exact int64 fixed point; restart '
@@ -667,6 +701,7 @@ def main():
     ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
+    ap.add_argument('--cpu-seeds', type=int, default=4, help='seeds of the C3 CPU baseline sample (x 3 sectors)')
     ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')
     ap.add_argument('--acc', default='exact', choices=['exact', 'fixed64', 'fp64'], help='H.v accumulation')
     args = ap.parse_args()

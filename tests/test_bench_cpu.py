@@ -51,3 +51,20 @@ def test_bytes_per_row(bench):
     assert abs(bench.hv_bytes_per_row(kb, 'complex') - 1037.1) < 0.05
     # one launch at N=30 moves 81.4 GB of algorithmic bytes
     assert abs(bench.hv_bytes_per_row(kb, 'real_storage') * 155117520 / 1e9 - 81.4) < 0.05
+
+
+def test_c3_cpu_sample(bench):
+    """The disorder-sweep CPU baseline solves what the batched sweep solves:
+    the chain J1-J2 with the realisation's fields, in each sector; its lowest
+    levels match dense diagonalisation."""
+    import numpy as np
+    N, nev = 12, 2
+    fields = [oracle.rd_hi(s, N, -2.0, 2.0) for s in (0, 1)]
+    sps, cores, ev = bench.c3_cpu_sample(fields, (0, 1), N, 1.0, 0.2, nev, 1e-10)
+    assert sps > 0 and cores >= 1
+    for mag in (0, 1):
+        for hi, got in zip(fields, ev[mag]):
+            M = oracle.Model(oracle.CHAIN1D, N, 1, N, mag, 1.0, 1.0, 0.2, 0.2)
+            M.build(3, hi)
+            want = np.linalg.eigvalsh(M.dense())[:nev]
+            assert np.allclose(got, want, rtol=1e-10, atol=0), (mag, got, want)
