@@ -68,3 +68,24 @@ def test_c3_cpu_sample(bench):
             M.build(3, hi)
             want = np.linalg.eigvalsh(M.dense())[:nev]
             assert np.allclose(got, want, rtol=1e-10, atol=0), (mag, got, want)
+
+
+def test_reference_arm_json_contract():
+    """`bench.py --impl reference` (the oracle port on the host cores, bounded
+    sample) prints one JSON line with the same metric and workload as the GPU
+    arm, impl "reference", a cpu_baseline describing the run, and an e2e
+    entry with no host-device bytes."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--steps', '1',
+                        '--warmup', '0'], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line['impl'] == 'reference'
+    assert line['unit'] == 's' and line['higher_is_better'] is False
+    assert line['config']['workload'].startswith('c5 ') and line['config']['dim'] == 155117520
+    cb = line['cpu_baseline']
+    assert cb['kind'] in ('port', 'reference') and cb['cores'] >= 1 and cb['value'] == line['value'] > 0
+    assert 'times 334 H.v per solve' in cb['sample']
+    assert line['e2e'] == {'value': line['value'], 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
