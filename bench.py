@@ -24,6 +24,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = 'eigensolve s & H·v GB/s at N=30; disorder samples/s batched vs plain @res1e-9'
+DTYPE_NOTE = ('FP64 real storage of the Krylov basis (the complex128 solve of the reference with its exactly-zero '
+              'imaginary parts dropped); H.v sums in exact int64 fixed point (error below 2^-57 of max|x| per '
+              'entry); Gram-Schmidt and restart products FP64 or exact (every product FP64 or better)')
 
 WORKLOADS = {
     # name: (lattice, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol)
@@ -33,11 +36,6 @@ WORKLOADS = {
     # same family, sized for profiler captures (vectors 0.64 GB, above L2)
     'p28': ('square2D', 28, 4, 7, 1.0, 1.0, 0.55, 0.55, 0, 4, 16, 1e-9),
 }
-# H.v applications the Krylov-Schur run needs on each workload (seed 0), as
-# measured by the device run; the CPU restatement runs the same algorithm from
-# the same start vector, so its count is the same.  Used only to extrapolate
-# the bounded CPU sample of the reference arm (a workload not listed uses 300).
-NHV = {'c5': 334}
 
 
 def _rank_info():
@@ -135,99 +133,155 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle port on the host cores, bounded sample.
+# CPU baseline: the oracle port on the host cores.
 # ---------------------------------------------------------------------------
-class CpuSample:
-    """CSR SpMV (int64 columns, complex128 values, the reference's matrix
-    layout) and one CGS pass over 12 vectors on all host threads, at the
-    largest size of the same family whose explicit matrix fits host memory
-    (N=24 4x6 for the N=30 workload).  Per-row costs are scaled to the
-    workload's basis and multiplied by the solver's H.v count.  The matrix
-    build is setup, not timed (as the device run excludes its own setup)."""
+# The reference's CPU path assembles the explicit matrix (PETSc AIJ, 64-bit
+# indices, complex128 values).  At N=30 that is about 235 GB, beyond host
+# memory, so the measured CPU solve is the largest member of the same family
+# that the bench can build and solve within its budget: the 4x6 J1-J2 lattice
+# (N=24, 2.7M states, 138M stored entries, 3.3 GB).
+CPU_SAMPLE = {'c5': (24, 4, 6), 'p28': (24, 4, 6)}
+# H.v applications of the device solve of each workload from the seeded start
+# vector; the reference arm runs in a process of its own with no device solve
+# beside it, so it takes the count from here.  The GPU arm uses the count of
+# its own solve instead.
+NHV_DEVICE = {'c5': 334}
 
-    def __init__(self, wl):
-        import numpy as np
+
+def host_info():
+    """CPU model, logical cores, host RAM and the explicit-matrix sizes the
+    reference would need (PETSc AIJ: 8-byte column + 16-byte value per entry,
+    8 bytes per row pointer)."""
+    model = None
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(':')
+            if k.strip() in ('Model name', 'Vendor ID') and v.strip() and v.strip() != '-':
+                model = (model + ' / ' if model else '') + v.strip()
+    except Exception:
+        pass
+    ram = None
+    try:
+        for line in open('/proc/meminfo'):
+            if line.startswith('MemTotal:'):
+                ram = int(line.split()[1]) * 1024
+    except Exception:
+        pass
+    import oracle
+
+    def explicit_bytes(N, lx, ly):
+        nn, nnn = oracle.bond_pairs(oracle.SQUARE2D, N, lx, ly)
+        dim = math.comb(N, N // 2)
+        nnz = dim * (1 + kbar(N, N // 2, list(map(tuple, nn)) + list(map(tuple, nnn))))
+        return 24 * nnz + 8 * (dim + 1)
+    sizes = {'N=24 4x6': explicit_bytes(24, 4, 6), 'N=28 4x7': explicit_bytes(28, 4, 7),
+             'N=30 6x5': explicit_bytes(30, 6, 5)}
+    return {'cpu_model': model, 'logical_cores': os.cpu_count(), 'ram_bytes': ram,
+            'explicit_matrix_bytes': {k: int(v) for k, v in sizes.items()},
+            'explicit_matrix_fits_ram': {k: (bool(ram and v < 0.8 * ram) if ram else None) for k, v in sizes.items()}}
+
+
+class CpuSolve:
+    """One full CPU Krylov-Schur eigensolve by the oracle port on all host
+    threads: the explicit matrix in the reference layout (int64 columns,
+    complex128 values, rows sorted as PETSc AIJ keeps them) and the
+    Krylov-Schur restatement in complex128, with the workload's nev, ncv,
+    tolerance and start vector.  The matrix build is setup (as the device
+    run's is) and timed separately.  A few extra SpMVs split the solve's time
+    per step into the SpMV and the rest (orthogonalisation, restarts), which
+    is what the extrapolation to a larger basis scales."""
+
+    def __init__(self, wl, size=None):
         import oracle
         self.wl = wl
         ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
-        self.N, self.mag = N, mag
-        self.sN, self.slx, self.sly = (24, 4, 6) if N > 24 else (N, lx, ly)
+        self.cfg = (N, mag, nev, ncv, tol, J1, D1, J2, D2)
         self.lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
-        self.M = oracle.Model(self.lt, self.sN, self.slx, self.sly, 0, J1, D1, J2, D2)
+        if size is None:
+            size = CPU_SAMPLE.get(wl, (N, lx, ly))
+        self.sN, self.slx, self.sly = size
+        t0 = time.perf_counter()
+        self.M = oracle.Model(self.lt, self.sN, self.slx, self.sly, mag, J1, D1, J2, D2)
         self.nnz = self.M.build(3)
-        n = self.M.dim
-        self.x = oracle.start_vector(1, n)
-        # an orthonormal basis, so repeated CGS passes on w stay bounded
-        q, _ = np.linalg.qr(np.stack([oracle.start_vector(10 + i, n) for i in range(12)]).T)
-        self.V = np.ascontiguousarray(q.T)
-        self.w = oracle.start_vector(2, n)
-        nn, nnn = oracle.bond_pairs(self.lt, N, lx, ly)
-        self.nnz_row_f = 1 + kbar(N, mag + N // 2, list(map(tuple, nn)) + (list(map(tuple, nnn)) if J2 else []))
-        self.M.apply(self.x)  # warm
+        self.t_build = time.perf_counter() - t0
+        self.dim = self.M.dim
 
-    def run(self, nhv, budget_s=8.0):
+    def run(self):
+        import numpy as np
         import oracle
-        n = self.M.dim
+        N, mag, nev, ncv, tol, J1, D1, J2, D2 = self.cfg
         t0 = time.perf_counter()
-        reps = 0
-        while True:
-            self.M.apply(self.x)
+        r = self.M.eps_solve(nev=nev, ncv=ncv, tol=tol, seed=0, vectors=False)
+        t_solve = time.perf_counter() - t0
+        x = oracle.start_vector(1, self.dim)
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or (reps < 20 and time.perf_counter() - t0 < 1.0):
+            self.M.apply(x)
             reps += 1
-            if time.perf_counter() - t0 > budget_s / 2 or reps >= 50:
-                break
         t_spmv = (time.perf_counter() - t0) / reps
-        t0 = time.perf_counter()
-        creps = 0
-        while True:
-            oracle.cgs_step(self.V, self.w)
-            creps += 1
-            if time.perf_counter() - t0 > budget_s / 4 or creps >= 20:
-                break
-        t_cgs = (time.perf_counter() - t0) / creps
-        full_dim = math.comb(self.N, self.mag + self.N // 2)
-        nnz_row_s = self.nnz / n
-        t_hv_full = t_spmv * (full_dim / n) * (self.nnz_row_f / nnz_row_s)
-        # CGS with one refinement: two passes per step over ~12 vectors on average
-        t_step = t_hv_full + 2 * t_cgs * (full_dim / n)
-        return {
-            'value': t_step * nhv, 'unit': 's', 'cores': oracle.get_threads(), 'kind': 'port',
-            'sample': ('N=%d %dx%d explicit-CSR SpMV (%d reps, %.4f s each) + CGS pass over 12 vectors '
-                       '(%.4f s), scaled to N=%d rows (x%.2f) and nnz/row (x%.3f), times %d H.v per solve'
-                       % (self.sN, self.slx, self.sly, reps, t_spmv, t_cgs, self.N, full_dim / n,
-                          self.nnz_row_f / nnz_row_s, nhv)),
-        }
+        return {'N': self.sN, 'lattice': '%dx%d' % (self.slx, self.sly), 'dim': self.dim, 'nnz': self.nnz,
+                'build_s': self.t_build, 'solve_s': t_solve, 'nhv': r['nhv'], 'its': r['its'],
+                'nconv': r['nconv'], 'eigenvalues': [float(e) for e in np.sort(r['evals'])[:nev]],
+                'spmv_s': t_spmv, 'threads': oracle.get_threads()}
+
+
+def cpu_extrapolate(meas, wl, nhv):
+    """Seconds of the CPU solve of workload wl, from a measured solve of a
+    smaller member of the family: per step, the SpMV scales with the stored
+    entries and the rest with the basis size; times the H.v count nhv."""
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    import oracle
+    lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
+    nn, nnn = oracle.bond_pairs(lt, N, lx, ly)
+    pairs = list(map(tuple, nn)) + (list(map(tuple, nnn)) if J2 else [])
+    dim = math.comb(N, mag + N // 2)
+    nnz = dim * (1 + kbar(N, mag + N // 2, pairs))
+    per_step = meas['solve_s'] / max(meas['nhv'], 1)
+    other = max(0.0, per_step - meas['spmv_s'])
+    t = nhv * (meas['spmv_s'] * nnz / meas['nnz'] + other * dim / meas['dim'])
+    note = ('measured N=%d %s CPU solve (%.2f s, %d H.v, %.4f s per SpMV) scaled per step to N=%d: SpMV by stored '
+            'entries (x%.2f), orthogonalisation by basis size (x%.2f); times %d H.v'
+            % (meas['N'], meas['lattice'], meas['solve_s'], meas['nhv'], meas['spmv_s'], N, nnz / meas['nnz'],
+               dim / meas['dim'], nhv))
+    return t, note
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle port: explicit matrix in the
+    reference layout, Krylov-Schur in complex128) on all host threads.  Each
+    step is one full CPU solve of the largest family member that fits
+    (N=24 4x6 for the N=30 workload), timed end to end; the line's value
+    extrapolates it to the workload (kind 'port-extrapolated').  Steps are
+    capped at 2 solves so the run stays within a few minutes; warm-up solves
+    are not run (the matrix build, untimed, touches all memory first)."""
     ws, rk, lr = _rank_info()
     if rk != 0:
         return 0
     wl = args.workload
-    import oracle
     ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
-    nhv = NHV.get(wl)
-    times = []
-    res = None
-    sample = CpuSample(wl) if N > 24 else None
-    for step in range(args.warmup + args.steps):
-        if sample is not None:
-            res = sample.run(nhv or 300)
-        else:
-            t0 = time.perf_counter()
-            lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
-            M = oracle.Model(lt, N, lx, ly, mag, J1, D1, J2, D2)
-            M.build(3)
-            r = M.eps_solve(nev=nev, ncv=ncv, tol=tol, seed=0, vectors=False)
-            res = {'value': time.perf_counter() - t0, 'unit': 's', 'cores': oracle.get_threads(), 'kind': 'port',
-                   'sample': 'full CPU eigensolve (CSR build + Krylov-Schur), nhv=%d' % r['nhv']}
-        if step >= args.warmup:
-            times.append(res['value'])
-    v = sum(times) / len(times)
-    res['value'] = v
-    line = {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': v * 1e3, 'higher_is_better': False, 'scaling': 'weak',
+    size = None
+    if getattr(args, 'cpu_size', None):
+        size = tuple(int(v) for v in args.cpu_size.split(','))
+    cs = CpuSolve(wl, size)
+    nrun = max(1, min(args.steps, 2))
+    runs = [cs.run() for _ in range(nrun)]
+    meas = dict(runs[-1])
+    meas['solve_s'] = sum(r['solve_s'] for r in runs) / nrun
+    meas['solve_s_each'] = [r['solve_s'] for r in runs]
+    if (cs.sN, cs.slx, cs.sly) == (N, lx, ly):
+        v, kind, note = meas['solve_s'], 'port', 'full CPU eigensolve of the workload itself'
+    else:
+        v, note = cpu_extrapolate(meas, wl, NHV_DEVICE.get(wl, meas['nhv']))
+        kind = 'port-extrapolated'
+        note += ' (the H.v count of the device solve of this workload from the same start vector)'
+    cpu = {'value': v, 'unit': 's', 'cores': meas['threads'], 'kind': kind, 'sample': note,
+           'measured': meas, 'host': host_info()}
+    line = {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': nrun, 'warmup': 0,
+            'ms_per_step': v * 1e3, 'higher_is_better': False, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'c128', 'data': 'synthetic',
-            'config': workload_config(wl), 'impl': 'reference', 'cpu_baseline': res,
+            'config': workload_config(wl), 'impl': 'reference', 'cpu_baseline': cpu,
+            'timed_region_s': sum(r['solve_s'] for r in runs),
             'e2e': {'value': v, 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
     return 0
@@ -299,27 +353,23 @@ def c3_cpu_sample(fields, sectors, N, J1, J2, nev, tol):
     return len(sectors) * len(fields) / dt, oracle.get_threads(), evals
 
 
-def run_disorder(args):
+C3 = dict(N=20, J1=1.0, J2=0.2, W=2.0, nev=2, ncv=16, tol=1e-9)
+
+
+def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     """C3: disorder sweep, chain N=20 (J1=1, J2=0.2, Delta=1), h_i ~ U[-2, 2]
-    from mt19937_64(seed) for seed = 0..511 (RandomDisorder::hi_init with
-    srand_seq[k] = seed), Sz = 0, 1, 2: 1536 solves (lowest 2 pairs,
-    eps_tol 1e-9).  Batched: one lockstep batch per sector.  Plain: the same
-    solves issued one at a time (a bounded subset, timed per solve)."""
+    from mt19937_64(seed) (RandomDisorder::hi_init with srand_seq[k] = seed),
+    Sz = 0, 1, 2, lowest 2 pairs at eps_tol 1e-9.  Batched: one batch per
+    sector over all `seeds`, timed on the host around the three solves (each
+    returns its results to the host).  Plain: the same solves one at a time
+    for `plain_sample` seeds per sector spread over the whole seed range
+    (every restart tile of the batch), timed per solve, eigenvalues checked
+    against the batch at 1e-8."""
     import numpy as np
     import torch
-    from lsquantumed_gb300.build import build
-    build()
-    import lsquantumed_gb300 as ed
-    N, J1, J2, W, nev, tol = 20, 1.0, 0.2, 2.0, 2, 1e-9
-    ws, rk, lr = _rank_info()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group('gloo')
-    torch.cuda.set_device(lr)
-    nseeds = args.seeds
-    mine = shard_units(nseeds, rk, ws)  # this rank's seeds (weak scaling: every rank a share)
-    env = ed.Environment(nspins=N, device=lr)
-    fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in mine])
+    N, J1, J2, W, nev, ncv, tol = (C3[k] for k in ('N', 'J1', 'J2', 'W', 'nev', 'ncv', 'tol'))
+    env = ed.Environment(nspins=N, device=torch.cuda.current_device())
+    fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in seeds])
     sectors = (0, 1, 2)
     hams = {}
     for mag in sectors:
@@ -328,87 +378,193 @@ def run_disorder(args):
         h.build_diag(env)
         h.build_off_diag(env)
         hams[mag] = (b, h)
-    # batched
-    for _ in range(1 if args.warmup else 0):  # warm-up on a small batch
-        bt = ed.DisorderBatch(hams[0][1], fields[:8])
-        bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
-        del bt
+    bt = ed.DisorderBatch(hams[0][1], fields[:8])  # warm-up on a small batch
+    bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
+    del bt
     torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
     k0 = env.kernel_count()
     t0 = time.perf_counter()
     max_err, its, bad = 0.0, [], 0
     batch_evals = {}
     for mag in sectors:
         bt = ed.DisorderBatch(hams[mag][1], fields)
-        bt.set_restart_arithmetic(args.restart)
-        r = bt.solve(nev=nev, ncv=16, tol=tol, seed=0)
+        bt.set_restart_arithmetic(restart)
+        r = bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
         max_err = max(max_err, float(r['errs'].max()))
         bad += int((r['nconv'] < nev).sum())
         its.append(r['its'])
         batch_evals[mag] = r['evals']
         del bt
     torch.cuda.synchronize()
-    t_batch = dist_reduce(time.perf_counter() - t0, ws, 'max')
+    t_batch = time.perf_counter() - t0
     launches = env.kernel_count() - k0
-    max_err = dist_reduce(max_err, ws, 'max')
-    bad = int(dist_reduce(bad, ws, 'sum'))
-    nsolve = nseeds * len(sectors)
-    if rk != 0:
-        return 0
-    # plain: one solve at a time on a subset
-    nplain = min(args.plain_sample, len(mine))
+    nplain = min(plain_sample, len(seeds))
+    pick = sorted(set(np.linspace(0, len(seeds) - 1, nplain).round().astype(int).tolist()))
     t0 = time.perf_counter()
     agree = True
+    perr = 0.0
     for mag in sectors:
         b, _ = hams[mag]
-        for sd in range(nplain):
+        for k in pick:
             h = ed.Hamiltonian(env, b, ed.chain1D(env), J1, 1.0, J2, J2)
             h.build_diag(env)
             h.build_off_diag(env)
-            h.build_disorder(env, fields[sd])
-            eps = ed.Solver.SolverInit(h, nev, 16)
+            h.build_disorder(env, fields[k])
+            eps = ed.Solver.SolverInit(h, nev, ncv)
             ed.Solver.EPSSetTolerances(eps, tol)
+            eps.set_restart_arithmetic(restart)
             ed.Solver.solve(env, eps)
             for i in range(nev):
-                e, _ = ed.Solver.eigenvalue(eps, i)
-                agree &= abs(e - batch_evals[mag][sd][i]) <= 1e-8 * abs(e)
+                e, er = ed.Solver.eigenvalue(eps, i)
+                perr = max(perr, er)
+                agree &= abs(e - batch_evals[mag][k][i]) <= 1e-8 * abs(e)
             ed.Solver.SolverClean(eps)
     torch.cuda.synchronize()
-    t_plain = (time.perf_counter() - t0) / (nplain * len(sectors))
-    # CPU baseline: the oracle port on a bounded subset of the same solves
+    t_plain = (time.perf_counter() - t0) / (len(pick) * len(sectors))
+    nsolve = len(seeds) * len(sectors)
+    return {'batched_samples_per_s': nsolve / t_batch, 'plain_samples_per_s': 1.0 / t_plain,
+            'batched_over_plain': (nsolve / t_batch) * t_plain, 'batched_seconds': t_batch, 'solves': nsolve,
+            'max_rel_residual': max_err, 'plain_max_rel_residual': perr, 'unconverged': bad,
+            'restarts_per_sector': its, 'gpu_launches': launches, 'restart_arithmetic': restart,
+            'plain_sample': '%d seeds per sector (indices %s), one solve at a time' % (len(pick), pick),
+            'eigenvalues_agree_1e-8': bool(agree), 'fields': fields, 'batch_evals': batch_evals,
+            'config': 'chain1D N=20 J1=1 J2=0.2 Delta=1, h_i~U[-2,2] seeds %d..%d, Sz=0,1,2, nev=2, ncv=16, '
+                      'eps_tol=1e-9, dims %s' % (seeds[0], seeds[-1], [b.size for b, _ in hams.values()])}
+
+
+def run_disorder(args):
+    """C3 as its own line: samples/s of the batched sweep over the 1,536
+    solves, the plain one-at-a-time rate beside it, and a CPU baseline from
+    the oracle port on a bounded subset.  Under torchrun the seeds are split
+    over the ranks (no data-path collective; host scalars reduced)."""
+    import numpy as np
+    import torch
+    from lsquantumed_gb300.build import build
+    build()
+    import lsquantumed_gb300 as ed
+    ws, rk, lr = _rank_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    torch.cuda.set_device(lr)
+    nseeds = args.seeds
+    mine = shard_units(nseeds, rk, ws)
+    if ws > 1:
+        torch.distributed.barrier()
+    r = disorder_sweep(ed, None, mine, args.restart, args.plain_sample)
+    t_batch = dist_reduce(r['batched_seconds'], ws, 'max')
+    max_err = dist_reduce(r['max_rel_residual'], ws, 'max')
+    bad = int(dist_reduce(r['unconverged'], ws, 'sum'))
+    nsolve = nseeds * 3
+    if rk != 0:
+        return 0
+    N, J1, J2, nev, tol = C3['N'], C3['J1'], C3['J2'], C3['nev'], C3['tol']
     cpu = None
     if not args.no_cpu:
         try:
             k = max(1, min(args.cpu_seeds, len(mine)))
-            sps, cores, cev = c3_cpu_sample(fields[:k], sectors, N, J1, J2, nev, tol)
-            cagree = all(abs(cev[mag][i][q] - batch_evals[mag][i][q]) <= 1e-8 * abs(cev[mag][i][q])
-                         for mag in sectors for i in range(k) for q in range(nev))
+            sps, cores, cev = c3_cpu_sample(r['fields'][:k], (0, 1, 2), N, J1, J2, nev, tol)
+            cagree = all(abs(cev[mag][i][q] - r['batch_evals'][mag][i][q]) <= 1e-8 * abs(cev[mag][i][q])
+                         for mag in (0, 1, 2) for i in range(k) for q in range(nev))
             cpu = {'value': sps, 'unit': 'samples/s', 'cores': cores, 'kind': 'port',
-                   'sample': '%d seeds x %d sectors: full CPU eigensolves (explicit CSR build + Krylov-Schur, '
-                             'nev=2, tol 1e-9), the rate extrapolated to the sweep' % (k, len(sectors)),
+                   'sample': '%d seeds x 3 sectors: full CPU eigensolves (explicit CSR build + Krylov-Schur, '
+                             'nev=2, tol 1e-9), the rate extrapolated to the sweep' % k,
                    'eigenvalues_agree_1e-8': bool(cagree)}
         except Exception as ex:  # reported, never fatal
             cpu = {'value': None, 'unit': 'samples/s', 'cores': None, 'kind': 'port', 'sample': 'failed: %s' % ex}
+    out = {k: v for k, v in r.items() if k not in ('fields', 'batch_evals', 'config')}
+    out.update(batched_seconds=t_batch, max_rel_residual=max_err, unconverged=bad,
+               batched_samples_per_s=nsolve / t_batch)
     line = {'metric': METRIC, 'workload': 'c3', 'value': nsolve / t_batch, 'unit': 'samples/s',
             'higher_is_better': True, 'n_gpus': ws, 'steps': 1, 'warmup': args.warmup,
             'scaling': 'strong',  # the 1,536 solves are split over the ranks by seed
-            'batched': {'samples_per_s': nsolve / t_batch, 'seconds': t_batch, 'solves': nsolve,
-                        'restarts_per_sector': its, 'max_rel_residual': max_err, 'unconverged': bad,
-                        'gpu_launches': launches, 'restart_arithmetic': args.restart},
-            'plain': {'samples_per_s': 1.0 / t_plain, 'seconds_per_solve': t_plain,
-                      'sample': '%d seeds x %d sectors, one solve at a time' % (nplain, len(sectors))},
-            'batched_over_plain': (nsolve / t_batch) * t_plain,
-            'cpu_baseline': cpu,
-            'eigenvalues_agree_1e-8': bool(agree), 'dtype': 'f64', 'data': 'synthetic',
-            'dtype_note': 'FP64 real storage of the Krylov basis (the complex128 solve of the reference with its '
-                          'exactly-zero imaginary parts dropped); H.v sums in exact int64 fixed point; restart '
-                          'products as float pairs on the FP32 units from 2^22 states up',
-            'config': {'workload': 'c3 chain1D N=20 J1=1 J2=0.2 Delta=1, h_i~U[-2,2] seeds 0..%d, Sz=0,1,2, '
-                                   'nev=2, ncv=16, eps_tol=1e-9' % (nseeds - 1), 'dims': [b.size for b, _ in hams.values()]}}
+            'batched': out, 'cpu_baseline': cpu, 'dtype': 'f64', 'data': 'synthetic',
+            'dtype_note': DTYPE_NOTE,
+            'config': {'workload': 'c3 ' + r['config'].replace('seeds 0..', 'seeds 0..')}}
     print(json.dumps(line))
     return 0
+
+
+C4 = {'4x4': (16, 4, 4), '4x6': (24, 4, 6)}
+
+
+def gradient_timing(ed, restart='auto', seed=71):
+    """C4: adjoint gradients on the 4x4 and 4x6 J1-J2 lattices (J2 = 0.5,
+    Delta = 1) with per-bond couplings J_b = base_b (1 + 0.1 z_b),
+    z_b ~ N(0, 1) from mt19937_64(seed), D_b = J_b, and fields
+    h_i ~ U[-0.5, 0.5] from mt19937_64(seed + 1).  Timed on the host (each
+    step returns host results): the solve (nev=4, tol 1e-12), the
+    Hellmann-Feynman gradient of E0 and of the lowest-4 sum, and the adjoint
+    (MINRES) gradient of <S_0.S_far>.  One bond and one field derivative of
+    E0 are checked against central differences (step 1e-5) of device
+    energies."""
+    import numpy as np
+    import torch
+    out = {}
+    for name, (N, lx, ly) in C4.items():
+        env = ed.Environment(nspins=N)
+        b = ed.Basis(env, 0)
+        lat = ed.square2D(env, lx, ly)
+        pairs = np.concatenate([lat.nn_pairs, lat.nnn_pairs])
+        z = ed.random_normal(seed, len(pairs))
+        J = np.where(np.arange(len(pairs)) < len(lat.nn_pairs), 1.0, 0.5) * (1 + 0.1 * z)
+        D = J.copy()
+        hi = ed.random_fields(seed + 1, N, -0.5, 0.5)
+
+        def solve(Jx, Dx, hx, nev=4):
+            h = ed.Hamiltonian.from_bonds(env, b, pairs, Jx, Dx)
+            h.build_diag(env)
+            h.build_off_diag(env)
+            h.build_disorder(env, hx)
+            eps = ed.Solver.SolverInit(h, nev, 20)
+            ed.Solver.EPSSetTolerances(eps, 1e-12)
+            eps.set_restart_arithmetic(restart)
+            ed.Solver.solve(env, eps)
+            return h, eps
+        solve(J, D, hi)  # warm-up (run-time compiled kernels, allocations)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h, eps = solve(J, D, hi)
+        e = [ed.Solver.eigenvalue(eps, n)[0] for n in range(4)]
+        t_solve = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, v0, _ = ed.Solver.solution(eps, 0)
+        dJ, dD, dh = ed.Adjoint.energy_gradient(b, pairs, v0)
+        t_e0 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sJ, sD, sh = ed.Adjoint.eigenvalue_sum_gradient(eps, pairs, 4)
+        t_sum = time.perf_counter() - t0
+        far = (lx // 2) * ly + ly // 2
+        obs = [(1.0, ed.Adjoint.SISJ, 0, far)]
+        t0 = time.perf_counter()
+        val, cJ, cD, ch, info = ed.Adjoint.expectation_gradient(h, pairs, e[0], v0, obs, tol=1e-10)
+        t_corr = time.perf_counter() - t0
+        ed.Solver.SolverClean(eps)
+        d = 1e-5
+
+        def e0(Jx, Dx, hx):
+            _, ep = solve(Jx, Dx, hx, nev=1)
+            v = ed.Solver.eigenvalue(ep, 0)[0]
+            ed.Solver.SolverClean(ep)
+            return v
+        # J_q and D_q together (Delta = 1 ties them): dE0/dJ_q + dE0/dD_q
+        q = len(pairs) // 3
+        Jp, Jm = J.copy(), J.copy()
+        Jp[q] += d
+        Jm[q] -= d
+        fdJ = (e0(Jp, Jp, hi) - e0(Jm, Jm, hi)) / (2 * d)
+        hp, hm = hi.copy(), hi.copy()
+        hp[1] += d
+        hm[1] -= d
+        fdh = (e0(J, D, hp) - e0(J, D, hm)) / (2 * d)
+        out[name] = {'N': N, 'dim': b.size, 'bonds': len(pairs), 'solve_s': t_solve, 'grad_e0_s': t_e0,
+                     'grad_sum4_s': t_sum, 'grad_corr_minres_s': t_corr, 'minres_its': info['its'],
+                     'minres_relres': info['relres'], 'E': e, 'S0_Sfar': val,
+                     'fd_check': {'bond': q, 'dE0_dJ': float(dJ[q] + dD[q]), 'fd': fdJ,
+                                  'rel_err': abs(fdJ - dJ[q] - dD[q]) / max(1.0, abs(fdJ)),
+                                  'site': 1, 'dE0_dh': float(dh[1]), 'fd_h': fdh,
+                                  'rel_err_h': abs(fdh - dh[1]) / max(1.0, abs(fdh))}}
+    return out
 
 
 def hv_bytes_per_row(kb, mode):
@@ -616,21 +772,40 @@ def run_ours(args):
                'd2h_bytes_per_step': int(16 * dim * nev), 'steps': 1,
                'eigenvalues_match_device_run': bool(np.allclose(vals2, evals, rtol=1e-10, atol=0))}
 
+    # the same solve at the largest size the reference's CPU path can hold,
+    # on the device and on the host cores (both measured in this run)
     cpu = None
+    same = None
+    c3 = c4 = None
     if rk == 0 and not args.no_cpu:
         try:
-            cpu = CpuSample(wl).run(st['nhv']) if N > 24 else None
-            if cpu is None:
-                import oracle
-                lt = oracle.SQUARE2D if ltype == 'square2D' else oracle.CHAIN1D
-                t0 = time.perf_counter()
-                M = oracle.Model(lt, N, lx, ly, mag, J1, D1, J2, D2)
-                M.build(3)
-                r = M.eps_solve(nev=nev, ncv=ncv, tol=tol, seed=0, vectors=False)
-                cpu = {'value': time.perf_counter() - t0, 'unit': 's', 'cores': oracle.get_threads(),
-                       'kind': 'port', 'sample': 'full CPU eigensolve, nhv=%d' % r['nhv']}
+            cs = CpuSolve(wl)
+            meas = cs.run()
+            if (cs.sN, cs.slx, cs.sly) == (N, lx, ly):
+                cpu = {'value': meas['solve_s'], 'unit': 's', 'cores': meas['threads'], 'kind': 'port',
+                       'sample': 'full CPU eigensolve of the workload itself', 'measured': meas}
+            else:
+                v, note = cpu_extrapolate(meas, wl, st['nhv'])
+                cpu = {'value': v, 'unit': 's', 'cores': meas['threads'], 'kind': 'port-extrapolated',
+                       'sample': note + ' (the H.v count of this run\'s device solve)', 'measured': meas}
+                gs = device_solve_seconds(ed, env, cs.sN, cs.slx, cs.sly, wl, args.restart)
+                same = {'N': cs.sN, 'lattice': '%dx%d' % (cs.slx, cs.sly), 'gpu_solve_s': gs['seconds'],
+                        'gpu_nhv': gs['nhv'], 'cpu_solve_s': meas['solve_s'], 'cpu_nhv': meas['nhv'],
+                        'cpu_cores': meas['threads'], 'cpu_over_gpu': meas['solve_s'] / gs['seconds'],
+                        'eigenvalues_agree_1e-10': bool(np.allclose(gs['eigenvalues'], meas['eigenvalues'],
+                                                                    rtol=1e-10, atol=0))}
+            cpu['host'] = host_info()
         except Exception as ex:  # reported, never fatal
             cpu = {'value': None, 'unit': 's', 'cores': None, 'kind': 'port', 'sample': 'failed: %s' % ex}
+    if rk == 0 and wl == 'c5' and not args.no_extra:
+        try:
+            c3 = disorder_sweep(ed, env, list(range(args.seeds)), args.restart, args.plain_sample)
+        except Exception as ex:
+            c3 = {'failed': str(ex)}
+        try:
+            c4 = gradient_timing(ed, args.restart)
+        except Exception as ex:
+            c4 = {'failed': str(ex)}
 
     if rk != 0:
         return 0
@@ -638,9 +813,8 @@ def run_ours(args):
         'metric': METRIC, 'value': ms_step / 1e3, 'unit': 's', 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_step, 'higher_is_better': False, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload_config(wl),
-        'dtype_note': 'FP64 real storage of the Krylov basis (the complex128 solve of the reference with its '
-                  'exactly-zero imaginary parts dropped); H.v sums in exact int64 fixed point; restart '
-                  'products as float pairs on the FP32 units from 2^22 states up',
+        'dtype_note': DTYPE_NOTE if args.restart != 'pair' else DTYPE_NOTE + '; restart products as float pairs '
+                      'on the FP32 units (requested: error below 2^-45 per product)',
         'e2e': e2e, 'gpu_launches': launches,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
                      'traffic': traffic,
@@ -658,10 +832,46 @@ def run_ours(args):
                    'restart_arithmetic': args.restart,
                    'eigenvalues': evals,
                    'rel_residuals': errs},
-        'clocks': clocks, 'cpu_baseline': cpu,
+        'clocks': clocks, 'cpu_baseline': cpu, 'same_size_gpu_vs_cpu': same, 'c3': c3, 'c4': c4,
     }
     print(json.dumps(line))
     return 0
+
+
+def device_solve_seconds(ed, env_unused, N, lx, ly, wl, restart, reps=3):
+    """Device-resident solve of the workload's family member N (lx x ly) with
+    the workload's nev / ncv / tol: one warm-up solve, then the mean of
+    `reps` solves timed with CUDA events on the current stream."""
+    import torch
+    ltype, _, _, _, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    env = ed.Environment(nspins=N)
+    b = ed.Basis(env, mag)
+    lat = ed.square2D(env, lx, ly) if ltype == 'square2D' else ed.chain1D(env)
+    H = ed.Hamiltonian(env, b, lat, J1, D1, J2, D2)
+    H.build_diag(env)
+    H.build_off_diag(env)
+
+    def one():
+        eps = ed.Solver.SolverInit(H, nev, ncv if ncv else ed.PETSC_DEFAULT)
+        ed.Solver.EPSSetTolerances(eps, tol, 0)
+        eps.set_restart_arithmetic(restart)
+        ed.Solver.solve(env, eps)
+        return eps
+    ed.Solver.SolverClean(one())
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(reps):
+        eps = one()
+        if k < reps - 1:
+            ed.Solver.SolverClean(eps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    st = eps.stats()
+    ev = sorted(ed.Solver.eigenvalue(eps, i)[0] for i in range(min(nev, st['nreported'])))
+    ed.Solver.SolverClean(eps)
+    return {'seconds': e0.elapsed_time(e1) / 1e3 / reps, 'nhv': st['nhv'], 'eigenvalues': ev}
 
 
 def start_vector_host(n, seed=0):
@@ -695,7 +905,11 @@ def main():
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
     ap.add_argument('--restart', default='auto', choices=('auto', 'fp64', 'pair'),
-                    help='restart-combination products of the real-storage solve (auto: float pairs from 2^22 states)')
+                    help='restart-combination products of the real-storage solve (auto: the fastest form with every '
+                         'product FP64 or better; pair: float pairs on the FP32 units)')
+    ap.add_argument('--no-extra', action='store_true', help='skip the C3 / C4 sub-objects of the default line')
+    ap.add_argument('--cpu-size', default=None,
+                    help='N,lx,ly of the measured CPU solve (default: the largest family member that fits)')
     ap.add_argument('--real-storage', action='store_true',
                     help='--hv-only on real vectors in real storage (float64, as inside the solve)')
     ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')

@@ -129,6 +129,13 @@ int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host);
  * ED_ENOTSUP otherwise.  No counterpart in the reference (PETSc vectors there
  * are complex128). */
 int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev);
+/* ed_ham_apply_real fused with the two reductions a Lanczos step takes from
+ * the product: *xy_host = x^T y and *yy_host = ||y||^2 (either may be NULL),
+ * in the same pass over the rows (the H.v the eigensolver runs).  y equals
+ * ed_ham_apply_real's bit for bit.  Synchronises the context's stream.  No
+ * counterpart in the reference (SLEPc forms these with separate VecDot /
+ * VecNorm calls after MatMult). */
+int ed_ham_apply_real_dot(ed_ham* h, const double* x_dev, double* y_dev, double* xy_host, double* yy_host);
 /* y = H x (device vectors) without allocating any device memory: for
  * callers that cannot let a library call cudaMalloc, e.g. code running under
  * a framework that owns the whole device memory pool, or a loop that cannot
@@ -140,8 +147,12 @@ int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev);
  * ED_NOALLOC_MAX_STATES basis states (ED_EINVAL beyond), uniform J1/J2
  * Hamiltonians only (ED_ENOTSUP for per-bond ones).  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race on it, so order them. */
+ * that first call before any stream capture.  The address belongs to the
+ * device's context: after a device reset (cudaDeviceReset, or a framework
+ * resetting the primary context) the next call sees a new current context
+ * and looks the address up again, so make that call, too, outside a stream
+ * capture.  All calls share the array: calls that overlap on the GPU race on
+ * it, so order them. */
 #define ED_NOALLOC_MAX_STATES (1 << 22)
 int ed_ham_apply_noalloc(ed_ham* h, const ed_cplx* x_dev, ed_cplx* y_dev);
 /* Explicit CSR on the device (when it fits); then ed_ham_set_mode(ED_HAM_CSR)
@@ -197,8 +208,9 @@ int ed_eps_set_seed(ed_eps* e, uint64_t seed);
  * products.  ED_RESTART_PAIR: float-pair products on the FP32 units (each
  * FP64 value split into hi + lo, error below 2^-45 of |v y| per product;
  * storage and sums stay FP64), 1.5x faster on GB300, whose FP64 unit bounds
- * this step.  ED_RESTART_AUTO (default): pairs from 2^22 basis states up.
- * No counterpart in the reference (FP64 throughout). */
+ * this step, but below FP64 accuracy, so only on request.  ED_RESTART_AUTO
+ * (default): the fastest form whose every product is FP64 or better.  No
+ * counterpart in the reference (FP64 throughout). */
 #define ED_RESTART_AUTO 0
 #define ED_RESTART_FP64 1
 #define ED_RESTART_PAIR 2
@@ -237,8 +249,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
 /* Eigenvector i of realisation b into a contiguous device vector. */
 int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev);
 int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv);
-/* Products of the restart combination, as ed_eps_set_restart_arithmetic
- * (ED_RESTART_AUTO: float pairs from 2^22 entries of the [dim][B] block up). */
+/* Products of the restart combination, as ed_eps_set_restart_arithmetic. */
 int ed_batch_set_restart_arithmetic(ed_batch* bt, int mode);
 
 /* ---- measurements: replace SiSj/SzSz/SpSm/SmSp::ExpectVal

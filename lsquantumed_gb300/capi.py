@@ -69,6 +69,7 @@ SIGNATURES = {
     'ed_ham_apply': [vp, vp, vp],
     'ed_ham_apply_host': [vp, vp, vp],
     'ed_ham_apply_real': [vp, vp, vp],
+    'ed_ham_apply_real_dot': [vp, vp, vp, P(dbl), P(dbl)],
     'ed_ham_apply_noalloc': [vp, vp, vp],
     'ed_ham_build_csr': [vp, P(i64)],
     'ed_ham_set_mode': [vp, i32],

@@ -1025,10 +1025,9 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     // restart: new columns 0..l-1 = V Y_b[:, 0..l-1]
     std::vector<double*> outc(freel.begin(), freel.begin() + l_keep);
     {
-      // float-pair products from 2^22 block entries up (the FP64 unit bounds
-      // the FP64 form there), unless FP64 is forced
-      const bool pair = bt->restart_arith == ED_RESTART_PAIR ||
-                        (bt->restart_arith == ED_RESTART_AUTO && colA >= ((int64_t)1 << 22));
+      // float-pair products only on request: the default keeps every
+      // product at FP64 or better
+      const bool pair = bt->restart_arith == ED_RESTART_PAIR;
       if (pair) {
         // pageable source: staged by the time cudaMemcpyAsync returns
         std::vector<float2> Yp(Yall.size());

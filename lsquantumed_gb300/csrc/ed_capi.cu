@@ -455,6 +455,18 @@ int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev) {
   return ed_launch_hv_r(h, x_dev, y_dev);
 }
 
+int ed_ham_apply_real_dot(ed_ham* h, const double* x_dev, double* y_dev, double* xy_host, double* yy_host) {
+  if (!h || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
+  if (x_dev == y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");
+  if (!ed_lin_supported(h)) return ed_fail(ED_ENOTSUP, "real-storage H.v needs the two-table fixed-point kernel");
+  double2 dot;
+  double y2 = 0.0;
+  ED_TRY(ed_launch_hv_dot_any(h, x_dev, y_dev, true, &dot, &y2));
+  if (xy_host) *xy_host = dot.x;
+  if (yy_host) *yy_host = y2;
+  return ED_OK;
+}
+
 int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host) {
   if (!h || !x_host || !y_host) return ed_fail(ED_EINVAL, "null argument");
   ed_ctx* ctx = h->ctx;

@@ -271,8 +271,8 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
   }
   e->real_storage = true;
   e->real_coeffs = true;
-  e->restart_pair =
-      e->restart_arith == ED_RESTART_PAIR || (e->restart_arith == ED_RESTART_AUTO && n >= ((int64_t)1 << 22));
+  // float pairs only on request: the default keeps every product at FP64 or better
+  e->restart_pair = e->restart_arith == ED_RESTART_PAIR;
   std::vector<double*> freelist;
   e->col_r.assign(m + 1, nullptr);
   for (int i = 0; i < e->pool_cols; ++i) {

@@ -1042,18 +1042,47 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[ED_NOALLOC_HEAD
                                                                   (size_t)ED_NOALLOC_MAX_STATES * sizeof(longlong2)];
 
 static std::mutex g_noalloc_mutex;
+// Per device: the context the address was looked up in, and the address.  A
+// device reset (cudaDeviceReset, or a host framework resetting the primary
+// context) gives the device a new context and the array a new address, so the
+// cached one is used only while the current context is the one it came from.
+static void* g_noalloc_ctx[64] = {nullptr};
 static void* g_noalloc_ptr[64] = {nullptr};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side symbol is not a device address).
+// The driver's cuCtxGetCurrent, through the runtime (the library does not
+// link libcuda); nullptr where the driver does not provide it.
+typedef int (*ed_cu_ctx_get_current_t)(void**);
+static ed_cu_ctx_get_current_t noalloc_ctx_getter() {
+  static ed_cu_ctx_get_current_t fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (ed_cu_ctx_get_current_t)p;
+  }
+  return fn;
+}
+
+// Device address of the scratch array on the current device (the host-side
+// symbol is not a device address): looked up with cudaGetSymbolAddress the
+// first time on each device, and again whenever the device's current context
+// differs from the one of the cached address.
 static int noalloc_scratch(int device, unsigned char** out) {
   if (device < 0 || device >= 64) return ed_fail(ED_ENOTSUP, "device index above 63");
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[device]) {
+  void* cur = nullptr;
+  ed_cu_ctx_get_current_t get = noalloc_ctx_getter();
+  if (get && get(&cur) != 0) cur = nullptr;
+  if (!g_noalloc_ptr[device] || (cur && cur != g_noalloc_ctx[device])) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return ed_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    if (get && get(&cur) != 0) cur = nullptr;  // the lookup may have made the primary context current
     g_noalloc_ptr[device] = p;
+    g_noalloc_ctx[device] = cur;
   }
   *out = (unsigned char*)g_noalloc_ptr[device];
   return ED_OK;

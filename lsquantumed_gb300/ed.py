@@ -320,6 +320,23 @@ class Hamiltonian:
         call('ed_ham_apply_real', self._h, _p(xd), _p(y))
         return y
 
+    def apply_real_dot(self, x, out=None):
+        """(y, x^T y, ||y||^2) with y = H x in real storage, the three formed in
+        one pass over the rows (the product the eigensolver runs).  y equals
+        apply_real(x) bit for bit."""
+        torch = _torch()
+        if isinstance(x, np.ndarray):
+            x = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64))
+        if x.dtype != torch.float64 or x.numel() != self.size:
+            raise InvalidArgument(capi.ED_EINVAL, 'expected a float64 vector of %d entries' % self.size)
+        xd = x.to('cuda').contiguous()
+        y = out if out is not None else torch.empty_like(xd)
+        if y.dtype != torch.float64 or y.numel() != self.size or not y.is_contiguous():
+            raise InvalidArgument(capi.ED_EINVAL, 'out must be a contiguous float64 vector of %d entries' % self.size)
+        xy, yy = ctypes.c_double(), ctypes.c_double()
+        call('ed_ham_apply_real_dot', self._h, _p(xd), _p(y), ctypes.byref(xy), ctypes.byref(yy))
+        return y, xy.value, yy.value
+
     def mult(self, x, y):
         call('ed_ham_apply', self._h, _p(x), _p(y))
         return 0

@@ -720,6 +720,69 @@ void orc_model_apply(void* m, const double* x, double* y) {
 }
 void orc_start_vector(uint64_t seed, int64_t n, double* v) { start_vector(seed, n, (cplx*)v); }
 
+// Real parts of the seeded start vector (the entries start_vector writes into
+// the real parts), for inputs too large to hold twice.
+void orc_start_vector_r(uint64_t seed, int64_t n, double* v) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    uint64_t h1 = splitmix64(seed * 0xD1B54A32D192ED03ull + 2 * (uint64_t)i);
+    v[i] = 2.0 * u01(h1) - 1.0;
+  }
+}
+
+// Selected rows of y = H x for the assembled uniform-coupling Hamiltonian
+// (build_diag then build_off_diag), evaluated row by row without building
+// the basis or the matrix, so that it runs at any N the ranks fit:
+//   state  = BasisHelper::search_elem(row)            src/basis.cpp:9-36
+//   diag   = build_diag's rule on get_elem_diag       include/hamiltonian.tmpl_func.hpp:129-225, :391-426
+//   cols   = get_coup_elems, nn pass then nnn pass    include/hamiltonian.tmpl_func.hpp:229-344, :350-387
+//            (flip both bits, HamiltHelper::search_index, src/hamiltonian.cpp:9-27)
+//   y[row] = diag * x[row] + sum_cols J * 0.5 * x[col]
+// x is the seeded start vector (entries computed on demand from the same
+// counter hash); complex_x = 0 takes its real parts only.  y_out holds
+// (re, im) per requested row.
+void orc_rows_apply_seeded(int ltype, int nspins, int lx, int ly, int total_mag, double J1, double D1, double J2,
+                           double D2, uint64_t seed, int complex_x, int64_t nrows, const int64_t* rows,
+                           double* y_out) {
+  binom_init();
+  const int nup = total_mag + nspins / 2;
+  Lat L = make_lat(ltype, nspins, lx, ly);
+  const uint64_t base = seed * 0xD1B54A32D192ED03ull;
+  auto xv = [&](int64_t i) {
+    double re = 2.0 * u01(splitmix64(base + 2 * (uint64_t)i)) - 1.0;
+    double im = complex_x ? 2.0 * u01(splitmix64(base + 2 * (uint64_t)i + 1)) - 1.0 : 0.0;
+    return cplx(re, im);
+  };
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t q = 0; q < nrows; ++q) {
+    const int64_t r = rows[q];
+    const uint64_t s = orc_search_elem(r, nspins, nup);
+    double dval = 0.0;
+    if (!(std::fabs(D1) < 1e-14 && std::fabs(D2) < 1e-14)) {
+      if (std::fabs(D1) >= 1e-14) {
+        int64_t t = elem_diag(0, s, L);
+        if (t != 0) dval += D1 * 0.25 * t;
+      }
+      if (std::fabs(D2) >= 1e-14) {
+        int64_t t = elem_diag(1, s, L);
+        if (t != 0) dval += D2 * 0.25 * t;
+      }
+    }
+    cplx acc = dval * xv(r);
+    std::vector<int64_t> cols;
+    if (std::fabs(J1) >= 1e-14) {
+      coup_elems(0, s, L, cols);
+      for (int64_t c : cols) acc += (J1 * 0.5) * xv(c);
+    }
+    if (std::fabs(J2) >= 1e-14) {
+      coup_elems(1, s, L, cols);
+      for (int64_t c : cols) acc += (J2 * 0.5) * xv(c);
+    }
+    y_out[2 * q] = acc.real();
+    y_out[2 * q + 1] = acc.imag();
+  }
+}
+
 // Krylov-Schur on the explicit matrix.  evals/errs sized >= ncv; evecs
 // (nullable) n x ncv complex column-major.  Returns the number of Ritz pairs
 // reported (>= nconv).

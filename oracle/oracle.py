@@ -64,6 +64,9 @@ def lib():
                 'orc_model_diag': (None, [vp, vp]),
                 'orc_model_apply': (None, [vp, vp, vp]),
                 'orc_start_vector': (None, [u64, i64, vp]),
+                'orc_start_vector_r': (None, [u64, i64, vp]),
+                'orc_rows_apply_seeded': (None, [i32, i32, i32, i32, i32, dbl, dbl, dbl, dbl, u64, i32, i64, vp,
+                                                 vp]),
                 'orc_eps_solve': (i32, [vp, i32, i32, i32, dbl, i32, u64, vp, vp, vp, P(i32), P(i32), P(i64)]),
                 'orc_expect': (None, [vp, i32, i32, i32, vp, vp]),
                 'orc_sqz': (None, [vp, i32, vp, vp]),
@@ -180,6 +183,26 @@ def start_vector(seed, n):
     out = np.zeros(n, dtype=np.complex128)
     lib().orc_start_vector(seed, n, _p(out))
     return out
+
+
+def start_vector_r(seed, n):
+    """Real parts of start_vector(seed, n), without the complex copy."""
+    out = np.zeros(n, dtype=np.float64)
+    lib().orc_start_vector_r(seed, n, _p(out))
+    return out
+
+
+def rows_apply_seeded(ltype, nspins, lx, ly, total_mag, J1, D1, J2, D2, seed, rows, complex_x=False):
+    """Rows `rows` of H x for the uniform-coupling Hamiltonian (build_diag +
+    build_off_diag), x = start_vector(seed) (its real parts unless complex_x),
+    each row evaluated on its own from the reference's per-row rules; no
+    basis or matrix is built, so any N whose ranks fit 64 bits works."""
+    r = np.ascontiguousarray(rows, dtype=np.int64)
+    out = np.zeros(2 * len(r), dtype=np.float64)
+    lib().orc_rows_apply_seeded(ltype, nspins, lx, ly, total_mag, J1, D1, J2, D2, seed, 1 if complex_x else 0,
+                                len(r), _p(r), _p(out))
+    y = out[0::2] + 1j * out[1::2]
+    return y if complex_x else y.real.copy()
 
 
 def vecdot(x, y):

@@ -71,21 +71,50 @@ def test_c3_cpu_sample(bench):
 
 
 def test_reference_arm_json_contract():
-    """`bench.py --impl reference` (the oracle port on the host cores, bounded
-    sample) prints one JSON line with the same metric and workload as the GPU
-    arm, impl "reference", a cpu_baseline describing the run, and an e2e
-    entry with no host-device bytes."""
+    """`bench.py --impl reference` (the oracle port on the host cores: full CPU
+    eigensolves of a smaller member of the workload's family, here the 4x4
+    lattice to keep the test short) prints one JSON line with the same metric
+    and workload as the GPU arm, impl "reference", steps = the solves it
+    actually ran, a cpu_baseline that carries the measured solve and labels
+    the extrapolated value, and an e2e entry with no host-device bytes."""
     import json
     import subprocess
     import sys
-    r = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--steps', '1',
-                        '--warmup', '0'], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--steps', '5',
+                        '--warmup', '3', '--cpu-size', '16,4,4'], capture_output=True, text=True, timeout=600,
+                       cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line['impl'] == 'reference'
     assert line['unit'] == 's' and line['higher_is_better'] is False
     assert line['config']['workload'].startswith('c5 ') and line['config']['dim'] == 155117520
+    assert line['steps'] == 2 and line['warmup'] == 0  # solves actually run (capped at 2)
     cb = line['cpu_baseline']
-    assert cb['kind'] in ('port', 'reference') and cb['cores'] >= 1 and cb['value'] == line['value'] > 0
-    assert 'times 334 H.v per solve' in cb['sample']
+    assert cb['kind'] == 'port-extrapolated' and cb['cores'] >= 1 and cb['value'] == line['value'] > 0
+    m = cb['measured']
+    assert m['N'] == 16 and m['dim'] == 12870 and m['nhv'] > 0 and len(m['solve_s_each']) == 2
+    assert abs(line['timed_region_s'] - sum(m['solve_s_each'])) < 1e-9
+    assert cb['host']['logical_cores'] >= 1
     assert line['e2e'] == {'value': line['value'], 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
+
+
+def test_cpu_extrapolation_model(bench):
+    """The N=30 estimate scales the measured per-step SpMV by stored entries
+    and the rest of the step by basis size, times the H.v count."""
+    meas = {'N': 24, 'lattice': '4x6', 'dim': 2704156, 'nnz': 137980548, 'solve_s': 30.0, 'nhv': 300,
+            'spmv_s': 0.06}
+    t, note = bench.cpu_extrapolate(meas, 'c5', 334)
+    dim30 = 155117520
+    nnz30 = dim30 * (1 + 120 * 30 / (2 * 29))
+    want = 334 * (0.06 * nnz30 / meas['nnz'] + 0.04 * dim30 / meas['dim'])
+    assert abs(t - want) <= 1e-9 * want
+    assert 'times 334 H.v' in note
+
+
+def test_host_info(bench):
+    info = bench.host_info()
+    assert info['logical_cores'] >= 1
+    sizes = info['explicit_matrix_bytes']
+    # N=30 6x5: 155M rows x (1 + 62.07) entries x 24 B = 235 GB
+    assert 230e9 < sizes['N=30 6x5'] < 240e9
+    assert 3.0e9 < sizes['N=24 4x6'] < 3.6e9

@@ -122,6 +122,30 @@ def test_matrices(golden, orc):
                     assert _close_g(v, w), (rec['name'], r, c, v, w)
 
 
+@pytest.mark.parametrize('case', [
+    (0, 12, 1, 12, 0, 1.0, 1.0, 0.0, 0.0),
+    (1, 8, 2, 4, 1, 1.0, 0.3, 0.55, 0.2),   # 2x4: every bond appears twice
+    (1, 12, 4, 3, 0, 1.0, 1.0, 0.5, 0.5),
+    (1, 16, 4, 4, -2, 0.7, 1.3, 0.55, 0.55),
+    (2, 12, 6, 2, 0, 1.0, 1.0, 0.5, 0.5),
+    (1, 20, 4, 5, 0, 1.0, 1.0, 0.5, 0.5),
+])
+def test_rows_apply_matches_matrix(orc, case):
+    """The row-by-row restatement (used at N=30, where no matrix fits) equals
+    the explicit matrix built by the golden-pinned restatement on every row,
+    to summation order (1e-13 absolute, |x_i| < 1), real and complex input."""
+    ltype, N, lx, ly, mag, J1, D1, J2, D2 = case
+    M = Model(ltype, N, lx, ly, mag, J1, D1, J2, D2)
+    M.build(3)
+    rows = np.arange(M.dim, dtype=np.int64)
+    x = orc.start_vector(7, M.dim)
+    got = orc.rows_apply_seeded(ltype, N, lx, ly, mag, J1, D1, J2, D2, 7, rows, complex_x=True)
+    assert np.abs(got - M.apply(x)).max() <= 1e-13
+    got_r = orc.rows_apply_seeded(ltype, N, lx, ly, mag, J1, D1, J2, D2, 7, rows)
+    assert np.abs(got_r - M.apply(x.real.astype(np.complex128)).real).max() <= 1e-13
+    assert np.array_equal(orc.start_vector_r(7, M.dim), x.real)
+
+
 def _solve(M, nev, tol=1e-12):
     return M.eps_solve(nev=nev, ncv=max(2 * nev, nev + 15), tol=tol, seed=0)
 

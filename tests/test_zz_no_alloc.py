@@ -4,10 +4,11 @@ or a loop that cannot afford an allocation's synchronisation).  It keeps its
 scratch in one static device array, so the call allocates nothing.
 
 Checked through the C ABI against ed_ham_apply, which computes the same
-fixed-point H.v with buffers it allocates itself: two calls in a row (the
-shared scratch must not carry stale state into the second call), within the
-H.v tolerance the other tests use (1e-14 * ||x||_2).  This file is collected
-last so a failure here leaves every other test already run.
+fixed-point H.v with buffers it allocates itself, and against the oracle's
+explicit-matrix product: two calls in a row (the shared scratch must not
+carry stale state into the second call), within the H.v tolerance the other
+tests use (1e-14 * ||x||_2).  This file is collected last so a failure here
+leaves every other test already run.
 """
 import ctypes
 
@@ -36,11 +37,14 @@ def _ham(ed, env, N, lx, ly, mag):
 
 def test_noalloc_matches_apply_twice(setup):
     import torch
+    import oracle
     ed = setup
     lib = ed.capi.lib()
     env = ed.Environment(nspins=20)
     b, h = _ham(ed, env, 20, 4, 5, 0)
     h.set_accumulation('fixed64')
+    M = oracle.Model(1, 20, 4, 5, 0, 1.0, 1.0, 0.5, 0.5)
+    M.build(3)
     gen = torch.Generator(device='cuda').manual_seed(1234)
     for call in range(2):
         x = torch.complex(torch.rand(b.size, dtype=torch.float64, device='cuda', generator=gen) * 2 - 1,
@@ -61,6 +65,8 @@ def test_noalloc_matches_apply_twice(setup):
         tol = 1e-14 * torch.linalg.vector_norm(x).item()
         err = (y_new - y_ref).abs().max().item()
         assert err <= tol, (call, err, tol)
+        err_orc = np.abs(y_new.cpu().numpy() - M.apply(x.cpu().numpy())).max()
+        assert err_orc <= tol, (call, err_orc, tol)
 
 
 def test_noalloc_rejects_large_basis(setup):
