@@ -283,7 +283,7 @@ def run_reference(args):
             'config': workload_config(wl), 'impl': 'reference', 'cpu_baseline': cpu,
             'timed_region_s': sum(r['solve_s'] for r in runs),
             'e2e': {'value': v, 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
-    print(json.dumps(line))
+    print(json.dumps(line, default=_json_default))
     return 0
 
 
@@ -481,7 +481,7 @@ def run_disorder(args):
             'batched': out, 'cpu_baseline': cpu, 'dtype': 'f64', 'data': 'synthetic',
             'dtype_note': DTYPE_NOTE,
             'config': {'workload': 'c3 ' + r['config'].replace('seeds 0..', 'seeds 0..')}}
-    print(json.dumps(line))
+    print(json.dumps(line, default=_json_default))
     return 0
 
 
@@ -537,7 +537,7 @@ def gradient_timing(ed, restart='auto', seed=71):
         far = (lx // 2) * ly + ly // 2
         obs = [(1.0, ed.Adjoint.SISJ, 0, far)]
         t0 = time.perf_counter()
-        val, cJ, cD, ch, info = ed.Adjoint.expectation_gradient(h, pairs, e[0], v0, obs, tol=1e-10)
+        val, cJ, cD, ch, info = ed.Adjoint.expectation_gradient(h, pairs, e[0], v0, obs, tol=1e-9, max_it=4000)
         t_corr = time.perf_counter() - t0
         ed.Solver.SolverClean(eps)
         d = 1e-5
@@ -777,6 +777,7 @@ def run_ours(args):
     cpu = None
     same = None
     c3 = c4 = None
+    t_cpu = time.perf_counter()
     if rk == 0 and not args.no_cpu:
         try:
             cs = CpuSolve(wl)
@@ -797,15 +798,27 @@ def run_ours(args):
             cpu['host'] = host_info()
         except Exception as ex:  # reported, never fatal
             cpu = {'value': None, 'unit': 's', 'cores': None, 'kind': 'port', 'sample': 'failed: %s' % ex}
+    sections = {'cpu_baseline_and_same_size_s': time.perf_counter() - t_cpu}
+    rates = None
+    if rk == 0:
+        try:
+            rates = env.probe_rates()
+        except Exception as ex:
+            rates = {'failed': str(ex)}
     if rk == 0 and wl == 'c5' and not args.no_extra:
+        t0 = time.perf_counter()
         try:
             c3 = disorder_sweep(ed, env, list(range(args.seeds)), args.restart, args.plain_sample)
+            c3 = {k: v for k, v in c3.items() if k not in ('fields', 'batch_evals')}
         except Exception as ex:
             c3 = {'failed': str(ex)}
+        sections['c3_s'] = time.perf_counter() - t0
+        t0 = time.perf_counter()
         try:
             c4 = gradient_timing(ed, args.restart)
         except Exception as ex:
             c4 = {'failed': str(ex)}
+        sections['c4_s'] = time.perf_counter() - t0
 
     if rk != 0:
         return 0
@@ -833,9 +846,20 @@ def run_ours(args):
                    'eigenvalues': evals,
                    'rel_residuals': errs},
         'clocks': clocks, 'cpu_baseline': cpu, 'same_size_gpu_vs_cpu': same, 'c3': c3, 'c4': c4,
+        'unit_rates': rates, 'bench_sections_s': sections,
     }
-    print(json.dumps(line))
+    print(json.dumps(line, default=_json_default))
     return 0
+
+
+def _json_default(o):
+    """numpy scalars and arrays in the JSON line."""
+    import numpy as np
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    if isinstance(o, np.generic):
+        return o.item()
+    raise TypeError('not JSON serializable: %r' % type(o))
 
 
 def device_solve_seconds(ed, env_unused, N, lx, ly, wl, restart, reps=3):
@@ -908,6 +932,8 @@ def main():
                     help='restart-combination products of the real-storage solve (auto: the fastest form with every '
                          'product FP64 or better; pair: float pairs on the FP32 units)')
     ap.add_argument('--no-extra', action='store_true', help='skip the C3 / C4 sub-objects of the default line')
+    ap.add_argument('--probe-rates', action='store_true',
+                    help='print the measured FP64 FMA / FP64 mma / FP16-FP32 mma rates and exit')
     ap.add_argument('--cpu-size', default=None,
                     help='N,lx,ly of the measured CPU solve (default: the largest family member that fits)')
     ap.add_argument('--real-storage', action='store_true',
@@ -925,6 +951,12 @@ def main():
         return run_reference(args)
     if args.hv_only:
         return run_hv_only(args)
+    if args.probe_rates:
+        from lsquantumed_gb300.build import build
+        build()
+        import lsquantumed_gb300 as ed
+        print(json.dumps(ed.Environment(nspins=2).probe_rates()))
+        return 0
     if args.workload == 'c3':
         return run_disorder(args)
     return run_ours(args)

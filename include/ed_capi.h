@@ -67,6 +67,13 @@ int ed_ctx_profile(ed_ctx* ctx, int enable);
 /* H.v launches recorded and their summed device time in milliseconds. */
 int ed_ctx_profile_read(ed_ctx* ctx, int64_t* n_hv, double* ms_hv);
 
+/* Arithmetic rates of the units the dense contractions could use, measured on
+ * the context's device in TFLOP/s (register-resident loops on every SM, CUDA
+ * events): FP64 FMA, FP64 tensor mma (m8n8k4), and FP16-input FP32-accumulate
+ * tensor mma (m16n8k16).  Any output may be NULL.  No counterpart in the
+ * reference; for the benchmark's reports. */
+int ed_probe_rates(ed_ctx* ctx, double* dfma_tflops, double* dmma_tflops, double* hmma_tflops);
+
 /* ---- device vectors: replace MatCreateVecs / VecDestroy / VecGetArray ---- */
 /* n complex128 entries on the context's device (uninitialised). */
 int ed_vec_create(ed_ctx* ctx, int64_t n, ed_cplx** vec_dev);
@@ -207,14 +214,39 @@ int ed_eps_set_seed(ed_eps* e, uint64_t seed);
  * the two-table H.v).  ED_RESTART_FP64: FP64 FMA beside exact integer
  * products.  ED_RESTART_PAIR: float-pair products on the FP32 units (each
  * FP64 value split into hi + lo, error below 2^-45 of |v y| per product;
- * storage and sums stay FP64), 1.5x faster on GB300, whose FP64 unit bounds
- * this step, but below FP64 accuracy, so only on request.  ED_RESTART_AUTO
- * (default): the fastest form whose every product is FP64 or better.  No
- * counterpart in the reference (FP64 throughout). */
+ * storage and sums stay FP64), below FP64 accuracy, so only on request.
+ * ED_RESTART_EXACT: exact slices on the tensor cores for the restart
+ * combination and the Gram-Schmidt projections (ed_bv_mult_real,
+ * ed_bv_dot_real; ncv <= 32).  ED_RESTART_AUTO (default): ED_RESTART_FP64.
+ * No counterpart in the reference (FP64 throughout). */
 #define ED_RESTART_AUTO 0
 #define ED_RESTART_FP64 1
 #define ED_RESTART_PAIR 2
+#define ED_RESTART_EXACT 3
 int ed_eps_set_restart_arithmetic(ed_eps* e, int mode);
+/* The restart combination on its own: out_c = sum_{i<m} V_i Y[i*ldY + c] for
+ * c < l, real device vectors of n entries (V_dev and out_dev: host arrays of
+ * device pointers; out must not alias V; Y on the host).  This is SLEPc's
+ * BVMultInPlace inside the Krylov-Schur restart (reached from EPSSolve,
+ * src/solver.cpp:45).  arith: ED_RESTART_FP64, ED_RESTART_PAIR, or
+ * ED_RESTART_EXACT: the products on the tensor cores in exact 8-bit slices of
+ * 63-bit fixed point (per 128-row tile of V, per column of Y), level sums
+ * combined exactly and rounded once to FP64 (m <= 32, ED_ENOTSUP beyond);
+ * ED_RESTART_AUTO picks what the solver would by default (ED_RESTART_FP64).
+ * Synchronises the stream. */
+int ed_bv_mult_real(ed_ctx* ctx, const double* const* V_dev, int m, const double* Y_host, int ldY, int l,
+                    double* const* out_dev, int64_t n, int arith);
+/* The Gram-Schmidt projection on its own: h_host[i] = V_i^T w, i < m, real
+ * device vectors of n entries with |V_i entries| <= 1 (orthonormal columns,
+ * as in the Krylov basis); SLEPc's BVDotVec in the orthogonalisation of the
+ * Krylov-Schur expansion (reached from EPSSolve, src/solver.cpp:45).
+ * arith: ED_RESTART_FP64 / ED_RESTART_AUTO (FP64 FMA), or ED_RESTART_EXACT:
+ * the products on the tensor cores in exact 8-bit slices of 63-bit fixed
+ * point (per 128-row tile and column), summed exactly within each CTA,
+ * rounded once per slice level and CTA and summed in FP64 across CTAs.
+ * Synchronises the stream. */
+int ed_bv_dot_real(ed_ctx* ctx, const double* const* V_dev, int m, const double* w_dev, int64_t n, int arith,
+                   double* h_host);
 /* EPSSetInitialSpace with one vector (normalised by the solver); on_device
  * selects whether v points to device or host memory.  NULL clears it. */
 int ed_eps_set_initial_vector(ed_eps* e, const ed_cplx* v, int on_device);

@@ -1,10 +1,13 @@
 // lsqed.hpp — header-only C++ shim that re-creates LSQuantumED's hot-path
-// class interfaces on top of the C ABI in ed_capi.h, so drivers written
-// against the reference (examples/main.cpp, main_disorder.cpp, ex1-4.cpp)
-// keep their structure.  PETSc types map as: PetscInt -> int64_t,
-// PetscReal -> double, PetscScalar -> std::complex<double>,
-// PetscErrorCode -> int, Mat -> the Hamiltonian itself, Vec -> lsqed::Vec
-// (a device vector), EPS -> lsqed::EPS.
+// class interfaces on top of the C ABI in ed_capi.h, with the PETSc handle
+// types the reference's drivers use: Mat (Hamiltonian<L>::hamilt), Vec
+// (device vectors from MatCreateVecs, freed by VecDestroy) and EPS.  PETSc
+// types map as: PetscInt -> int64_t, PetscReal -> double, PetscScalar ->
+// lsqed::Scalar (complex, converting to its real part where a double is
+// expected, as PETSc's C complex scalars do in C++), PetscErrorCode -> int.
+// lsqed_dropin.hpp adds the global names, option parsing and logging calls
+// so that the reference's drivers (examples/main.cpp, main_disorder.cpp,
+// ex1-4.cpp) compile with only their #include lines replaced.
 //
 // Link with -ledgb300 (lsquantumed_gb300/_lib/libedgb300.so).
 #pragma once
@@ -22,10 +25,56 @@ namespace lsqed {
 
 typedef int64_t PetscInt;
 typedef double PetscReal;
-typedef std::complex<double> PetscScalar;
 typedef int PetscErrorCode;
+enum PetscBool { PETSC_FALSE = 0, PETSC_TRUE = 1 };
 static const PetscInt PETSC_DECIDE = -1;
 static const PetscInt PETSC_DEFAULT = -2;
+
+// Complex scalar (complex128).  It converts implicitly to double (its real
+// part) and from double, and mixes with double in arithmetic, like PETSc's
+// C complex scalars in C++ code: drivers written for real and for complex
+// PETSc builds compile against it unchanged.
+struct Scalar {
+  double re = 0.0, im = 0.0;
+  Scalar() {}
+  Scalar(double r) : re(r) {}
+  Scalar(double r, double i) : re(r), im(i) {}
+  Scalar(const std::complex<double>& z) : re(z.real()), im(z.imag()) {}
+  operator double() const { return re; }
+  std::complex<double> c() const { return std::complex<double>(re, im); }
+  double real() const { return re; }
+  double imag() const { return im; }
+  Scalar& operator+=(const Scalar& o) { re += o.re; im += o.im; return *this; }
+  Scalar& operator-=(const Scalar& o) { re -= o.re; im -= o.im; return *this; }
+  Scalar& operator*=(const Scalar& o) { *this = Scalar(c() * o.c()); return *this; }
+  Scalar& operator/=(const Scalar& o) { *this = Scalar(c() / o.c()); return *this; }
+  Scalar& operator+=(double o) { re += o; return *this; }
+  Scalar& operator-=(double o) { re -= o; return *this; }
+  Scalar& operator*=(double o) { re *= o; im *= o; return *this; }
+  Scalar& operator/=(double o) { re /= o; im /= o; return *this; }
+};
+inline Scalar operator+(Scalar a, const Scalar& b) { return a += b; }
+inline Scalar operator-(Scalar a, const Scalar& b) { return a -= b; }
+inline Scalar operator*(Scalar a, const Scalar& b) { return a *= b; }
+inline Scalar operator/(Scalar a, const Scalar& b) { return a /= b; }
+inline Scalar operator+(Scalar a, double b) { return a += b; }
+inline Scalar operator-(Scalar a, double b) { return a -= b; }
+inline Scalar operator*(Scalar a, double b) { return a *= b; }
+inline Scalar operator/(Scalar a, double b) { return a /= b; }
+inline Scalar operator+(double a, const Scalar& b) { return Scalar(a) += b; }
+inline Scalar operator-(double a, const Scalar& b) { return Scalar(a) -= b; }
+inline Scalar operator*(double a, const Scalar& b) { return Scalar(a) *= b; }
+inline Scalar operator/(double a, const Scalar& b) { return Scalar(a) /= b; }
+inline Scalar operator+(Scalar a, int b) { return a += (double)b; }
+inline Scalar operator*(Scalar a, int b) { return a *= (double)b; }
+inline Scalar operator/(Scalar a, int b) { return a /= (double)b; }
+inline Scalar operator/(Scalar a, PetscInt b) { return a /= (double)b; }
+inline Scalar operator-(const Scalar& a) { return Scalar(-a.re, -a.im); }
+typedef Scalar PetscScalar;
+inline double PetscRealPart(const Scalar& z) { return z.re; }
+inline double PetscRealPart(double x) { return x; }
+inline double PetscImaginaryPart(const Scalar& z) { return z.im; }
+inline double PetscImaginaryPart(double) { return 0.0; }
 
 inline std::string last_error() {
   char buf[1024];
@@ -40,6 +89,11 @@ inline void throw_on(int rc) {
   if (rc == ED_EINVAL) throw std::invalid_argument(last_error());
   throw std::runtime_error(last_error());
 }
+#define ED_TRY_SHIM(expr)           \
+  do {                              \
+    int _rc = (expr);               \
+    if (_rc != ED_OK) return _rc;   \
+  } while (0)
 
 // ---------------------------------------------------------------------------
 // Environment (include/environment.hpp:20-53)
@@ -65,6 +119,16 @@ inline void parse_solver_options(int argc, char** argv) {
   }
 }
 
+// The command line, kept for the option queries of the drivers (the
+// reference's PETSc options database, filled by SlepcInitialize).
+struct CommandLine {
+  std::vector<std::string> args;
+};
+inline CommandLine& command_line() {
+  static CommandLine c;
+  return c;
+}
+
 class Environment {
  public:
   PetscInt nspins = 0;
@@ -72,20 +136,24 @@ class Environment {
   bool disorder_flg = false;
   ed_ctx* ctx = nullptr;
 
-  Environment(int argc, char** argv, const char* /*help*/ = nullptr) {
-    parse_solver_options(argc, argv);
-    throw_on(ed_ctx_create(0, nullptr, &ctx));
-  }
+  Environment(int argc, char** argv, const char* /*help*/ = nullptr) { init(argc, argv); }
   Environment(int argc, char** argv, PetscInt m_nspins, const char* /*help*/ = nullptr) {
     if (m_nspins % 2 != 0) throw std::invalid_argument("The total number of spins has to be EVEN.");
     if (m_nspins <= 0) throw std::invalid_argument("The total number of spins has to be POSITIVE.");
     nspins = m_nspins;
-    parse_solver_options(argc, argv);
-    throw_on(ed_ctx_create(0, nullptr, &ctx));
+    init(argc, argv);
   }
   ~Environment() { ed_ctx_destroy(ctx); }
   Environment(const Environment&) = delete;
   Environment& operator=(const Environment&) = delete;
+
+ private:
+  void init(int argc, char** argv) {
+    command_line().args.assign(argv, argv + (argv ? argc : 0));
+    parse_solver_options(argc, argv);
+    if (ed_ctx_create(0, nullptr, &ctx) != ED_OK)
+      throw std::runtime_error("Slepc was not correctly initialized\n" + last_error());
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -148,27 +216,61 @@ class honeycomb2D : public Lattice {
 };
 
 // ---------------------------------------------------------------------------
-// Device vector (PETSc Vec), created by MatCreateVecs(h)
+// PETSc handles: Vec (a device vector of complex128 entries) and Mat (the
+// Hamiltonian's matrix-free operator).  MatCreateVecs / VecDestroy follow
+// PETSc's calling convention (src/solver.cpp, examples/*.cpp).
 // ---------------------------------------------------------------------------
-class Vec {
- public:
+struct _p_Vec {
   ed_ctx* ctx = nullptr;
   ed_cplx* d = nullptr;
   PetscInt n = 0;
-  Vec() {}
-  Vec(Environment& env, PetscInt size) : ctx(env.ctx), n(size) { throw_on(ed_vec_create(ctx, n, &d)); }
-  ~Vec() { ed_vec_destroy(d); }
-  Vec(const Vec&) = delete;
-  Vec& operator=(const Vec&) = delete;
-  std::vector<PetscScalar> to_host() const {
-    std::vector<PetscScalar> out((size_t)n);
-    throw_on(ed_vec_to_host(ctx, d, reinterpret_cast<ed_cplx*>(out.data()), n));
-    return out;
-  }
-  void from_host(const std::vector<PetscScalar>& v) {
-    throw_on(ed_vec_from_host(ctx, reinterpret_cast<const ed_cplx*>(v.data()), d, n));
-  }
 };
+typedef _p_Vec* Vec;
+struct _p_Mat {
+  ed_ctx* ctx = nullptr;
+  ed_ham* h = nullptr;
+  PetscInt n = 0;
+};
+typedef _p_Mat* Mat;
+
+inline PetscErrorCode VecCreateOnDevice(ed_ctx* ctx, PetscInt n, Vec* v) {
+  Vec x = new _p_Vec();
+  x->ctx = ctx;
+  x->n = n;
+  int rc = ed_vec_create(ctx, n, &x->d);
+  if (rc != ED_OK) {
+    delete x;
+    return rc;
+  }
+  *v = x;
+  return ED_OK;
+}
+// MatCreateVecs(mat, &right, &left): vectors the operator can act on / fill.
+inline PetscErrorCode MatCreateVecs(Mat A, Vec* right, Vec* left) {
+  if (!A) return ED_EINVAL;
+  if (right) ED_TRY_SHIM(VecCreateOnDevice(A->ctx, A->n, right));
+  if (left) ED_TRY_SHIM(VecCreateOnDevice(A->ctx, A->n, left));
+  return ED_OK;
+}
+inline PetscErrorCode VecDestroy(Vec* v) {
+  if (!v || !*v) return ED_OK;
+  ed_vec_destroy((*v)->d);
+  delete *v;
+  *v = nullptr;
+  return ED_OK;
+}
+inline PetscErrorCode VecGetSize(Vec v, PetscInt* n) {
+  *n = v ? v->n : 0;
+  return ED_OK;
+}
+// Host copies (VecGetArray with a copy back), for drivers that post-process.
+inline std::vector<PetscScalar> VecToHost(Vec v) {
+  std::vector<ed_cplx> tmp((size_t)v->n);
+  throw_on(ed_vec_to_host(v->ctx, v->d, tmp.data(), v->n));
+  std::vector<PetscScalar> out((size_t)v->n);
+  for (size_t k = 0; k < tmp.size(); ++k) out[k] = PetscScalar(tmp[k].re, tmp[k].im);
+  return out;
+}
 
 // ---------------------------------------------------------------------------
 // Hamiltonian<L> (include/hamiltonian.hpp:187-299)
@@ -176,26 +278,35 @@ class Vec {
 template <typename L>
 class Hamiltonian {
  public:
-  ed_ham* hamilt = nullptr;  // the reference's `Mat hamilt`
+  Mat hamilt = nullptr;  // the reference's `Mat hamilt` (hamiltonian.hpp:187)
   Basis& basis;
   L& lattice;
   PetscReal J1, Delta1, J2, Delta2;
 
   Hamiltonian(Environment& env, Basis& b, L& lat, PetscReal m_J1, PetscReal m_D1, PetscReal m_J2, PetscReal m_D2)
       : basis(b), lattice(lat), J1(m_J1), Delta1(m_D1), J2(m_J2), Delta2(m_D2) {
+    hamilt = new _p_Mat();
+    hamilt->ctx = env.ctx;
+    hamilt->n = b.size;
     int rc = ed_ham_create(env.ctx, b.h, lat.nn.data(), (int64_t)lat.nn.size() / 2, lat.nnn.data(),
-                           (int64_t)lat.nnn.size() / 2, J1, Delta1, J2, Delta2, &hamilt);
-    if (rc != ED_OK) throw std::runtime_error("The matrix has not been properly initialized.\n" + last_error());
+                           (int64_t)lat.nnn.size() / 2, J1, Delta1, J2, Delta2, &hamilt->h);
+    if (rc != ED_OK) {
+      delete hamilt;
+      throw std::runtime_error("The matrix has not been properly initialized.\n" + last_error());
+    }
   }
-  ~Hamiltonian() { ed_ham_destroy(hamilt); }
+  ~Hamiltonian() {
+    ed_ham_destroy(hamilt->h);
+    delete hamilt;
+  }
   Hamiltonian(const Hamiltonian&) = delete;
   Hamiltonian& operator=(const Hamiltonian&) = delete;
 
-  PetscErrorCode build_diag(Environment&) { return ed_ham_build_diag(hamilt); }
-  PetscErrorCode build_off_diag(Environment&) { return ed_ham_build_off_diag(hamilt); }
+  PetscErrorCode build_diag(Environment&) { return ed_ham_build_diag(hamilt->h); }
+  PetscErrorCode build_off_diag(Environment&) { return ed_ham_build_off_diag(hamilt->h); }
   PetscErrorCode build_disorder(Environment& env, PetscReal* hi) {
     env.disorder_flg = true;
-    return ed_ham_build_disorder(hamilt, hi);
+    return ed_ham_build_disorder(hamilt->h, hi);
   }
   PetscInt hamilt_size() const { return basis.size; }
   PetscReal hamilt_J1() const { return J1; }
@@ -212,10 +323,13 @@ struct EPS {
 };
 
 namespace Solver {
-template <typename L>
-inline PetscErrorCode SolverInit(EPS& solver, Hamiltonian<L>& h, PetscInt nev, PetscInt ncv = PETSC_DEFAULT,
+// SolverInit(EPS&, Mat, nev, ncv, mpd) (include/solver.hpp:27-31):
+// Hermitian, Krylov-Schur, smallest real; -eps_tol / -eps_max_it of the
+// command line applied as EPSSetFromOptions would.
+inline PetscErrorCode SolverInit(EPS& solver, Mat matrix, PetscInt nev, PetscInt ncv = PETSC_DEFAULT,
                                  PetscInt mpd = PETSC_DEFAULT) {
-  PetscErrorCode rc = ed_eps_create(h.hamilt, (int)nev, (int)ncv, (int)mpd, &solver.e);
+  if (!matrix) return ED_EINVAL;
+  PetscErrorCode rc = ed_eps_create(matrix->h, (int)nev, (int)ncv, (int)mpd, &solver.e);
   const SolverOptions& o = solver_options();  // EPSSetFromOptions
   if (rc == ED_OK && (o.eps_tol > 0.0 || o.eps_max_it > 0)) rc = ed_eps_set_tolerances(solver.e, o.eps_tol, o.eps_max_it);
   return rc;
@@ -233,12 +347,20 @@ inline PetscErrorCode solve(Environment&, EPS& solver, PetscInt& nconv) {
   return rc;
 }
 // Solver::solution (src/solver.cpp:58-68): eigenvalue, relative error, and
-// the eigenvector copied into the device vector x.
+// the eigenvector copied into the device vector x (from MatCreateVecs).
 inline PetscErrorCode solution(EPS& solver, PetscInt index, PetscScalar& value, Vec& x, PetscReal& error) {
   double ev = 0.0, err = 0.0;
-  int rc = ed_eps_get_eigenpair(solver.e, (int)index, &ev, &err, x.d);
+  int rc = ed_eps_get_eigenpair(solver.e, (int)index, &ev, &err, x ? x->d : nullptr);
   value = PetscScalar(ev, 0.0);
   error = err;
+  return rc;
+}
+// The same with the eigenvalue in a double (drivers written for a real PETSc
+// build, e.g. examples/ex1.cpp).
+inline PetscErrorCode solution(EPS& solver, PetscInt index, double& value, Vec& x, double& error) {
+  PetscScalar v;
+  int rc = solution(solver, index, v, x, error);
+  value = v.re;
   return rc;
 }
 inline PetscErrorCode SolverClean(EPS& solver) {
@@ -260,13 +382,15 @@ class Correlation {
   PetscScalar ExpectVal(Environment&, PetscInt spin_i, PetscInt spin_j, Vec& state) {
     int32_t pr[2] = {(int32_t)spin_i, (int32_t)spin_j};
     ed_cplx out;
-    throw_on(ed_expect_pairs(basis.h, op, state.d, pr, 1, &out));
+    throw_on(ed_expect_pairs(basis.h, op, state->d, pr, 1, &out));
     return PetscScalar(out.re, out.im);
   }
   // All N*N values in one fused pass (row-major [i][j]).
   std::vector<PetscScalar> AllPairs(Vec& state) {
     std::vector<PetscScalar> out((size_t)(basis.nspins * basis.nspins));
-    throw_on(ed_expect_all_pairs(basis.h, op, state.d, reinterpret_cast<ed_cplx*>(out.data())));
+    std::vector<ed_cplx> tmp(out.size());
+    throw_on(ed_expect_all_pairs(basis.h, op, state->d, tmp.data()));
+    for (size_t k = 0; k < tmp.size(); ++k) out[k] = PetscScalar(tmp[k].re, tmp[k].im);
     return out;
   }
 };
@@ -330,7 +454,7 @@ inline PetscScalar sublattice_sum(Basis& b, const std::vector<const std::vector<
     for (PetscInt i : *sl)
       for (PetscInt j : *sl) { pairs.push_back((int32_t)i); pairs.push_back((int32_t)j); }
   std::vector<ed_cplx> out(pairs.size() / 2);
-  throw_on(ed_expect_pairs(b.h, ED_OP_SISJ, state.d, pairs.data(), (int64_t)out.size(), out.data()));
+  throw_on(ed_expect_pairs(b.h, ED_OP_SISJ, state->d, pairs.data(), (int64_t)out.size(), out.data()));
   PetscScalar e = 0.0;
   for (auto& v : out) e += PetscScalar(v.re, v.im);
   return e;
@@ -377,21 +501,27 @@ template <typename L, typename SQ>
 inline PetscErrorCode DynStructFactor(Environment& env, DSF_data<L>& data, PetscScalar gs, Vec& state,
                                       PetscInt dis_iter = 0) {
   EPS solver;
-  PetscErrorCode rc = Solver::SolverInit(solver, *data.h1, data.nev, data.ncv, data.mpd);
+  PetscErrorCode rc = Solver::SolverInit(solver, data.h1->hamilt, data.nev, data.ncv, data.mpd);
   if (rc != ED_OK) return rc;
   PetscInt nconv = 0;
   const int nev = (int)data.nev;
   const size_t dim1 = (size_t)data.b1->size;
-  Vec vecs(env, (PetscInt)(dim1 * (size_t)nev));
+  Vec vecs = nullptr;
+  rc = VecCreateOnDevice(env.ctx, (PetscInt)(dim1 * (size_t)nev), &vecs);
+  if (rc != ED_OK) {
+    Solver::SolverClean(solver);
+    return rc;
+  }
   std::vector<double> ev((size_t)nev);
   rc = Solver::solve(env, solver, nconv);
   for (int n = 0; n < nev && rc == ED_OK; ++n) {
     double er = 0.0;
-    rc = ed_eps_get_eigenpair(solver.e, n, &ev[(size_t)n], &er, vecs.d + (size_t)n * dim1);
+    rc = ed_eps_get_eigenpair(solver.e, n, &ev[(size_t)n], &er, vecs->d + (size_t)n * dim1);
   }
   std::vector<ed_cplx> c((size_t)env.nspins * (size_t)nev);
-  if (rc == ED_OK) rc = ed_dsf_coefficients(data.b0->h, data.b1->h, SQ::op, state.d, vecs.d, nev, c.data());
+  if (rc == ED_OK) rc = ed_dsf_coefficients(data.b0->h, data.b1->h, SQ::op, state->d, vecs->d, nev, c.data());
   Solver::SolverClean(solver);
+  VecDestroy(&vecs);
   if (rc != ED_OK) return rc;
   const std::string fn = std::string(data.path) + "/dsf_d" + std::to_string((long)dis_iter) + ".dat";
   FILE* fp = std::fopen(fn.c_str(), "w");
@@ -399,7 +529,7 @@ inline PetscErrorCode DynStructFactor(Environment& env, DSF_data<L>& data, Petsc
   std::fprintf(fp, "#------------------------------- Parameters -------------------------------------\n");
   std::fprintf(fp, "#%7s:   %ld  \n", " nspins", (long)env.nspins);
   std::fprintf(fp, "#%7s:   %ld  \n", " nev", (long)data.nev);
-  std::fprintf(fp, "#%7s:   %.16f  \n", " GS", gs.real());
+  std::fprintf(fp, "#%7s:   %.16f  \n", " GS", gs.re);
   std::fprintf(fp, "#%7s:   %.5f  %4s:   %.5f  %4s:   %.5f  %4s:   %.5f\n", "J1", data.h0->hamilt_J1(), "D1",
                data.h0->hamilt_D1(), "J2", data.h0->hamilt_J2(), "D2", data.h0->hamilt_D2());
   if (data.disorder)
@@ -409,7 +539,7 @@ inline PetscErrorCode DynStructFactor(Environment& env, DSF_data<L>& data, Petsc
   for (PetscInt s = 0; s < env.nspins; ++s) {
     std::fprintf(fp, "# spin: %ld\n", (long)s);
     for (int n = 0; n < nev; ++n)
-      std::fprintf(fp, "%.13e  %.13e\n", ev[(size_t)n] - gs.real(), c[(size_t)s * (size_t)nev + (size_t)n].re);
+      std::fprintf(fp, "%.13e  %.13e\n", ev[(size_t)n] - gs.re, c[(size_t)s * (size_t)nev + (size_t)n].re);
   }
   std::fclose(fp);
   return ED_OK;

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, 'libedgb300.so')
 
 SOURCES = ['ed_capi.cu', 'ed_basis.cu', 'ed_hamiltonian.cu', 'ed_linalg.cu', 'ed_eps.cu', 'ed_measure.cu',
            'ed_batch.cu', 'ed_adjoint.cu', 'ed_hv_lin.cu',
-           'ed_spectrum.cu', 'ed_hv_jit.cu']
+           'ed_spectrum.cu', 'ed_hv_jit.cu', 'ed_peaks.cu', 'ed_tc.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2', '-Xcompiler', '-fopenmp',
          '--expt-relaxed-constexpr', '-I' + os.path.join(ROOT, 'include')]

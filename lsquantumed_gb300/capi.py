@@ -16,7 +16,7 @@ ED_OP_SZSZ, ED_OP_SPSM, ED_OP_SMSP, ED_OP_SISJ = 0, 1, 2, 3
 ED_HAM_MATRIX_FREE, ED_HAM_CSR = 0, 1
 ED_ACC_FP64, ED_ACC_EXACT, ED_ACC_FIXED64 = 0, 1, 2
 ED_TERM_XY, ED_TERM_ZZ, ED_TERM_Z, ED_TERM_SISJ = 0, 1, 2, 3
-ED_RESTART_AUTO, ED_RESTART_FP64, ED_RESTART_PAIR = 0, 1, 2
+ED_RESTART_AUTO, ED_RESTART_FP64, ED_RESTART_PAIR, ED_RESTART_EXACT = 0, 1, 2, 3
 
 _ERRNAMES = {1: 'EINVAL', 2: 'ECUDA', 3: 'ENOMEM', 4: 'ESTATE', 5: 'ENOTCONV', 6: 'ENOTSUP'}
 
@@ -48,6 +48,7 @@ SIGNATURES = {
     'ed_ctx_kernel_count': [vp, P(i64)],
     'ed_ctx_profile': [vp, i32],
     'ed_ctx_profile_read': [vp, P(i64), P(dbl)],
+    'ed_probe_rates': [vp, P(dbl), P(dbl), P(dbl)],
     'ed_vec_create': [vp, i64, P(vp)],
     'ed_vec_destroy': [vp],
     'ed_vec_to_host': [vp, vp, vp, i64],
@@ -84,6 +85,8 @@ SIGNATURES = {
     'ed_eps_set_tolerances': [vp, dbl, i32],
     'ed_eps_set_seed': [vp, u64],
     'ed_eps_set_restart_arithmetic': [vp, i32],
+    'ed_bv_mult_real': [vp, vp, i32, vp, i32, i32, vp, i64, i32],
+    'ed_bv_dot_real': [vp, vp, i32, vp, i64, i32, vp],
     'ed_batch_set_restart_arithmetic': [vp, i32],
     'ed_eps_set_initial_vector': [vp, vp, i32],
     'ed_eps_solve': [vp, P(i32)],

@@ -455,6 +455,43 @@ int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev) {
   return ed_launch_hv_r(h, x_dev, y_dev);
 }
 
+int ed_bv_mult_real(ed_ctx* ctx, const double* const* V_dev, int m, const double* Y_host, int ldY, int l,
+                    double* const* out_dev, int64_t n, int arith) {
+  if (!ctx || !V_dev || !Y_host || !out_dev) return ed_fail(ED_EINVAL, "null argument");
+  if (m < 1 || l < 1 || n < 1 || ldY < l) return ed_fail(ED_EINVAL, "bad dimensions");
+  if (m > 127 || l > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  for (int i = 0; i < m; ++i)
+    for (int c = 0; c < l; ++c)
+      if (V_dev[i] == out_dev[c]) return ed_fail(ED_EINVAL, "out must not alias V");
+  if (arith == ED_RESTART_AUTO) arith = ED_RESTART_FP64;
+  if (arith != ED_RESTART_FP64 && arith != ED_RESTART_PAIR && arith != ED_RESTART_EXACT)
+    return ed_fail(ED_EINVAL, "unknown restart arithmetic");
+  if (arith == ED_RESTART_EXACT && m > 32) return ed_fail(ED_ENOTSUP, "the exact restart takes at most 32 vectors");
+  ED_CUDA(cudaSetDevice(ctx->device));
+  return ed_restart_combine_r(ctx, V_dev, m, Y_host, ldY, l, out_dev, n, arith);
+}
+
+int ed_bv_dot_real(ed_ctx* ctx, const double* const* V_dev, int m, const double* w_dev, int64_t n, int arith,
+                   double* h_host) {
+  if (!ctx || !V_dev || !w_dev || !h_host) return ed_fail(ED_EINVAL, "null argument");
+  if (m < 1 || n < 1) return ed_fail(ED_EINVAL, "bad dimensions");
+  if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  if (arith == ED_RESTART_AUTO) arith = ED_RESTART_FP64;
+  if (arith != ED_RESTART_FP64 && arith != ED_RESTART_EXACT) return ed_fail(ED_EINVAL, "unknown dot arithmetic");
+  ED_CUDA(cudaSetDevice(ctx->device));
+  double* w = const_cast<double*>(w_dev);  // read only: no local step
+  if (arith == ED_RESTART_EXACT) {
+    double w2 = 0.0;
+    ED_TRY(ed_multidot_r(ctx, nullptr, 0, w, n, nullptr, 0.0, nullptr, 0.0, nullptr, &w2));
+    const double bound = std::sqrt(w2) * (1.0 + 0x1p-40);
+    if (bound > 0.0) {
+      const int rc = ed_multidot_tc(ctx, V_dev, m, w, n, nullptr, 0.0, nullptr, 0.0, bound, h_host);
+      if (rc != ED_ENOTSUP) return rc;
+    }
+  }
+  return ed_multidot_r(ctx, V_dev, m, w, n, nullptr, 0.0, nullptr, 0.0, h_host, nullptr);
+}
+
 int ed_ham_apply_real_dot(ed_ham* h, const double* x_dev, double* y_dev, double* xy_host, double* yy_host) {
   if (!h || !x_dev || !y_dev) return ed_fail(ED_EINVAL, "null argument");
   if (x_dev == y_dev) return ed_fail(ED_EINVAL, "x and y must not alias");

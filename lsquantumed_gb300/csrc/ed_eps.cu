@@ -42,7 +42,7 @@ struct ed_eps {
   double* w_r = nullptr;
   std::vector<double*> col_r;
   int restart_arith = ED_RESTART_AUTO;  // ed_eps_set_restart_arithmetic
-  bool restart_pair = false;            // float-pair restart products in this real-storage solve
+  int restart_mode = ED_RESTART_FP64;   // the form this real-storage solve uses
 };
 
 void ed_jacobi_eig(int m, std::vector<double>& A, std::vector<double>& theta, std::vector<double>& Y) {
@@ -216,14 +216,34 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
   // no norm in the projection pass (one FP64 FMA per row less on the FP64
   // bound kernel): the norm before the update is sqrt(||w_after||^2 + sum c_i^2)
   // (Pythagoras against the orthonormal basis), formed after the update
-  ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
-                       beta_prev, c.data(), nullptr));
+  const bool exact = e->restart_mode == ED_RESTART_EXACT;
+  const double margin = 1.0 + 0x1p-40;  // rounding of the bounds themselves
+  int rc = ED_ENOTSUP;
+  if (exact) {
+    // max |w - a v_j - b v_j-1| <= ||w|| + |a| + |b| (unit columns)
+    const double bound = (std::sqrt(y2) + std::fabs(a) + (three_term ? std::fabs(beta_prev) : 0.0)) * margin;
+    rc = ed_multidot_tc(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
+                        beta_prev, bound, c.data());
+    if (rc == ED_ENOTSUP)  // the local step is done; the dots again in FP64
+      rc = ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr);
+  } else {
+    rc = ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, e->col_r[j], a, three_term ? e->col_r[j - 1] : nullptr,
+                       beta_prev, c.data(), nullptr);
+  }
+  ED_TRY(rc);
   double n0 = -1.0;
   h[j] += a;
   if (three_term) h[j - 1] += beta_prev;
   for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 1)
-      ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
+    if (pass == 1) {
+      int r2 = ED_ENOTSUP;
+      if (exact)
+        r2 = ed_multidot_tc(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, std::sqrt(n2) * margin,
+                            c.data());
+      if (r2 == ED_ENOTSUP)
+        r2 = ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr);
+      ED_TRY(r2);
+    }
     ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, wmax));
     for (int i = 0; i <= j; ++i) h[i] += c[i];
     *nw = std::sqrt(n2);
@@ -262,6 +282,11 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
   ed_ham* H = e->h;
   ed_ctx* ctx = H->ctx;
   const int64_t n = H->basis->dim;
+  // float pairs and exact slices only on request; the default keeps every
+  // product at FP64 or better (FP64 FMA beside exact integers)
+  e->restart_mode = e->restart_arith == ED_RESTART_AUTO ? ED_RESTART_FP64 : e->restart_arith;
+  if (e->restart_mode == ED_RESTART_EXACT && m > 32)
+    return ed_fail(ED_ENOTSUP, "the exact tensor-core restart takes at most 32 basis vectors (ncv <= 32)");
   e->pool_cols = 2 * m + 1;
   if (cudaMalloc(&e->pool_r, sizeof(double) * (size_t)n * e->pool_cols) != cudaSuccess ||
       cudaMalloc(&e->w_r, sizeof(double) * (size_t)n) != cudaSuccess) {
@@ -271,8 +296,6 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
   }
   e->real_storage = true;
   e->real_coeffs = true;
-  // float pairs only on request: the default keeps every product at FP64 or better
-  e->restart_pair = e->restart_arith == ED_RESTART_PAIR;
   std::vector<double*> freelist;
   e->col_r.assign(m + 1, nullptr);
   for (int i = 0; i < e->pool_cols; ++i) {
@@ -349,7 +372,7 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
     }
     std::vector<double*> outc(freelist.begin(), freelist.begin() + l);
     std::vector<const double*> inc(e->col_r.begin(), e->col_r.begin() + m);
-    ED_TRY(ed_restart_combine_r(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n, e->restart_pair));
+    ED_TRY(ed_restart_combine_r(ctx, inc.data(), m, Y.data(), m, l, outc.data(), n, e->restart_mode));
     std::vector<double*> newcol(m + 1, nullptr);
     for (int c = 0; c < l; ++c) newcol[c] = outc[c];
     newcol[l] = e->col_r[m];
@@ -567,7 +590,7 @@ int ed_eps_set_seed(ed_eps* e, uint64_t seed) {
 
 int ed_eps_set_restart_arithmetic(ed_eps* e, int mode) {
   if (!e) return ed_fail(ED_EINVAL, "null solver");
-  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR)
+  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR && mode != ED_RESTART_EXACT)
     return ed_fail(ED_EINVAL, "unknown restart arithmetic");
   e->restart_arith = mode;
   return ED_OK;

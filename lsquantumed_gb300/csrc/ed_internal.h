@@ -237,10 +237,21 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
                 double* wnorm2_host, double* wmax_host = nullptr);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);
-// pair: the products in float-pair arithmetic on the FP32 units (see
-// ed_linalg.cu) instead of FP64 FMA beside exact integer products.
+// arith: ED_RESTART_FP64 (FP64 FMA beside exact integer products),
+// ED_RESTART_PAIR (float-pair products on the FP32 units, ed_linalg.cu) or
+// ED_RESTART_EXACT (exact slices on the tensor cores, ed_tc.cu; m <= 32).
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
-                         double* const* out, int64_t n, bool pair = false);
+                         double* const* out, int64_t n, int arith = ED_RESTART_FP64);
+// h_host[i] = V_i^T w (i < nv) on the tensor cores in exact slices
+// (ed_tc.cu); with vj the local step w <- w - a vj - b vjm1 first (written
+// back).  wbound: an upper bound on max |w| after the local step; ED_ENOTSUP
+// when it did not hold (the local step is then done, the dots are not).
+int ed_multidot_tc(ed_ctx* ctx, const double* const* cols, int nv, double* w, int64_t n, const double* vj, double a,
+                   const double* vjm1, double b, double wbound, double* h_host);
+// out_c = sum_i V_i Y[i][c], c < l, on the tensor cores in exact slices
+// (ed_tc.cu).  ED_ENOTSUP (nothing launched) for m outside 1..32.
+int ed_restart_combine_tc(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
+                          double* const* out, int64_t n);
 int ed_residual_norm2_r(ed_ctx* ctx, const double* hx, const double* x, double theta, int64_t n, double* r2_host,
                         double* x2_host);
 int ed_start_vector_r(ed_ctx* ctx, uint64_t seed, int64_t n, double* v);

@@ -719,8 +719,10 @@ __global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, c
 }
 
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
-                         double* const* out, int64_t n, bool pair) {
+                         double* const* out, int64_t n, int arith) {
   if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
+  if (arith == ED_RESTART_EXACT) return ed_restart_combine_tc(ctx, cols, m, Y, ldY, l, out, n);
+  const bool pair = arith == ED_RESTART_PAIR;
   ColPtrsR cp = make_cols_r(cols, m);
   ColPtrs op;
   for (int i = 0; i < 128; ++i) op.p[i] = nullptr;

@@ -88,7 +88,8 @@ static int run(Environment& env, L& lat, const Args& a) {
   std::vector<int64_t> seeds((size_t)a.rep);
   throw_on(ed_random_seeds(a.reprod ? 1 : 0, a.rep, seeds.data()));
   std::vector<double> hi((size_t)a.n, 0.0);
-  Vec state(env, b.size);
+  Vec state = nullptr;
+  throw_on(MatCreateVecs(h.hamilt, &state, nullptr));
   double magAF = 0.0, magSTR = 0.0;
   std::printf(" iter          k          ||Ax-kx||/||kx||\n ----    -------------   ------------------\n");
   for (PetscInt repet = 0; repet < a.rep; ++repet) {
@@ -97,7 +98,7 @@ static int run(Environment& env, L& lat, const Args& a) {
       throw_on(h.build_disorder(env, hi.data()));
     }
     EPS solver;
-    throw_on(Solver::SolverInit(solver, h, a.nev, a.ncv));
+    throw_on(Solver::SolverInit(solver, h.hamilt, a.nev, a.ncv));
     throw_on(Solver::EPSSetTolerances(solver, a.tol, a.max_it));
     PetscInt nconv = 0;
     throw_on(Solver::solve(env, solver, nconv));
@@ -105,7 +106,7 @@ static int run(Environment& env, L& lat, const Args& a) {
     PetscReal err;
     if (nconv > 0) {
       throw_on(Solver::solution(solver, 0, eig, state, err));
-      std::printf("  %ld     %12f       %12g\n\n", (long)repet, eig.real(), err);
+      std::printf("  %ld     %12f       %12g\n\n", (long)repet, PetscRealPart(eig), err);
     }
     Solver::SolverClean(solver);
     AF<L> af{lat, 2};
@@ -133,6 +134,7 @@ static int run(Environment& env, L& lat, const Args& a) {
       throw_on(Phys::DynStructFactor<L, Sqz>(env, dsf_data, eig, state, repet));
     }
   }
+  VecDestroy(&state);
   return 0;
 }
 

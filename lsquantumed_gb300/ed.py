@@ -44,6 +44,53 @@ def as_device_vector(x, n=None):
     return t
 
 
+def restart_code(mode):
+    m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR,
+         'exact': capi.ED_RESTART_EXACT}.get(mode)
+    if m is None:
+        raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
+    return m
+
+
+def bv_mult_real(env, V, Y, out=None, arith='auto'):
+    """out[:, c] = sum_i V[:, i] Y[i, c] for real device vectors: the
+    Krylov-Schur restart combination on its own (ed_bv_mult_real).  V is a
+    list of m float64 CUDA tensors of n entries, Y an (m, l) array; returns
+    the l output tensors."""
+    torch = _torch()
+    m = len(V)
+    Yh = np.ascontiguousarray(Y, dtype=np.float64)
+    if Yh.ndim != 2 or Yh.shape[0] != m:
+        raise InvalidArgument(capi.ED_EINVAL, 'Y must be (m, l)')
+    n = V[0].numel()
+    l = Yh.shape[1]
+    for v in V:
+        if v.dtype != torch.float64 or v.numel() != n or not v.is_cuda or not v.is_contiguous():
+            raise InvalidArgument(capi.ED_EINVAL, 'V must hold contiguous float64 CUDA vectors of one length')
+    if out is None:
+        out = [torch.empty(n, dtype=torch.float64, device=V[0].device) for _ in range(l)]
+    vp = (ctypes.c_void_p * m)(*[v.data_ptr() for v in V])
+    op = (ctypes.c_void_p * l)(*[o.data_ptr() for o in out])
+    call('ed_bv_mult_real', env.handle, vp, m, _p(Yh), l, l, op, n, restart_code(arith))
+    return out
+
+
+def bv_dot_real(env, V, w, arith='auto'):
+    """h[i] = V[i]^T w for real device vectors (ed_bv_dot_real): the
+    Gram-Schmidt projection on its own.  V: list of float64 CUDA tensors with
+    entries of magnitude <= 1, w: float64 CUDA tensor; returns numpy h."""
+    torch = _torch()
+    m = len(V)
+    n = w.numel()
+    for v in list(V) + [w]:
+        if v.dtype != torch.float64 or v.numel() != n or not v.is_cuda or not v.is_contiguous():
+            raise InvalidArgument(capi.ED_EINVAL, 'V and w must be contiguous float64 CUDA vectors of one length')
+    h = np.zeros(m)
+    vp = (ctypes.c_void_p * m)(*[v.data_ptr() for v in V])
+    call('ed_bv_dot_real', env.handle, vp, m, _p(w), n, restart_code(arith), _p(h))
+    return h
+
+
 # ---------------------------------------------------------------------------
 # Environment (src/environment.cpp:8-49)
 # ---------------------------------------------------------------------------
@@ -89,6 +136,13 @@ class Environment:
     def profile(self, enable=True):
         """Start (clearing) or stop CUDA-event timing of the H.v launches."""
         call('ed_ctx_profile', self._h, 1 if enable else 0)
+
+    def probe_rates(self):
+        """Measured TFLOP/s of FP64 FMA, FP64 tensor mma and FP16/FP32 tensor mma
+        on this device (ed_probe_rates)."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        call('ed_probe_rates', self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {'dfma_tflops': a.value, 'dmma_f64_tflops': b.value, 'hmma_f16_f32_tflops': c.value}
 
     def profile_read(self):
         """(H.v launches, summed device milliseconds) since profile(True)."""
@@ -424,12 +478,11 @@ class EPS:
 
     def set_restart_arithmetic(self, mode):
         """Products of the restart combination V Y in a real-storage solve:
-        'fp64', 'pair' (float pairs on the FP32 units, storage and sums FP64)
-        or 'auto' (pairs from 2^22 basis states up)."""
-        m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR}.get(mode)
-        if m is None:
-            raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
-        call('ed_eps_set_restart_arithmetic', self._h, m)
+        'fp64', 'pair' (float pairs on the FP32 units, storage and sums FP64;
+        below FP64 accuracy), 'exact' (exact slices on the tensor cores for
+        the restart and the Gram-Schmidt projections, ncv <= 32) or 'auto'
+        (fp64)."""
+        call('ed_eps_set_restart_arithmetic', self._h, restart_code(mode))
 
     def set_initial_vector(self, v):
         """EPSSetInitialSpace with one vector: numpy (host) or CUDA tensor."""
@@ -552,12 +605,11 @@ class DisorderBatch:
         return out
 
     def set_restart_arithmetic(self, mode):
-        """Products of the restart combination: 'fp64', 'pair' or 'auto' (as
-        EPS.set_restart_arithmetic; pairs from 2^22 entries of the block up)."""
-        m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR}.get(mode)
-        if m is None:
-            raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
-        call('ed_batch_set_restart_arithmetic', self._h, m)
+        """Products of the restart combination: 'fp64', 'pair' or 'auto'
+        (FP64; pairs only on request)."""
+        if mode == 'exact':
+            raise InvalidArgument(capi.ED_EINVAL, "the batched sweep has no 'exact' restart")
+        call('ed_batch_set_restart_arithmetic', self._h, restart_code(mode))
 
     def solve(self, nev=1, ncv=0, tol=1e-8, max_it=0, seed=0):
         ev = np.zeros((self.B, nev))

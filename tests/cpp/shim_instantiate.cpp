@@ -10,9 +10,10 @@ void use_all(Environment& env, L& lat) {
   Hamiltonian<L> h0{env, b0, lat, 1.0, 1.0, 0.5, 0.5}, h1{env, b1, lat, 1.0, 1.0, 0.5, 0.5};
   h0.build_diag(env);
   h0.build_off_diag(env);
-  Vec state(env, b0.size);
+  Vec state = nullptr;
+  MatCreateVecs(h0.hamilt, &state, nullptr);
   EPS eps;
-  Solver::SolverInit(eps, h0, 2);
+  Solver::SolverInit(eps, h0.hamilt, 2);
   Solver::EPSSetTolerances(eps, 1e-9, 0);
   PetscInt nconv = 0;
   Solver::solve(env, eps, nconv);
@@ -40,6 +41,11 @@ void use_all(Environment& env, L& lat) {
   d.b1 = &b0;
   d.h1 = &h0;
   Phys::DynStructFactor<L, Sqz>(env, d, e0, state);
+  double e1 = 0.0, err1 = 0.0;
+  Solver::solution(eps, 0, e1, state, err1);
+  double m2 = Phys::SquaredSubLattMagAF(env, b0, af, state);
+  (void)m2;
+  VecDestroy(&state);
 }
 
 int main(int argc, char** argv) {
@@ -51,8 +57,10 @@ int main(int argc, char** argv) {
   use_all(env, square);
   use_all(env, honey);
   Striped<square2D> st{square, 4};
-  Vec v(env, 1);
   Basis b{env, 0};
+  Vec v = nullptr;
+  VecCreateOnDevice(env.ctx, b.size, &v);
   Phys::SquaredSubLattMagSTR(env, b, st, v);
+  VecDestroy(&v);
   return 0;
 }
