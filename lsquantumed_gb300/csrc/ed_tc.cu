@@ -379,7 +379,7 @@ template <bool LOCAL>
 __global__ void __launch_bounds__(DT_THREADS) k_dots_tc(const __grid_constant__ DotCols cols, int ng, double* __restrict__ w,
                                                         const double* __restrict__ vj, double a,
                                                         const double* __restrict__ vjm1, double b, int qref,
-                                                        int64_t n, double* __restrict__ partial, int item0, int nblk,
+                                                        int64_t n, unsigned long long* __restrict__ part,
                                                         int* __restrict__ err) {
   __shared__ __align__(1024) unsigned char sA[16 * 16 * 128];  // [rg][i][s][row] halves
   __shared__ __align__(1024) unsigned char sB[16 * 2 * 128];   // [rg][t-group][t][row] halves
@@ -537,14 +537,12 @@ __global__ void __launch_bounds__(DT_THREADS) k_dots_tc(const __grid_constant__ 
     }
     __syncthreads();
   }
-  // lane (i, s): acc 2^(8(7-s)) 2^(Pref + Qref - 126) with Pref = 1; sum the
-  // slices of a column (lanes 8i .. 8i+7 of one warp) in a fixed order
+  // lane (i, s): acc at the unit 2^(8(7-s)) 2^(Pref + Qref - 126), Pref = 1;
+  // the exact sum over the CTAs is k_dots_finish's
   if (warp < 4) {
-    double v = 0.0;
-    if (di < ng) v = fx128_to_double(acc_hi, acc_lo, 8 * (7 - ds) + 1 + (qref - 1022) - 126);
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o, 8);
-    if (ds == 0 && di < ng) partial[(size_t)(item0 + di) * nblk + blockIdx.x] = v;
+    unsigned long long* dst = part + ((size_t)blockIdx.x * 128 + tid) * 2;
+    dst[0] = acc_lo;
+    dst[1] = (unsigned long long)acc_hi;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -552,7 +550,131 @@ __global__ void __launch_bounds__(DT_THREADS) k_dots_tc(const __grid_constant__ 
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DT_TMEM_COLS));
 }
 
+// Magnitude of a 4-word (256-bit) unsigned integer times 2^X, rounded to
+// nearest even, as FP64 with the given sign; integer operations only.
+__device__ __forceinline__ double u256_to_double(const unsigned long long (&w)[4], int X, bool neg) {
+  int k = 3;
+  while (k > 0 && w[k] == 0ull) --k;
+  if (w[k] == 0ull) return 0.0;
+  const int L = 64 * k + 64 - __clzll((long long)w[k]);  // bit length
+  // the top 64 bits (leading bit at 63) and a sticky bit for the rest
+  unsigned long long top, rest;
+  const int sh = L - 64;  // bits below the top word
+  if (sh <= 0) {
+    top = w[0] << (-sh);
+    rest = 0ull;
+  } else {
+    const int q = sh >> 6, r = sh & 63;
+    top = r ? ((w[q] >> r) | (q + 1 < 4 ? (w[q + 1] << (64 - r)) : 0ull)) : w[q];
+    rest = r ? (w[q] & ((1ull << r) - 1ull)) : 0ull;
+    for (int j = 0; j < q; ++j) rest |= w[j];
+  }
+  unsigned long long m = top >> 11;  // 53 bits
+  const unsigned long long low = top & 0x7FFull;
+  const bool up = low > 0x400ull || (low == 0x400ull && (rest != 0ull || (m & 1ull)));
+  m += up ? 1ull : 0ull;
+  int bexp = X + L + 1022;
+  if (m >> 53) {
+    m >>= 1;
+    ++bexp;
+  }
+  if (bexp <= 0) return 0.0;
+  const unsigned long long bits =
+      ((unsigned long long)neg << 63) | ((unsigned long long)bexp << 52) | (m & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+// Exact sum of the CTAs' lane accumulators of k_dots_tc (thread = lane
+// (i, s)), the slices of each column combined with their weights 2^(8(7-s))
+// in 256-bit integers, and one rounding per column:
+// h[item0 + i] = total_i 2^(Pref + Qref - 126).
+__global__ void __launch_bounds__(128) k_dots_finish(const unsigned long long* __restrict__ part, int nblk, int ng,
+                                                     int qref, double* __restrict__ h, int item0) {
+  __shared__ unsigned long long sh[128][4];
+  const int t = threadIdx.x, i = t >> 3, sl = t & 7;
+  // 192-bit signed sum of nblk 128-bit values
+  unsigned long long a0 = 0ull, a1 = 0ull, a2 = 0ull;
+  for (int b = 0; b < nblk; ++b) {
+    const unsigned long long lo = part[((size_t)b * 128 + t) * 2];
+    const unsigned long long hi = part[((size_t)b * 128 + t) * 2 + 1];
+    const unsigned long long ext = (long long)hi < 0 ? ~0ull : 0ull;
+    const unsigned long long s0 = a0 + lo;
+    const unsigned long long c0 = s0 < a0 ? 1ull : 0ull;
+    const unsigned long long s1 = a1 + hi;
+    const unsigned long long c1 = s1 < a1 ? 1ull : 0ull;
+    const unsigned long long s1b = s1 + c0;
+    const unsigned long long c1b = s1b < s1 ? 1ull : 0ull;
+    a2 += ext + c1 + c1b;
+    a1 = s1b;
+    a0 = s0;
+  }
+  // times 2^(8(7-s)) into 256 bits (sign-extended)
+  const int sh8 = 8 * (7 - sl);
+  unsigned long long v[4];
+  const unsigned long long a3 = (long long)a2 < 0 ? ~0ull : 0ull;
+  if (sh8 == 0) {
+    v[0] = a0; v[1] = a1; v[2] = a2; v[3] = a3;
+  } else {
+    v[0] = a0 << sh8;
+    v[1] = (a1 << sh8) | (a0 >> (64 - sh8));
+    v[2] = (a2 << sh8) | (a1 >> (64 - sh8));
+    v[3] = (a3 << sh8) | (a2 >> (64 - sh8));
+  }
+  for (int k = 0; k < 4; ++k) sh[t][k] = v[k];
+  __syncthreads();
+  if (sl == 0 && i < ng) {
+    unsigned long long w[4] = {0ull, 0ull, 0ull, 0ull};
+    for (int q = 0; q < 8; ++q) {
+      unsigned long long carry = 0ull;
+      for (int k = 0; k < 4; ++k) {
+        const unsigned long long x = sh[t + q][k];
+        const unsigned long long s1 = w[k] + x;
+        const unsigned long long c1 = s1 < w[k] ? 1ull : 0ull;
+        const unsigned long long s2 = s1 + carry;
+        const unsigned long long c2 = s2 < s1 ? 1ull : 0ull;
+        w[k] = s2;
+        carry = c1 + c2;
+      }
+    }
+    const bool neg = (long long)w[3] < 0;
+    if (neg) {  // two's complement negation
+      unsigned long long carry = 1ull;
+      for (int k = 0; k < 4; ++k) {
+        const unsigned long long x = ~w[k] + carry;
+        carry = (carry && x == 0ull) ? 1ull : 0ull;
+        w[k] = x;
+      }
+    }
+    h[item0 + i] = u256_to_double(w, 1 + (qref - 1022) - 126, neg);
+  }
+}
+
 }  // namespace
+
+// CTAs of a tensor-core kernel that fit one SM at once, from its registers,
+// shared memory, threads and TMEM columns.  (The occupancy query reports one
+// CTA per SM for kernels that allocate tensor memory, which would leave the
+// per-tile latency of these kernels exposed.)
+template <typename K>
+static int tc_ctas_per_sm(K kern, int threads, size_t dyn_smem, int tmem_cols) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  int dev = 0, smem_sm = 0, regs_sm = 0, thr_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  const size_t per_cta_smem = dyn_smem + fa.sharedSizeBytes + 1024;  // + the per-CTA reserve
+  int n = 512 / tmem_cols;
+  n = std::min(n, (int)((size_t)smem_sm / std::max<size_t>(per_cta_smem, 1)));
+  n = std::min(n, thr_sm / threads);
+  const int regs = std::max(fa.numRegs, 1) * threads;
+  n = std::min(n, regs_sm / regs);
+  return std::max(n, 1);
+}
 
 // Host: B operand for one group of up to 8 outputs (columns c0..c0+nc-1 of
 // Y, row-major ldY), in the shared-memory layout of the kernel, and the
@@ -611,9 +733,7 @@ int ed_restart_combine_tc(ed_ctx* ctx, const double* const* cols, int m, const d
   ED_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   auto kern = m <= 16 ? k_restart_tc<16> : k_restart_tc<32>;
   ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TC_THREADS, smem));
-  per_sm = std::max(1, std::min(per_sm, 512 / TC_TMEM_COLS));
+  const int per_sm = tc_ctas_per_sm(kern, TC_THREADS, smem, TC_TMEM_COLS);
   const int64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->num_sms * per_sm));
   TcCols cp;
@@ -641,31 +761,34 @@ int ed_multidot_tc(ed_ctx* ctx, const double* const* cols, int nv, double* w, in
   int qe = 0;
   std::frexp(wbound, &qe);  // wbound < 2^qe
   const int qref = qe + 1022;  // biased exponent E with max |w| < 2^(E - 1022)
-  int per_sm = 0;
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dots_tc<false>, DT_THREADS, 0));
-  per_sm = std::max(1, std::min(per_sm, 512 / DT_TMEM_COLS));
+  const int per_sm = tc_ctas_per_sm(k_dots_tc<false>, DT_THREADS, 0, DT_TMEM_COLS);
   const int64_t ntiles = (n + 127) / 128;
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->num_sms * per_sm));
-  ED_TRY(ed_ensure_reduce(ctx, (size_t)nv * nblk + nv + 8));
-  int* d_err = (int*)(ctx->d_red + (size_t)nv * nblk + nv + 4);
-  ED_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   const int ngroups = (nv + DT_COLS - 1) / DT_COLS;
+  const size_t part_words = (size_t)nblk * 128 * 2;  // per group
+  ED_TRY(ed_ensure_reduce(ctx, (size_t)ngroups * part_words + nv + 8));
+  unsigned long long* part = (unsigned long long*)ctx->d_red;
+  double* h_dev = ctx->d_red + (size_t)ngroups * part_words;
+  int* d_err = (int*)(h_dev + nv + 4);
+  ED_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   for (int g = 0; g < ngroups; ++g) {
     const int v0 = g * DT_COLS, ng = std::min(DT_COLS, nv - v0);
     DotCols cp;
     for (int i = 0; i < DT_COLS; ++i) cp.p[i] = i < ng ? cols[v0 + i] : nullptr;
+    unsigned long long* pg = part + (size_t)g * part_words;
     if (g == 0 && vj)
-      k_dots_tc<true><<<nblk, DT_THREADS, 0, ctx->stream>>>(cp, ng, w, vj, a, vjm1, b, qref, n, ctx->d_red, v0, nblk,
-                                                           d_err);
+      k_dots_tc<true><<<nblk, DT_THREADS, 0, ctx->stream>>>(cp, ng, w, vj, a, vjm1, b, qref, n, pg, d_err);
     else
-      k_dots_tc<false><<<nblk, DT_THREADS, 0, ctx->stream>>>(cp, ng, w, nullptr, 0.0, nullptr, 0.0, qref, n, ctx->d_red,
-                                                            v0, nblk, d_err);
+      k_dots_tc<false><<<nblk, DT_THREADS, 0, ctx->stream>>>(cp, ng, w, nullptr, 0.0, nullptr, 0.0, qref, n, pg, d_err);
+    ED_CHECK_LAUNCH(ctx);
+    k_dots_finish<<<1, 128, 0, ctx->stream>>>(pg, nblk, ng, qref, h_dev, v0);
     ED_CHECK_LAUNCH(ctx);
   }
-  std::vector<double> out(nv);
-  ED_TRY(ed_finish_reduce(ctx, nv, nblk, out.data()));
-  int h_err = 0;
-  ED_CUDA(cudaMemcpy(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  // the sums and the error flag in one copy
+  ED_CUDA(cudaMemcpyAsync(ctx->h_red, h_dev, sizeof(double) * (nv + 5), cudaMemcpyDeviceToHost, ctx->stream));
+  ED_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> out(ctx->h_red, ctx->h_red + nv);
+  const int h_err = *(const int*)(ctx->h_red + nv + 4);
   if (h_err == 2) return ED_ENOTSUP;  // the bound on max |w| did not hold: nothing wrong, use FP64
   if (h_err) return ed_fail(ED_ECUDA, "tensor-core dot products: completion wait timed out");
   for (int i = 0; i < nv; ++i) h_host[i] = out[i];
