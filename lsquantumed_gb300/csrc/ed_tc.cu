@@ -30,11 +30,12 @@
 //    the partial sums.  A row holding a non-finite entry gives NaN outputs;
 //    results below 2^-1022 flush to zero.
 //
-// Requirements: m <= 32, nc <= 8, one GPU; the kernel takes one 128-row tile
-// at a time per CTA (persistent grid, up to 4 CTAs per SM, 128 TMEM columns
-// each).  The tensor-core wait is bounded: after 2^26 polls the kernel sets
-// an error flag, waits (again bounded) for its own MMAs, frees its TMEM and
-// returns; the host turns the flag into ED_ECUDA.
+// Requirements: m <= 32, nc <= 8, one GPU.  Persistent grid; each CTA
+// pipelines its tiles across loader, MMA and epilogue warps through two
+// shared-memory stages and two TMEM accumulators (256 columns per CTA).
+// Every wait is bounded: after 2^26 polls the kernel sets an error flag,
+// waits (again bounded) for its own MMAs, frees its TMEM and returns; the
+// host turns the flag into ED_ECUDA.
 #include "ed_internal.h"
 #include <cuda_fp16.h>
 #include <algorithm>
@@ -48,8 +49,6 @@ constexpr int TC_ROWS = 128;        // M: rows per tile = TMEM lanes
 constexpr int TC_N = 80;            // N: 9 levels x 8 outputs, padded to a multiple of 16
 constexpr int TC_LEVELS = 9;
 constexpr int TC_MAX_COLS = 32;     // m <= 32 keeps every level sum below 2^24
-constexpr int TC_TMEM_COLS = 128;   // allocation (power of two >= N)
-constexpr int TC_THREADS = 128;
 constexpr long long TC_WAIT_POLLS = 1ll << 26;
 
 struct TcCols {
@@ -145,171 +144,6 @@ __device__ __forceinline__ double fx128_to_double(long long hi, unsigned long lo
   return __longlong_as_double((long long)bits);
 }
 
-// Dynamic shared memory: A tile [K/8][16][8][8] halves, then B [K/8][10][8][8].
-template <int MAXC>
-__global__ void __launch_bounds__(TC_THREADS) k_restart_tc(const TcCols cols, int m, int kp, const uint4* __restrict__ Bg,
-                                                           TcOut out, int nc, int64_t n, int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ uint64_t s_bar;
-  __shared__ uint32_t s_tmem;
-  __shared__ int s_emax;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int kgroups = kp / 8;
-  unsigned char* sA = tc_smem;
-  unsigned char* sB = tc_smem + (size_t)kgroups * (TC_ROWS / 8) * 128;
-  // B operand (same for every tile), zero the padding column of A
-  {
-    const int nvec = kgroups * (TC_N / 8) * 8;  // 16-byte rows
-    for (int k = tid; k < nvec; k += TC_THREADS) reinterpret_cast<uint4*>(sB)[k] = Bg[k];
-    if (kp > 8 * m)
-      for (int r = tid; r < TC_ROWS; r += TC_THREADS)
-        *reinterpret_cast<uint4*>(sA + (size_t)m * (TC_ROWS / 8) * 128 + (r >> 3) * 128 + (r & 7) * 16) =
-            make_uint4(0, 0, 0, 0);
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
-                 "r"(TC_TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  const uint32_t tmem = s_tmem;
-  const uint32_t bar = smem_u32(&s_bar);
-  const uint32_t idesc = umma_idesc_f16(TC_ROWS, TC_N);
-  const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
-  const uint32_t a_lbo = (TC_ROWS / 8) * 128, b_lbo = (TC_N / 8) * 128;
-  const int64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
-  uint32_t phase = 0;
-  bool failed = false;
-  const __half2 one2 = __floats2half2_rn(1.0f, 1.0f), mone2 = __floats2half2_rn(-1.0f, -1.0f);
-  const __half2 offp = __floats2half2_rn(-1024.0f, -1024.0f), offn = __floats2half2_rn(1024.0f, 1024.0f);
-  for (int64_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
-    const int64_t row = t * TC_ROWS + tid;
-    const bool valid = row < n;
-    // load the row's m entries; largest exponent among the tile's finite entries
-    double v[MAXC];
-    int emax = 0;
-    bool bad = false;
-#pragma unroll
-    for (int i = 0; i < MAXC; ++i) {
-      if (i < m) {
-        v[i] = valid ? __ldg(cols.p[i] + row) : 0.0;
-        const int e = (int)((__double_as_longlong(v[i]) >> 52) & 0x7FF);
-        if (e == 0x7FF) bad = true; else emax = max(emax, e);
-      }
-    }
-    if (tid == 0) s_emax = 0;
-    __syncthreads();
-    atomicMax(&s_emax, emax);
-    __syncthreads();
-    const int E = s_emax;
-    // fixed point against the tile scale, eight signed FP16 slices per entry
-#pragma unroll
-    for (int i = 0; i < MAXC; ++i) {
-      if (i < m) {
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(v[i]);
-        const int e = (int)((bits >> 52) & 0x7FF);
-        unsigned long long q = 0ull;
-        if (e != 0 && e != 0x7FF) {
-          const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-          const int sh = e - E + 10;  // <= 10
-          if (sh >= 0) q = mant << sh;
-          else if (sh > -64) q = (mant + (1ull << (-sh - 1))) >> (-sh);
-        }
-        const bool ng = (bits >> 63) != 0ull;
-        const __half2 sg = ng ? mone2 : one2, of = ng ? offn : offp;
-        const uint32_t qh = (uint32_t)(q >> 32), ql = (uint32_t)q;
-        uint4 w;
-        w.x = slice_pair(qh, 0x4243u, sg, of);  // slices 0, 1 (bytes 7, 6 of q)
-        w.y = slice_pair(qh, 0x4041u, sg, of);  // slices 2, 3
-        w.z = slice_pair(ql, 0x4243u, sg, of);  // slices 4, 5
-        w.w = slice_pair(ql, 0x4041u, sg, of);  // slices 6, 7
-        *reinterpret_cast<uint4*>(sA + (size_t)i * a_lbo + (tid >> 3) * 128 + (tid & 7) * 16) = w;
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      for (int ks = 0; ks < kp / 16; ++ks) {
-        const uint64_t ad = umma_desc(a_base + ks * 2 * a_lbo, a_lbo, 128);
-        const uint64_t bd = umma_desc(b_base + ks * 2 * b_lbo, b_lbo, 128);
-        const uint32_t acc = ks > 0 ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                   : "memory");
-    }
-    const bool done = mbar_wait(bar, phase, TC_WAIT_POLLS);
-    if (!__syncthreads_and(done)) {  // the same decision in every thread
-      failed = true;
-      if (tid == 0) atomicExch(err, 1);
-      mbar_wait(bar, phase, TC_WAIT_POLLS);  // let our own MMAs finish before the TMEM is freed
-      break;
-    }
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    // epilogue: levels 0..3 into A_c, 4..8 into B_c (int64), then T_c = A_c 2^40 + B_c
-    long long Ah[8], Bl[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) Ah[c] = Bl[c] = 0;
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-      uint32_t d[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-          "%14, %15}, [%16];"
-          : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
-            "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
-          : "r"(taddr + (uint32_t)(16 * j)));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int u = 2 * j + h;
-        if (u < TC_LEVELS) {
-#pragma unroll
-          for (int c = 0; c < 8; ++c) {
-            const long long dv = (long long)__float2int_rz(__uint_as_float(d[h * 8 + c]));
-            if (u < 4) Ah[c] = Ah[c] * 256 + dv;
-            else Bl[c] = Bl[c] * 256 + dv;
-          }
-        }
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    if (valid) {
-      const int P = E - 1022;
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        if (c < nc) {
-          long long hi = Ah[c] >> 24;
-          unsigned long long lo = (unsigned long long)Ah[c] << 40;
-          const unsigned long long lo2 = lo + (unsigned long long)Bl[c];
-          hi += (Bl[c] >> 63) + (lo2 < lo ? 1ll : 0ll);
-          double r = fx128_to_double(hi, lo2, P + out.F[c] - 78);
-          if (bad) r = __longlong_as_double(0x7FF8000000000000ll);
-          out.p[c][row] = r;
-        }
-      }
-    }
-    __syncthreads();  // TMEM read and shared A consumed before the next tile's MMA / slices
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
-}
-
-
 // q = round(|v| 2^(63 - P)) for a tile whose largest biased exponent is E
 // (P = E - 1022, so q < 2^63); 0 for zeros, subnormals and non-finite v.
 __device__ __forceinline__ unsigned long long fx63(unsigned long long bits, int E) {
@@ -350,6 +184,242 @@ __device__ __forceinline__ void slices8_store(const unsigned long long (&bits)[8
     asm("prmt.b32 %0, %1, %2, %3;" : "=r"(w3) : "r"(P[6][sl >> 1]), "r"(P[7][sl >> 1]), "r"(sel));
     *reinterpret_cast<uint4*>(dst + sl * 16) = make_uint4(w0, w1, w2, w3);
   }
+}
+
+// Restart combination, pipelined across warp roles (one CTA loops over its
+// tiles t = blockIdx.x + k gridDim.x):
+//  * loader warps 0..3 (thread = row): load the row's m entries, the tile
+//    scale (largest exponent, over the four warps), the eight slices of
+//    each entry into shared stage k % 2, then arrive on full[stage];
+//  * warp 8, one thread: wait full[stage] and tempty[acc], issue the MMA
+//    chain into TMEM accumulator k % 2, commit to empty[stage] (the stage may
+//    be refilled) and tfull[acc];
+//  * epilogue warps 4..7 (thread = row = TMEM lane): wait tfull[acc], read
+//    the 9 levels of the 8 outputs, arrive on tempty[acc] (the accumulator
+//    may be reused), then combine the levels and store.
+// The tile scale and the rows' non-finite flags travel in a ring of 4 slots,
+// each with an mbarrier the epilogue waits on: a loader writing tile k has
+// seen the MMA of tile k - 2 complete, which needed the epilogue of tile
+// k - 4 to release its accumulator after reading slot k % 4, so the slot is
+// free and its barrier at most one phase ahead.
+// Every wait is bounded (TC_WAIT_POLLS polls): on a timeout the role sets
+// the error flag and leaves its loop; the other roles then time out too,
+// the issuing thread waits (bounded) for its own MMAs, and the TMEM is freed.
+constexpr int RS_THREADS = 288;  // loaders 0..3, epilogue 4..7, issuer 8
+constexpr int RS_TMEM_COLS = 256;  // two accumulators of TC_N columns
+
+struct RsShared {
+  uint64_t full[2], empty[2], tfull[2], tempty[2], meta[4], done;
+  uint32_t tmem;
+  int wmax[2][4];
+  uint32_t wbad[2][4];
+  int ok[2];
+  int E[4];
+  uint32_t bad[4][4];
+};
+
+template <int MAXC>
+__global__ void __launch_bounds__(RS_THREADS) k_restart_tc(const TcCols cols, int m, int kp, const uint4* __restrict__ Bg,
+                                                           TcOut out, int nc, int64_t n, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ RsShared S;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int kgroups = kp / 8;
+  const uint32_t a_lbo = (TC_ROWS / 8) * 128, b_lbo = (TC_N / 8) * 128;
+  const size_t a_bytes = (size_t)kgroups * a_lbo;
+  unsigned char* sB = tc_smem;
+  unsigned char* sA0 = tc_smem + (size_t)kgroups * b_lbo;  // stage st at sA0 + st * a_bytes
+  {
+    const int nvec = kgroups * (TC_N / 8) * 8;  // 16-byte rows of B
+    for (int k = tid; k < nvec; k += RS_THREADS) reinterpret_cast<uint4*>(sB)[k] = Bg[k];
+    if (kp > 8 * m)  // the zero padding column of A, in both stages
+      for (int r = tid; r < 2 * TC_ROWS; r += RS_THREADS)
+        *reinterpret_cast<uint4*>(sA0 + (size_t)(r / TC_ROWS) * a_bytes + (size_t)m * a_lbo + ((r % TC_ROWS) >> 3) * 128 +
+                                  (r & 7) * 16) =
+            make_uint4(0, 0, 0, 0);
+  }
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                 "r"(RS_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&S.full[i])), "r"(128));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.empty[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.tfull[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&S.tempty[i])), "r"(128));
+    }
+    for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.meta[i])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.done)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B and the padding, for the tensor core
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = S.tmem;
+  const int64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
+  if (warp < 4) {
+    // ---------------- loaders ----------------
+    const __half2 one2 = __floats2half2_rn(1.0f, 1.0f), mone2 = __floats2half2_rn(-1.0f, -1.0f);
+    const __half2 offp = __floats2half2_rn(-1024.0f, -1024.0f), offn = __floats2half2_rn(1024.0f, 1024.0f);
+    int k = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+      const int st = k & 1, ring = k & 3;
+      const int64_t row = t * TC_ROWS + tid;
+      const bool valid = row < n;
+      double v[MAXC];
+      int emax = 0;
+      bool bad = false;
+#pragma unroll
+      for (int i = 0; i < MAXC; ++i) {
+        if (i < m) {
+          v[i] = valid ? __ldg(cols.p[i] + row) : 0.0;
+          const int e = (int)((__double_as_longlong(v[i]) >> 52) & 0x7FF);
+          if (e == 0x7FF) bad = true; else emax = max(emax, e);
+        }
+      }
+      emax = __reduce_max_sync(0xFFFFFFFFu, (unsigned)emax);
+      const uint32_t badw = __ballot_sync(0xFFFFFFFFu, bad);
+      if (lane == 0) {
+        S.wmax[k & 1][warp] = emax;
+        S.wbad[k & 1][warp] = badw;
+      }
+      // one thread waits for the stage, so every loader takes the same branch
+      if (tid == 0) S.ok[k & 1] = mbar_wait(smem_u32(&S.empty[st]), ((k >> 1) & 1) ^ 1, TC_WAIT_POLLS) ? 1 : 0;
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (!S.ok[k & 1]) {
+        if (tid == 0) atomicExch(err, 1);
+        break;
+      }
+      const int E = max(max(S.wmax[k & 1][0], S.wmax[k & 1][1]), max(S.wmax[k & 1][2], S.wmax[k & 1][3]));
+      if (tid == 0) {  // the tile's scale and non-finite rows for the epilogue
+        S.E[ring] = E;
+        for (int q = 0; q < 4; ++q) S.bad[ring][q] = S.wbad[k & 1][q];
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&S.meta[ring])) : "memory");
+      }
+      unsigned char* a = sA0 + (size_t)st * a_bytes;
+#pragma unroll
+      for (int i = 0; i < MAXC; ++i) {
+        if (i < m) {
+          const unsigned long long bits = (unsigned long long)__double_as_longlong(v[i]);
+          const unsigned long long q = fx63(bits, E);
+          const bool ng = (bits >> 63) != 0ull;
+          const __half2 sg = ng ? mone2 : one2, of = ng ? offn : offp;
+          const uint32_t qh = (uint32_t)(q >> 32), ql = (uint32_t)q;
+          uint4 w;
+          w.x = slice_pair(qh, 0x4243u, sg, of);  // slices 0, 1 (bytes 7, 6 of q)
+          w.y = slice_pair(qh, 0x4041u, sg, of);  // slices 2, 3
+          w.z = slice_pair(ql, 0x4243u, sg, of);  // slices 4, 5
+          w.w = slice_pair(ql, 0x4041u, sg, of);  // slices 6, 7
+          *reinterpret_cast<uint4*>(a + (size_t)i * a_lbo + (tid >> 3) * 128 + (tid & 7) * 16) = w;
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&S.full[st])) : "memory");
+    }
+  } else if (warp < 8) {
+    // ---------------- epilogue ----------------
+    const int r = tid - 128;  // TMEM lane
+    int k = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+      const int ac = k & 1, ring = k & 3;
+      if (!mbar_wait(smem_u32(&S.tfull[ac]), (k >> 1) & 1, TC_WAIT_POLLS) ||
+          !mbar_wait(smem_u32(&S.meta[ring]), (k >> 2) & 1, TC_WAIT_POLLS)) {
+        atomicExch(err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      // read the ring before releasing the accumulator: once it is released,
+      // the loaders may reach tile k + 4 and refill slot k % 4
+      const int P = S.E[ring] - 1022;
+      const bool bad = (S.bad[ring][r >> 5] >> (r & 31)) & 1u;
+      long long Ah[8], Bl[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) Ah[c] = Bl[c] = 0;
+      const uint32_t taddr = tmem + ((uint32_t)((warp - 4) * 32) << 16) + (uint32_t)(ac * 128);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        uint32_t d[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+              "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+            : "r"(taddr + (uint32_t)(16 * j)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int u = 2 * j + h;
+          if (u < TC_LEVELS) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const long long dv = (long long)__float2int_rz(__uint_as_float(d[h * 8 + c]));
+              if (u < 4) Ah[c] = Ah[c] * 256 + dv;
+              else Bl[c] = Bl[c] * 256 + dv;
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&S.tempty[ac])) : "memory");
+      const int64_t row = t * TC_ROWS + r;
+      if (row < n) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          if (c < nc) {
+            long long hi = Ah[c] >> 24;
+            unsigned long long lo = (unsigned long long)Ah[c] << 40;
+            const unsigned long long lo2 = lo + (unsigned long long)Bl[c];
+            hi += (Bl[c] >> 63) + (lo2 < lo ? 1ll : 0ll);
+            double x = fx128_to_double(hi, lo2, P + out.F[c] - 78);
+            if (bad) x = __longlong_as_double(0x7FF8000000000000ll);
+            out.p[c][row] = x;
+          }
+        }
+      }
+    }
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t idesc = umma_idesc_f16(TC_ROWS, TC_N);
+    const uint32_t b_base = smem_u32(sB);
+    int k = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+      const int st = k & 1, ac = k & 1;
+      if (!mbar_wait(smem_u32(&S.full[st]), (k >> 1) & 1, TC_WAIT_POLLS) ||
+          !mbar_wait(smem_u32(&S.tempty[ac]), ((k >> 1) & 1) ^ 1, TC_WAIT_POLLS)) {
+        atomicExch(err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a_base = smem_u32(sA0 + (size_t)st * a_bytes);
+      for (int ks = 0; ks < kp / 16; ++ks) {
+        const uint64_t ad = umma_desc(a_base + ks * 2 * a_lbo, a_lbo, 128);
+        const uint64_t bd = umma_desc(b_base + ks * 2 * b_lbo, b_lbo, 128);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem + (uint32_t)(ac * 128)),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&S.empty[st]))
+                   : "memory");
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&S.tfull[ac]))
+                   : "memory");
+    }
+    // every MMA this thread issued has completed before the TMEM is freed
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(&S.done))
+                 : "memory");
+    if (!mbar_wait(smem_u32(&S.done), 0, TC_WAIT_POLLS)) atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(RS_TMEM_COLS));
 }
 
 // Dot products h_i = V_i^T w for up to 16 columns on the tensor cores, in
@@ -414,7 +484,7 @@ __global__ void __launch_bounds__(DT_THREADS) k_dots_tc(const __grid_constant__ 
   const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
   const int ci = tid >> 4, rg = tid & 15;  // this thread's column and 8-row group
   // drain lanes: warps 0..3, TMEM lane = tid = i * 8 + s
-  const int di = tid >> 3, ds = tid & 7;
+  const int di = tid >> 3;
   long long acc_hi = 0;
   unsigned long long acc_lo = 0;
   const int64_t ntiles = (n + 127) / 128;
@@ -714,7 +784,7 @@ int ed_restart_combine_tc(ed_ctx* ctx, const double* const* cols, int m, const d
   if (m < 1 || m > TC_MAX_COLS) return ED_ENOTSUP;
   const int kp = ((m + 1) / 2) * 16;
   const int kgroups = kp / 8;
-  const size_t smem = std::max<size_t>((size_t)kgroups * (TC_ROWS / 8 + TC_N / 8) * 128, 57 * 1024);
+  const size_t smem = (size_t)kgroups * (2 * (TC_ROWS / 8) + TC_N / 8) * 128;  // two A stages and B
   const size_t bwords = (size_t)kgroups * TC_N * 8;  // halves per group
   const int ngroups = (l + 7) / 8;
   ED_TRY(ed_ensure_reduce(ctx, (size_t)ngroups * bwords / 4 + 8));
@@ -733,13 +803,13 @@ int ed_restart_combine_tc(ed_ctx* ctx, const double* const* cols, int m, const d
   ED_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   auto kern = m <= 16 ? k_restart_tc<16> : k_restart_tc<32>;
   ED_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int per_sm = tc_ctas_per_sm(kern, TC_THREADS, smem, TC_TMEM_COLS);
+  const int per_sm = tc_ctas_per_sm(kern, RS_THREADS, smem, RS_TMEM_COLS);
   const int64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->num_sms * per_sm));
   TcCols cp;
   for (int i = 0; i < TC_MAX_COLS; ++i) cp.p[i] = i < m ? cols[i] : nullptr;
   for (int g = 0; g < ngroups; ++g) {
-    kern<<<grid, TC_THREADS, smem, ctx->stream>>>(cp, m, kp, (const uint4*)(dB + (size_t)g * bwords), outs[g],
+    kern<<<grid, RS_THREADS, smem, ctx->stream>>>(cp, m, kp, (const uint4*)(dB + (size_t)g * bwords), outs[g],
                                                   std::min(8, l - g * 8), n, d_err);
     ED_CHECK_LAUNCH(ctx);
   }
