@@ -495,7 +495,7 @@ def gradient_timing(ed, restart='auto', seed=71):
     h_i ~ U[-0.5, 0.5] from mt19937_64(seed + 1).  Timed on the host (each
     step returns host results): the solve (nev=4, tol 1e-12), the
     Hellmann-Feynman gradient of E0 and of the lowest-4 sum, and the adjoint
-    (MINRES) gradient of <S_0.S_far>.  One bond and one field derivative of
+    (MINRES, tol 1e-8, at most 4000 iterations) gradient of <S_0.S_far>.  One bond and one field derivative of
     E0 are checked against central differences (step 1e-5) of device
     energies."""
     import numpy as np
@@ -537,7 +537,7 @@ def gradient_timing(ed, restart='auto', seed=71):
         far = (lx // 2) * ly + ly // 2
         obs = [(1.0, ed.Adjoint.SISJ, 0, far)]
         t0 = time.perf_counter()
-        val, cJ, cD, ch, info = ed.Adjoint.expectation_gradient(h, pairs, e[0], v0, obs, tol=1e-9, max_it=4000)
+        val, cJ, cD, ch, info = ed.Adjoint.expectation_gradient(h, pairs, e[0], v0, obs, tol=1e-8, max_it=4000)
         t_corr = time.perf_counter() - t0
         ed.Solver.SolverClean(eps)
         d = 1e-5

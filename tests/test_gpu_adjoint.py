@@ -331,3 +331,70 @@ def test_c4_square_4x6_gradients(ed, envs):
     hm[5] -= d
     fd0 = (energies(J, D, hp)[0] - energies(J, D, hm)[0]) / (2 * d)
     assert abs(fd0 - dh[5]) <= 1e-6 * max(1.0, abs(fd0))
+
+
+def test_c4_square_4x4_minres_and_correlation_gradient(ed, envs):
+    """4x4 J1-J2 (N=16, Sz=0, dim 12,870) with per-bond couplings
+    J_b = base_b (1 + 0.1 z_b), D_b = J_b, fields U[-0.5, 0.5]: MINRES for
+    (H - E0) lam = P (O - <O>) psi0, O = S_0 . S_far, reaches relres <= 1e-11,
+    lam is orthogonal to psi0 and solves the projected system against the
+    oracle's explicit matrix (1e-9 relative); d<O>/dtheta for two bonds (J and
+    D) and one field against central differences (step 1e-4) of device
+    expectation values, 1e-6 relative."""
+    N, lx, ly, mag = 16, 4, 4, 0
+    pairs, J, D, hi = disordered(1, N, lx, ly, 81, J2=0.5)
+    env = envs(N)
+    b = ed.Basis(env, mag)
+    far = (lx // 2) * ly + ly // 2
+
+    def solve(Jx, Dx, hx):
+        h = ed.Hamiltonian.from_bonds(env, b, pairs, Jx, Dx)
+        h.build_diag(env)
+        h.build_off_diag(env)
+        h.build_disorder(env, hx)
+        eps = ed.Solver.SolverInit(h, 2, 20)
+        ed.Solver.EPSSetTolerances(eps, 1e-13)
+        ed.Solver.solve(env, eps)
+        e0, v, _ = ed.Solver.solution(eps, 0)
+        ed.Solver.SolverClean(eps)
+        return h, e0, v
+
+    def expval(Jx, Dx, hx):
+        _, _, v = solve(Jx, Dx, hx)
+        vn = v / np.sqrt(np.real(v.conj().dot(v).item()))
+        return float(np.real(ed.SiSj(env, b).ExpectVal(env, 0, far, vn)))
+
+    h, e0, v = solve(J, D, hi)
+    obs = [(1.0, ed.Adjoint.SISJ, 0, far)]
+    val, dJ, dD, dh, info = ed.Adjoint.expectation_gradient(h, pairs, e0, v, obs, tol=1e-12)
+    assert info['relres'] <= 1e-11, info
+    assert abs(val - expval(J, D, hi)) <= 1e-10
+    # the adjoint solve itself, against the oracle's explicit matrix
+    psi = v.cpu().numpy()
+    psi = psi / np.linalg.norm(psi)
+    opsi = ed.Adjoint.apply_observable(b, obs, psi).cpu().numpy()
+    rhs = opsi - np.vdot(psi, opsi) * psi
+    lam, its, rel = ed.Adjoint.minres(h, e0, rhs, q=psi, tol=1e-12)
+    lam = lam.cpu().numpy()
+    M = dense_model(N, mag, pairs, J, D, hi)
+    assert abs(np.vdot(psi, lam)) <= 1e-10 * np.linalg.norm(lam)
+    r = M.apply(lam) - e0 * lam - rhs
+    r = r - np.vdot(psi, r) * psi
+    assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(rhs), (np.linalg.norm(r), its, rel)
+    d = 1e-4
+    for q in (3, 40):
+        Jp, Jm = J.copy(), J.copy()
+        Jp[q] += d
+        Jm[q] -= d
+        fd = (expval(Jp, D, hi) - expval(Jm, D, hi)) / (2 * d)
+        assert abs(fd - dJ[q]) <= 1e-6 * max(1.0, abs(fd)), (q, fd, dJ[q])
+        Dp, Dm = D.copy(), D.copy()
+        Dp[q] += d
+        Dm[q] -= d
+        fd = (expval(J, Dp, hi) - expval(J, Dm, hi)) / (2 * d)
+        assert abs(fd - dD[q]) <= 1e-6 * max(1.0, abs(fd)), (q, fd, dD[q])
+    hp, hm = hi.copy(), hi.copy()
+    hp[5] += d
+    hm[5] -= d
+    fd = (expval(J, D, hp) - expval(J, D, hm)) / (2 * d)
+    assert abs(fd - dh[5]) <= 1e-6 * max(1.0, abs(fd)), (fd, dh[5])
