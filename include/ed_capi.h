@@ -132,8 +132,8 @@ int ed_ham_apply_host(ed_ham* h, const ed_cplx* x_host, ed_cplx* y_host);
 /* y = H x for real vectors (double[dim] on the device).  The Hamiltonian is
  * real symmetric, so this is ed_ham_apply on x + 0i with half the storage and
  * traffic; the result equals the real part of ed_ham_apply's bit for bit.
- * Needs the matrix-free two-table kernel (uniform couplings, ED_ACC_FIXED64):
- * ED_ENOTSUP otherwise.  No counterpart in the reference (PETSc vectors there
+ * Needs the matrix-free two-table kernel (ED_ACC_FIXED64; for per-bond
+ * couplings, the run-time compiled form): ED_ENOTSUP otherwise.  No counterpart in the reference (PETSc vectors there
  * are complex128). */
 int ed_ham_apply_real(ed_ham* h, const double* x_dev, double* y_dev);
 /* ed_ham_apply_real fused with the two reductions a Lanczos step takes from
@@ -178,7 +178,11 @@ int ed_ham_export_csr_host(ed_ham* h, int64_t* rowptr_host, int64_t* cols_host, 
  *     largest entry (error <= 2^-57 of max|x| per entry), sums exact in
  *     int64, rounded once to FP64;
  *   ED_ACC_FP64: gathered entries added in FP64.
- * Per-bond Hamiltonians always use FP64. */
+ * Per-bond Hamiltonians (ed_ham_create_bonds) with ED_ACC_FIXED64 use the
+ * run-time compiled two-table kernel where NVRTC is available: each bond's
+ * J_b / 2 becomes a 64-bit fixed-point constant (relative error below 2^-60
+ * of the largest coupling), each row's sum of c_b * xq is exact in 128 bits
+ * and rounded once; elsewhere, and with the other modes, they add in FP64. */
 int ed_ham_set_accumulation(ed_ham* h, int kind);
 /* Diagonal of the assembled matrix (MatGetDiagonal). */
 int ed_ham_diag_host(ed_ham* h, double* out_host);
@@ -192,8 +196,9 @@ int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len);
  * "u8-b1" (static kernels: unroll depth and register budget), "jit" /
  * "jit-b4" (kernel compiled at run time for this operator's bonds, without a
  * register limit / with 4 blocks per SM) or "auto" (autotuner, the default).  All variants give bit-identical results.  ED_ENOTSUP for
- * operators that do not use the two-table kernel (per-bond, CSR, FP64 or
- * 128-bit accumulation).  No counterpart in the reference. */
+ * operators that do not use the two-table kernel (CSR, FP64 or 128-bit
+ * accumulation), and for a static variant on a per-bond operator (only the
+ * run-time compiled ones exist there).  No counterpart in the reference. */
 int ed_ham_set_hv_variant(ed_ham* h, const char* name);
 
 /* ---- eigensolver: replaces Solver:: (src/solver.cpp:7-68) ----------------- */

@@ -239,6 +239,173 @@ JIT_KERNEL(k_hv_jit_b4_r, false, true, 4)
 JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
 )";
 
+// Per-bond couplings: every bond has its own J_b / 2, carried as a 64-bit
+// fixed-point immediate c_b; each flipped bond adds c_b * xq exactly into a
+// 128-bit accumulator, and the row's sum is rounded once to FP64 (integer
+// operations only), then scaled by 2^xexp.
+const char* kKernelsPB = R"(
+struct A128 { u64 lo; i64 hi; };
+__device__ __forceinline__ void mac(A128& a, i64 q, i64 c) {
+  const u64 pl = (u64)q * (u64)c;
+  const i64 ph = __mul64hi(q, c);
+  const u64 s = a.lo + pl;
+  a.hi += ph + (i64)(s < pl);
+  a.lo = s;
+}
+
+template <bool CHECK, bool RX>
+__device__ __forceinline__ void gatherw(const L2* __restrict__ xq, u32 g, bool on, i64 c, A128& ar, A128& ai,
+                                        bool& bad) {
+  if (RX) {
+    const i64 q = on ? ((const i64*)xq)[g] : 0ll;
+    if (CHECK) bad |= q == NAN_Q;
+    mac(ar, q, c);
+  } else {
+    L2 q;
+    if (on) q = xq[g]; else { q.x = 0; q.y = 0; }
+    if (CHECK) bad |= (q.x == NAN_Q) | (q.y == NAN_Q);
+    mac(ar, q.x, c);
+    mac(ai, q.y, c);
+  }
+}
+
+// a * 2^X rounded to nearest even (integer operations; below 2^-1022 -> 0)
+__device__ __forceinline__ double a128_to_double(A128 a, int X) {
+  u64 lo = a.lo;
+  i64 hi = a.hi;
+  const bool neg = hi < 0;
+  if (neg) { lo = ~lo + 1ull; hi = ~hi + (lo == 0ull ? 1ll : 0ll); }
+  const u64 uh = (u64)hi;
+  if (uh == 0ull && lo == 0ull) return 0.0;
+  const int L = uh ? 128 - __clzll((i64)uh) : 64 - __clzll((i64)lo);
+  u64 m;
+  int bexp = X + L + 1022;
+  if (L <= 53) {
+    m = lo << (53 - L);
+  } else {
+    const int sr = L - 53;  // 1 .. 75
+    u64 top, rest;
+    if (sr < 64) { top = (lo >> sr) | (uh << (64 - sr)); rest = lo & ((1ull << sr) - 1ull); }
+    else { top = uh >> (sr - 64); rest = (sr > 64 ? (uh & ((1ull << (sr - 64)) - 1ull)) : 0ull) | lo; }
+    m = top;
+    const u64 half = sr < 64 ? (1ull << (sr - 1)) : 0ull;
+    bool up;
+    if (sr < 64) up = rest > half || (rest == half && (m & 1ull));
+    else {
+      const u64 hb = sr == 64 ? (lo >> 63) : ((uh >> (sr - 65)) & 1ull);
+      const u64 below = sr == 64 ? (lo << 1) : ((uh & ((1ull << (sr - 65)) - 1ull)) | lo);
+      up = hb && (below != 0ull || (m & 1ull));
+    }
+    m += up ? 1ull : 0ull;
+    if (m >> 53) { m >>= 1; ++bexp; }
+  }
+  if (bexp <= 0) return 0.0;
+  return __longlong_as_double((i64)(((u64)neg << 63) | ((u64)bexp << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
+
+template <bool CHECK, bool RX, bool DOT, bool RIO>
+__device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
+                                     const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
+                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
+                                     int xexp, double* dacc) {
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const u32 s = states[r];
+    const u32 c0 = s & LOWMASK, c1 = s >> W0;
+    const u32 rr = (u32)r;
+    const u32 rb0 = rr - (u32)t0s[c0];
+    const u32 c0b = c0 << 1;
+    const u32 rb1 = rr - t1[c1];
+    A128 ar = {0ull, 0ll}, ai = {0ull, 0ll};
+    bool bad = false;
+    BONDS
+    const double d = diag[r];
+    D2 xv;
+    if (RIO) { xv.x = ((const double*)x)[r]; xv.y = 0.0; } else xv = x[r];
+    double yr = fma(d, xv.x, a128_to_double(ar, xexp));
+    double yi = RX ? d * xv.y : fma(d, xv.y, a128_to_double(ai, xexp));
+    if (CHECK && bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
+    if (RIO) ((double*)y)[r] = yr;
+    else { D2 o; o.x = yr; o.y = yi; y[r] = o; }
+    if (DOT) {
+      if (RIO) {
+        dacc[0] = fma(xv.x, yr, dacc[0]);
+        dacc[2] = fma(yr, yr, dacc[2]);
+      } else {
+        dacc[0] = fma(xv.x, yr, fma(xv.y, yi, dacc[0]));
+        dacc[1] = fma(xv.x, yi, fma(-xv.y, yr, dacc[1]));
+        dacc[2] = fma(yr, yr, fma(yi, yi, dacc[2]));
+      }
+    }
+  }
+}
+
+template <bool RX, bool DOT, bool RIO>
+__device__ __noinline__ void rows_checked(const u32* __restrict__ states, const double* __restrict__ diag,
+                                          const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
+                                          i64 dim, const unsigned short* __restrict__ t0s,
+                                          const u32* __restrict__ t1, int xexp, double* dacc) {
+  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+}
+
+template <bool DOT, bool RIO>
+__device__ __forceinline__ void body(const u32* __restrict__ states, const double* __restrict__ diag,
+                                     const D2* __restrict__ x, const L2* __restrict__ xq,
+                                     const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
+                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, int pbexp,
+                                     double* __restrict__ partial) {
+  extern __shared__ unsigned short t0s[];
+  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
+  __syncthreads();
+  const int xexp = gmax_p[0] - 1022 - sbits + pbexp;
+  double dacc[3] = {0.0, 0.0, 0.0};
+  const bool rx = RIO || gmax_p[2] == 0;
+  if (gmax_p[1]) {
+    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+  } else {
+    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+  }
+  if (DOT) {
+    __shared__ double sh[3 * 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < 3; ++k) {
+      double a = dacc[k];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0) sh[k * 32 + wid] = a;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      for (int k = 0; k < 3; ++k) {
+        double a = lane < nw ? sh[k * 32 + lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) partial[k * gridDim.x + blockIdx.x] = a;
+      }
+    }
+  }
+}
+
+#define JIT_KERNEL(NAME, DOT, RIO, MINB)                                                                  \
+  extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
+      const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
+      const u32* t1, int pbexp, double* partial) {                                                          \
+    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, pbexp, partial);                     \
+  }
+JIT_KERNEL(k_hv_jit_b2, false, false, 2)
+JIT_KERNEL(k_hv_jit_dot_b2, true, false, 2)
+JIT_KERNEL(k_hv_jit_b3, false, false, 3)
+JIT_KERNEL(k_hv_jit_dot_b3, true, false, 3)
+JIT_KERNEL(k_hv_jit_b4, false, false, 4)
+JIT_KERNEL(k_hv_jit_dot_b4, true, false, 4)
+JIT_KERNEL(k_hv_jit_b2_r, false, true, 2)
+JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 2)
+JIT_KERNEL(k_hv_jit_b3_r, false, true, 3)
+JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 3)
+JIT_KERNEL(k_hv_jit_b4_r, false, true, 4)
+JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
+)";
+
 // Register budgets of the generated kernels, by the budget index of
 // ed_jit_launch: 0, 1, 2 = two, four, three blocks of 256 per SM.
 const int kJitBudgets = 3;
@@ -325,11 +492,38 @@ std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
   return o.str();
 }
 
+// Per-bond form: the bond's own coefficient c instead of a type accumulator.
+std::string bond_code_pb(int cls, uint32_t m0, uint32_t m1, long long c) {
+  std::ostringstream o;
+  o << "{ ";
+  if (cls == 0) {
+    o << "const u32 t = c0 & " << hex(m0) << "; const bool on = (t != 0u) & (t != " << hex(m0)
+      << "); const u32 g = rb0 + T0B(c0b ^ " << hex(m0 << 1) << "); ";
+  } else if (cls == 1) {
+    o << "const u32 t = c1 & " << hex(m1) << "; const bool on = (t != 0u) & (t != " << hex(m1)
+      << "); const u32 g = rb1 + t1[c1 ^ " << hex(m1) << "]; ";
+  } else {
+    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = T0B(c0b ^ "
+      << hex(m0 << 1) << ") + t1[c1 ^ " << hex(m1) << "]; ";
+  }
+  char cb[40];
+  snprintf(cb, sizeof(cb), "(i64)0x%016llxull", (unsigned long long)c);
+  o << "gatherw<CHECK, RX>(xq, g, on, " << cb << ", ar, ai, bad); }\n    ";
+  return o.str();
+}
+
 }  // namespace
+
+bool ed_jit_available() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  load_apis();
+  return g_nvrtc.ok && g_drv.ok;
+}
 
 // Signature of the operator's bond words (the same hash the autotuner keys on).
 int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
-                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio) {
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio,
+                  const long long* coef, int pbexp) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   JitModule* mod = nullptr;
@@ -345,8 +539,9 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
       for (int cls = 0; cls < 3; ++cls)
         for (int t = 0; t < 2; ++t)
           for (int q = seg[cls * 2 + t]; q < seg[cls * 2 + t + 1]; ++q)
-            bonds << bond_code(cls, t, (uint32_t)words[q], (uint32_t)(words[q] >> 32));
-      std::string kern = kKernels;
+            bonds << (coef ? bond_code_pb(cls, (uint32_t)words[q], (uint32_t)(words[q] >> 32), coef[q])
+                           : bond_code(cls, t, (uint32_t)words[q], (uint32_t)(words[q] >> 32)));
+      std::string kern = coef ? kKernelsPB : kKernels;
       const size_t at = kern.find("BONDS");
       kern.replace(at, 5, bonds.str());
       std::string src = std::string(kPrelude) + "#define W0 " + std::to_string(w0) + "\n#define LOWMASK " +
@@ -418,7 +613,9 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   const uint32_t* t1 = b->d_lin_t1;
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
-  void* args[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  void* args_u[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  void* args_pb[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &pbexp, &partial};
+  void** args = coef ? args_pb : args_u;
   CUresult r = g_drv.launch(mod->fn[bg][kd][ri], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);
   if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");

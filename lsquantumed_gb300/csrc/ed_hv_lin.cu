@@ -19,6 +19,7 @@
 #include "ed_internal.h"
 #include "ed_device.cuh"
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -40,6 +41,10 @@ struct ed_lin {
   LinSegs segs{};
   int built_nb = -1;
   int variant[4] = {-1, -1, -1, -1};  // launch variants [2 * dot + real storage] chosen by lin_autotune; -1: not yet
+  // per-bond couplings: J_b / 2 of each word as fixed point, value = c * 2^pbexp
+  bool per_bond = false;
+  std::vector<long long> coef;
+  int pbexp = 0;
 };
 
 static uint64_t binom(int n, int k) {
@@ -110,6 +115,39 @@ static int lin_prepare(ed_ham* h) {
         }
       }
     sg.seg[6] = n;
+    L->per_bond = h->bs.per_bond != 0;
+    L->coef.clear();
+    if (L->per_bond) {
+      // one coupling per bond: the words by class only (the second type of
+      // each class stays empty), each with its J_b / 2 in fixed point.  With
+      // |xq| < 2^sbits and at most nb terms, |c| < 2^kc keeps every row's
+      // exact sum below 2^126.
+      n = 0;
+      std::vector<double> cf;
+      for (int cls = 0; cls < 3; ++cls) {
+        sg.seg[cls * 2] = n;
+        for (int q = 0; q < h->bs.nb; ++q) {
+          const uint32_t m = h->bs.mask[q];
+          if (__builtin_popcount(m) != 2) continue;
+          const uint32_t m0 = m & low, m1 = m >> b->lin_w0;
+          const int c = m1 == 0 ? 0 : (m0 == 0 ? 1 : 2);
+          if (c != cls) continue;
+          sg.word[n++] = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
+          cf.push_back(h->bs.chalf[h->bs.type[q]]);
+        }
+        sg.seg[cls * 2 + 1] = n;
+      }
+      sg.seg[6] = n;
+      double mx = 0.0;
+      for (double v : cf) mx = std::max(mx, std::fabs(v));
+      int e = 0;
+      if (mx > 0.0) std::frexp(mx, &e);  // mx < 2^e
+      int lg = 0;
+      while ((1 << lg) < h->bs.nb + 1) ++lg;
+      const int kc = 125 - ed_fx64_sbits(h) - lg;
+      for (double v : cf) L->coef.push_back(std::llround(std::ldexp(v, kc - e)));
+      L->pbexp = e - kc;
+    }
     L->built_nb = h->bs.nb;
   }
   return ED_OK;
@@ -278,8 +316,11 @@ __global__ void __launch_bounds__(256, MINB) k_hv_lin(const uint32_t* __restrict
   }
 }
 
+// Per-bond operators take the run-time compiled form only (their
+// coefficients are immediates of the generated code).
 bool ed_lin_supported(const ed_ham* h) {
-  return !h->bs.per_bond && h->mode != ED_HAM_CSR && h->hv_kernel == 2 && h->basis->nspins >= 2;
+  return h->mode != ED_HAM_CSR && h->hv_kernel == 2 && h->basis->nspins >= 2 &&
+         (!h->bs.per_bond || ed_jit_available());
 }
 
 // Launch variants (same results: the integer sums are exact, so the unroll
@@ -309,9 +350,10 @@ static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sb
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const ed_lin* L = h->lin;
+  if (L->per_bond && v < kJitVariant) v = kJitVariant + 1;  // no static per-bond form
   if (v >= kJitVariant)
     return ed_jit_launch(h, lin_signature(h), v - kJitVariant, x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg,
-                         L->segs.w0, rio);
+                         L->segs.w0, rio, L->per_bond ? L->coef.data() : nullptr, L->pbexp);
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
@@ -343,6 +385,11 @@ static uint64_t lin_signature(const ed_ham* h) {
   mix((uint64_t)sg.w0);
   for (int i = 0; i < 7; ++i) mix((uint64_t)sg.seg[i]);
   for (int i = 0; i < sg.seg[6]; ++i) mix(sg.word[i]);
+  if (h->lin->per_bond) {
+    mix(0x5045524230ull);  // the per-bond form: coefficients are part of the code
+    for (long long c : h->lin->coef) mix((uint64_t)c);
+    mix((uint64_t)(int64_t)h->lin->pbexp);
+  }
   return z;
 }
 
@@ -353,7 +400,7 @@ static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, 
   ed_lin* L = h->lin;
   ed_ctx* ctx = h->ctx;
   int& chosen = L->variant[2 * (dot ? 1 : 0) + (rio ? 1 : 0)];
-  chosen = 0;
+  chosen = L->per_bond ? kJitVariant + 1 : 0;
   if (h->basis->dim < (int64_t)1 << 20) return ED_OK;
   const auto key =
       std::make_tuple(ctx->device, h->basis->nspins, h->basis->nup, lin_signature(h), dot ? 1 : 0, rio ? 1 : 0);
@@ -370,7 +417,8 @@ static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, 
   ED_CUDA(cudaEventCreate(&e1));
   float best = 0.0f;
   int rc = ED_OK;
-  for (int v = 0; v < kNumAllVariants && rc == ED_OK; ++v) {
+  bool first = true;
+  for (int v = L->per_bond ? kJitVariant : 0; v < kNumAllVariants && rc == ED_OK; ++v) {
     rc = lin_launch(h, v, x, y, dot, sbits, nullptr, rio);
     if (v >= kJitVariant && rc == ED_ENOTSUP) {  // no run-time compiler here: keep the static choice
       rc = ED_OK;
@@ -382,9 +430,10 @@ static int lin_autotune(ed_ham* h, const void* x, void* y, int sbits, bool dot, 
     float ms = 0.0f;
     if (rc == ED_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
       rc = ed_fail(ED_ECUDA, "event timing");
-    if (rc == ED_OK && (v == 0 || ms < best)) {
+    if (rc == ED_OK && (first || ms < best)) {
       best = ms;
       chosen = v;
+      first = false;
     }
   }
   cudaEventDestroy(e0);
@@ -427,6 +476,8 @@ int ed_lin_set_variant(ed_ham* h, const char* name) {
   for (int i = 0; i < kNumLinVariants; ++i)
     if (strcmp(name, kLinVariants[i].name) == 0) v = i;
   if (v == -2) return ed_fail(ED_EINVAL, std::string("unknown H.v variant ") + name);
+  if (h->lin->per_bond && v >= 0 && v < kJitVariant)
+    return ed_fail(ED_ENOTSUP, "per-bond operators have only the run-time compiled H.v variants");
   for (int& c : h->lin->variant) c = v;
   return ED_OK;
 }

@@ -191,8 +191,14 @@ int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out,
 // The two-table H.v compiled at run time for one operator's bond words
 // (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
 // budget 0, 1, 2: register budget for 2, 4 or 3 blocks of 256 per SM.
+// coef (nullable): per-bond coefficients of the words (the per-bond form);
+// the row sums are then scaled by 2^pbexp.
 int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
-                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio);
+                  int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio,
+                  const long long* coef = nullptr, int pbexp = 0);
+// NVRTC and the driver entry points can be loaded (the run-time compiled
+// kernels can exist at all).
+bool ed_jit_available();
 void ed_lin_invalidate(ed_lin* L);
 const char* ed_lin_variant_name(const ed_ham* h, int dot);
 int ed_lin_set_variant(ed_ham* h, const char* name);
