@@ -194,8 +194,10 @@ int ed_ham_size(const ed_ham* h, int64_t* size);
 int ed_ham_hv_variant(const ed_ham* h, int dot, char* buf, size_t len);
 /* Force the matrix-free H.v launch variant: "u4-b6", "u4-b4", "u8-b4",
  * "u8-b1" (static kernels: unroll depth and register budget), "jit" /
- * "jit-b4" (kernel compiled at run time for this operator's bonds, without a
- * register limit / with 4 blocks per SM) or "auto" (autotuner, the default).  All variants give bit-identical results.  ED_ENOTSUP for
+ * "jit-b4" / "jit-b3" (kernel compiled at run time for this operator's bonds,
+ * blocks of 256 threads, 2 / 4 / 3 blocks per SM), "jit-w3" / "jit-w4" (the
+ * same with one block of 768 / 1024 threads per SM) or "auto" (autotuner,
+ * the default).  All variants give bit-identical results.  ED_ENOTSUP for
  * operators that do not use the two-table kernel (CSR, FP64 or 128-bit
  * accumulation), and for a static variant on a per-bond operator (only the
  * run-time compiled ones exist there).  No counterpart in the reference. */

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <sys/stat.h>
 #include <unistd.h>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -46,6 +47,7 @@ struct Driver {
   CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
                      void**, void**) = nullptr;
   CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+  CUresult (*set_attr)(CUfunction, CUfunction_attribute, int) = nullptr;  // optional
 };
 
 std::mutex g_mu;
@@ -93,6 +95,7 @@ void load_apis() {
   Driver& d = g_drv;
   d.ok = drv_sym("cuModuleLoadData", d.load) && drv_sym("cuModuleGetFunction", d.get) &&
          drv_sym("cuLaunchKernel", d.launch) && drv_sym("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
+  if (!drv_sym("cuFuncSetAttribute", d.set_attr)) d.set_attr = nullptr;
   if (!r.ok) g_why = "NVRTC symbols missing";
   if (!d.ok) g_why = "driver entry points missing";
 }
@@ -106,18 +109,24 @@ struct alignas(16) D2 { double x, y; };
 struct alignas(16) L2 { i64 x, y; };
 #define NAN_Q ((i64)0x8000000000000000ull)
 #define T0B(off) ((u32)*(const unsigned short*)((const char*)t0s + (off)))
+// element of the fixed-point input: real parts only (RX) or (re, im) pairs
+template <bool RX> struct XEt { typedef L2 T; };
+template <> struct XEt<true> { typedef i64 T; };
+template <bool RX> using XE = typename XEt<RX>::T;
 )";
 
 const char* kKernels = R"(
+// One bond's term: the target entry when the bond flips, else zero (a select,
+// not a branch, so the compiler keeps many gathers in flight).
 template <bool CHECK, bool RX>
-__device__ __forceinline__ void gather(const L2* __restrict__ xq, u32 g, bool on, i64& ar, i64& ai, bool& bad) {
+__device__ __forceinline__ void gather(const XE<RX>* p, bool on, i64& ar, i64& ai, bool& bad) {
   if (RX) {
-    const i64 q = on ? ((const i64*)xq)[g] : 0ll;
+    const i64 q = on ? *(const i64*)p : 0ll;
     if (CHECK) bad |= q == NAN_Q;
     ar += q;
   } else {
     L2 q;
-    if (on) q = xq[g]; else { q.x = 0; q.y = 0; }
+    if (on) q = *(const L2*)p; else { q.x = 0; q.y = 0; }
     if (CHECK) bad |= (q.x == NAN_Q) | (q.y == NAN_Q);
     ar += q.x;
     ai += q.y;
@@ -137,6 +146,7 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 rb0 = rr - (u32)t0s[c0];
     const u32 c0b = c0 << 1;  // byte offset of T0[c0]; T0[c0 ^ m] is at c0b ^ (m << 1)
     const u32 rb1 = rr - t1[c1];
+    const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     i64 a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     bool bad = false;
     BONDS
@@ -217,26 +227,37 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   }
 }
 
-#define JIT_KERNEL(NAME, DOT, RIO, MINB)                                                                  \
-  extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
+#define JIT_KERNEL(NAME, DOT, RIO, NT, MINB)                                                              \
+  extern "C" __global__ void __launch_bounds__(NT, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
       const u32* t1, double c0c, double c1c, double* partial) {                                             \
     body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);                  \
   }
 // register budgets: 2, 3 or 4 blocks of 256 per SM (128, 80 or 64 registers);
 // _r: real storage of x and y
-JIT_KERNEL(k_hv_jit_b2, false, false, 2)
-JIT_KERNEL(k_hv_jit_dot_b2, true, false, 2)
-JIT_KERNEL(k_hv_jit_b3, false, false, 3)
-JIT_KERNEL(k_hv_jit_dot_b3, true, false, 3)
-JIT_KERNEL(k_hv_jit_b4, false, false, 4)
-JIT_KERNEL(k_hv_jit_dot_b4, true, false, 4)
-JIT_KERNEL(k_hv_jit_b2_r, false, true, 2)
-JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 2)
-JIT_KERNEL(k_hv_jit_b3_r, false, true, 3)
-JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 3)
-JIT_KERNEL(k_hv_jit_b4_r, false, true, 4)
-JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
+JIT_KERNEL(k_hv_jit_b2, false, false, 256, 2)
+JIT_KERNEL(k_hv_jit_dot_b2, true, false, 256, 2)
+JIT_KERNEL(k_hv_jit_b3, false, false, 256, 3)
+JIT_KERNEL(k_hv_jit_dot_b3, true, false, 256, 3)
+JIT_KERNEL(k_hv_jit_b4, false, false, 256, 4)
+JIT_KERNEL(k_hv_jit_dot_b4, true, false, 256, 4)
+JIT_KERNEL(k_hv_jit_b2_r, false, true, 256, 2)
+JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 256, 2)
+JIT_KERNEL(k_hv_jit_b3_r, false, true, 256, 3)
+JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 256, 3)
+JIT_KERNEL(k_hv_jit_b4_r, false, true, 256, 4)
+JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 256, 4)
+// one block per SM (one copy of T0 in shared memory, the rest of the SM's
+// on-chip memory left to the L1 cache): 768 threads (80 registers) or 1024
+// threads (64 registers)
+JIT_KERNEL(k_hv_jit_w3, false, false, 768, 1)
+JIT_KERNEL(k_hv_jit_dot_w3, true, false, 768, 1)
+JIT_KERNEL(k_hv_jit_w4, false, false, 1024, 1)
+JIT_KERNEL(k_hv_jit_dot_w4, true, false, 1024, 1)
+JIT_KERNEL(k_hv_jit_w3_r, false, true, 768, 1)
+JIT_KERNEL(k_hv_jit_dot_w3_r, true, true, 768, 1)
+JIT_KERNEL(k_hv_jit_w4_r, false, true, 1024, 1)
+JIT_KERNEL(k_hv_jit_dot_w4_r, true, true, 1024, 1)
 )";
 
 // Per-bond couplings: every bond has its own J_b / 2, carried as a 64-bit
@@ -245,6 +266,12 @@ JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
 // operations only), then scaled by 2^xexp.
 const char* kKernelsPB = R"(
 struct A128 { u64 lo; i64 hi; };
+// the bonds' fixed-point couplings: a kernel parameter for the main path; the
+// out-of-line checked path reads the same values from global memory
+struct PBC {
+  i64 c[NBC];
+  __device__ __forceinline__ i64 operator[](int i) const { return c[i]; }
+};
 __device__ __forceinline__ void mac(A128& a, i64 q, i64 c) {
   const u64 pl = (u64)q * (u64)c;
   const i64 ph = __mul64hi(q, c);
@@ -254,15 +281,14 @@ __device__ __forceinline__ void mac(A128& a, i64 q, i64 c) {
 }
 
 template <bool CHECK, bool RX>
-__device__ __forceinline__ void gatherw(const L2* __restrict__ xq, u32 g, bool on, i64 c, A128& ar, A128& ai,
-                                        bool& bad) {
+__device__ __forceinline__ void gatherw(const XE<RX>* p, bool on, i64 c, A128& ar, A128& ai, bool& bad) {
   if (RX) {
-    const i64 q = on ? ((const i64*)xq)[g] : 0ll;
+    const i64 q = on ? *(const i64*)p : 0ll;
     if (CHECK) bad |= q == NAN_Q;
     mac(ar, q, c);
   } else {
     L2 q;
-    if (on) q = xq[g]; else { q.x = 0; q.y = 0; }
+    if (on) q = *(const L2*)p; else { q.x = 0; q.y = 0; }
     if (CHECK) bad |= (q.x == NAN_Q) | (q.y == NAN_Q);
     mac(ar, q.x, c);
     mac(ai, q.y, c);
@@ -303,11 +329,11 @@ __device__ __forceinline__ double a128_to_double(A128 a, int X) {
   return __longlong_as_double((i64)(((u64)neg << 63) | ((u64)bexp << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
-template <bool CHECK, bool RX, bool DOT, bool RIO>
+template <bool CHECK, bool RX, bool DOT, bool RIO, typename CF>
 __device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                      i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
-                                     int xexp, double* dacc) {
+                                     int xexp, double* dacc, const CF& cf) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
     const u32 s = states[r];
@@ -316,6 +342,7 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 rb0 = rr - (u32)t0s[c0];
     const u32 c0b = c0 << 1;
     const u32 rb1 = rr - t1[c1];
+    const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     A128 ar = {0ull, 0ll}, ai = {0ull, 0ll};
     bool bad = false;
     BONDS
@@ -344,8 +371,9 @@ template <bool RX, bool DOT, bool RIO>
 __device__ __noinline__ void rows_checked(const u32* __restrict__ states, const double* __restrict__ diag,
                                           const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                           i64 dim, const unsigned short* __restrict__ t0s,
-                                          const u32* __restrict__ t1, int xexp, double* dacc) {
-  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+                                          const u32* __restrict__ t1, int xexp, double* dacc,
+                                          const i64* __restrict__ gcf) {
+  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
 }
 
 template <bool DOT, bool RIO>
@@ -353,7 +381,7 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
                                      const D2* __restrict__ x, const L2* __restrict__ xq,
                                      const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
                                      const unsigned short* __restrict__ t0, const u32* __restrict__ t1, int pbexp,
-                                     double* __restrict__ partial) {
+                                     double* __restrict__ partial, const PBC& pbc, const i64* __restrict__ gcf) {
   extern __shared__ unsigned short t0s[];
   for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
@@ -361,11 +389,11 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   double dacc[3] = {0.0, 0.0, 0.0};
   const bool rx = RIO || gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
-    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
+    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
   } else {
-    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
-    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc);
+    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, pbc);
+    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, pbc);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -386,30 +414,43 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   }
 }
 
-#define JIT_KERNEL(NAME, DOT, RIO, MINB)                                                                  \
-  extern "C" __global__ void __launch_bounds__(256, MINB) NAME(const u32* states, const double* diag,        \
+#define JIT_KERNEL(NAME, DOT, RIO, NT, MINB)                                                              \
+  extern "C" __global__ void __launch_bounds__(NT, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
-      const u32* t1, int pbexp, double* partial) {                                                          \
-    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, pbexp, partial);                     \
+      const u32* t1, int pbexp, double* partial, const __grid_constant__ PBC pbc, const i64* gcf) {         \
+    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, pbexp, partial, pbc, gcf);           \
   }
-JIT_KERNEL(k_hv_jit_b2, false, false, 2)
-JIT_KERNEL(k_hv_jit_dot_b2, true, false, 2)
-JIT_KERNEL(k_hv_jit_b3, false, false, 3)
-JIT_KERNEL(k_hv_jit_dot_b3, true, false, 3)
-JIT_KERNEL(k_hv_jit_b4, false, false, 4)
-JIT_KERNEL(k_hv_jit_dot_b4, true, false, 4)
-JIT_KERNEL(k_hv_jit_b2_r, false, true, 2)
-JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 2)
-JIT_KERNEL(k_hv_jit_b3_r, false, true, 3)
-JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 3)
-JIT_KERNEL(k_hv_jit_b4_r, false, true, 4)
-JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 4)
+JIT_KERNEL(k_hv_jit_b2, false, false, 256, 2)
+JIT_KERNEL(k_hv_jit_dot_b2, true, false, 256, 2)
+JIT_KERNEL(k_hv_jit_b3, false, false, 256, 3)
+JIT_KERNEL(k_hv_jit_dot_b3, true, false, 256, 3)
+JIT_KERNEL(k_hv_jit_b4, false, false, 256, 4)
+JIT_KERNEL(k_hv_jit_dot_b4, true, false, 256, 4)
+JIT_KERNEL(k_hv_jit_b2_r, false, true, 256, 2)
+JIT_KERNEL(k_hv_jit_dot_b2_r, true, true, 256, 2)
+JIT_KERNEL(k_hv_jit_b3_r, false, true, 256, 3)
+JIT_KERNEL(k_hv_jit_dot_b3_r, true, true, 256, 3)
+JIT_KERNEL(k_hv_jit_b4_r, false, true, 256, 4)
+JIT_KERNEL(k_hv_jit_dot_b4_r, true, true, 256, 4)
+// one block per SM (one copy of T0 in shared memory, the rest of the SM's
+// on-chip memory left to the L1 cache): 768 threads (80 registers) or 1024
+// threads (64 registers)
+JIT_KERNEL(k_hv_jit_w3, false, false, 768, 1)
+JIT_KERNEL(k_hv_jit_dot_w3, true, false, 768, 1)
+JIT_KERNEL(k_hv_jit_w4, false, false, 1024, 1)
+JIT_KERNEL(k_hv_jit_dot_w4, true, false, 1024, 1)
+JIT_KERNEL(k_hv_jit_w3_r, false, true, 768, 1)
+JIT_KERNEL(k_hv_jit_dot_w3_r, true, true, 768, 1)
+JIT_KERNEL(k_hv_jit_w4_r, false, true, 1024, 1)
+JIT_KERNEL(k_hv_jit_dot_w4_r, true, true, 1024, 1)
 )";
 
 // Register budgets of the generated kernels, by the budget index of
-// ed_jit_launch: 0, 1, 2 = two, four, three blocks of 256 per SM.
-const int kJitBudgets = 3;
-const char* const kJitBudgetSuffix[kJitBudgets] = {"b2", "b4", "b3"};
+// ed_jit_launch: 0, 1, 2 = two, four, three blocks of 256 per SM; 3, 4 = one
+// block of 768 or 1024 per SM.
+const int kJitBudgets = 5;
+const char* const kJitBudgetSuffix[kJitBudgets] = {"b2", "b4", "b3", "w3", "w4"};
+const int kJitThreads[kJitBudgets] = {256, 256, 256, 768, 1024};
 
 struct JitModule {
   bool ok = false;
@@ -471,45 +512,41 @@ std::string hex(uint32_t v) {
   return b;
 }
 
-// One bond's code: class 0 (inside the low half), 1 (inside the high half),
-// 2 (across); type selects the accumulators (nn: a0/a1, nnn: a2/a3).
-std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1) {
-  std::ostringstream o;
-  const char* ar = type ? "a2" : "a0";
-  const char* ai = type ? "a3" : "a1";
-  o << "{ ";
-  if (cls == 0) {
-    o << "const u32 t = c0 & " << hex(m0) << "; const bool on = (t != 0u) & (t != " << hex(m0)
-      << "); const u32 g = rb0 + T0B(c0b ^ " << hex(m0 << 1) << "); ";
-  } else if (cls == 1) {
-    o << "const u32 t = c1 & " << hex(m1) << "; const bool on = (t != 0u) & (t != " << hex(m1)
-      << "); const u32 g = rb1 + t1[c1 ^ " << hex(m1) << "]; ";
-  } else {
-    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = T0B(c0b ^ "
-      << hex(m0 << 1) << ") + t1[c1 ^ " << hex(m1) << "]; ";
-  }
-  o << "gather<CHECK, RX>(xq, g, on, " << ar << ", " << ai << ", bad); }\n    ";
-  return o.str();
+// Flip test of a bond: with the bond's sites lo < hi in the state word, the
+// spins differ when bit lo of z_d = s ^ (s >> d), d = hi - lo, is set: one
+// AND with an immediate per bond.  The bonds are emitted grouped by d, each
+// group after its z_d, so that one z_d is live at a time.  A mask that is not
+// two distinct sites never flips (d = -1).
+std::string flip_test(uint32_t m0, uint32_t m1, int w0, int* d_out) {
+  const uint64_t m = (uint64_t)m0 | ((uint64_t)m1 << w0);
+  *d_out = -1;
+  if (__builtin_popcountll(m) != 2) return "false";
+  const int lo = __builtin_ctzll(m), hi = 63 - __builtin_clzll(m);
+  *d_out = hi - lo;
+  return "((z" + std::to_string(hi - lo) + " & " + hex(1u << lo) + ") != 0u)";
 }
 
-// Per-bond form: the bond's own coefficient c instead of a type accumulator.
-std::string bond_code_pb(int cls, uint32_t m0, uint32_t m1, long long c) {
-  std::ostringstream o;
-  o << "{ ";
-  if (cls == 0) {
-    o << "const u32 t = c0 & " << hex(m0) << "; const bool on = (t != 0u) & (t != " << hex(m0)
-      << "); const u32 g = rb0 + T0B(c0b ^ " << hex(m0 << 1) << "); ";
-  } else if (cls == 1) {
-    o << "const u32 t = c1 & " << hex(m1) << "; const bool on = (t != 0u) & (t != " << hex(m1)
-      << "); const u32 g = rb1 + t1[c1 ^ " << hex(m1) << "]; ";
-  } else {
-    o << "const bool on = ((c0 & " << hex(m0) << ") != 0u) != ((c1 & " << hex(m1) << ") != 0u); const u32 g = T0B(c0b ^ "
-      << hex(m0 << 1) << ") + t1[c1 ^ " << hex(m1) << "]; ";
-  }
-  char cb[40];
-  snprintf(cb, sizeof(cb), "(i64)0x%016llxull", (unsigned long long)c);
-  o << "gatherw<CHECK, RX>(xq, g, on, " << cb << ", ar, ai, bad); }\n    ";
-  return o.str();
+// Address of a bond's target entry, rank(s ^ m): class 0 (both sites in the
+// low half), 1 (both in the high half), 2 (across).
+std::string target(int cls, uint32_t m0, uint32_t m1) {
+  if (cls == 0) return "xe + (rb0 + T0B(c0b ^ " + hex(m0 << 1) + "))";
+  if (cls == 1) return "xe + (rb1 + t1[c1 ^ " + hex(m1) + "])";
+  return "xe + (T0B(c0b ^ " + hex(m0 << 1) + ") + t1[c1 ^ " + hex(m1) + "])";
+}
+
+// One bond's code; type selects the accumulators (nn: a0/a1, nnn: a2/a3).
+std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1, int w0, int* d) {
+  const char* ar = type ? "a2" : "a0";
+  const char* ai = type ? "a3" : "a1";
+  const std::string on = flip_test(m0, m1, w0, d);
+  return "gather<CHECK, RX>(" + target(cls, m0, m1) + ", " + on + ", " + ar + ", " + ai + ", bad);\n    ";
+}
+
+// Per-bond form: the bond's own coefficient (entry q of the kernel's
+// coefficient parameter) instead of a type accumulator.
+std::string bond_code_pb(int cls, uint32_t m0, uint32_t m1, int q, int w0, int* d) {
+  const std::string on = flip_test(m0, m1, w0, d);
+  return "gatherw<CHECK, RX>(" + target(cls, m0, m1) + ", " + on + ", cf[" + std::to_string(q) + "], ar, ai, bad);\n    ";
 }
 
 }  // namespace
@@ -523,7 +560,7 @@ bool ed_jit_available() {
 // Signature of the operator's bond words (the same hash the autotuner keys on).
 int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
                   int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio,
-                  const long long* coef, int pbexp) {
+                  const long long* coef, const long long* coef_dev, int pbexp) {
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   JitModule* mod = nullptr;
@@ -535,17 +572,29 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
     auto it = g_modules.find(key);
     if (it == g_modules.end()) {
       JitModule jm;
-      std::ostringstream bonds;
+      std::vector<std::pair<int, std::string>> code;  // (d, bond code)
+      std::vector<int> dists;
       for (int cls = 0; cls < 3; ++cls)
         for (int t = 0; t < 2; ++t)
-          for (int q = seg[cls * 2 + t]; q < seg[cls * 2 + t + 1]; ++q)
-            bonds << (coef ? bond_code_pb(cls, (uint32_t)words[q], (uint32_t)(words[q] >> 32), coef[q])
-                           : bond_code(cls, t, (uint32_t)words[q], (uint32_t)(words[q] >> 32)));
+          for (int q = seg[cls * 2 + t]; q < seg[cls * 2 + t + 1]; ++q) {
+            const uint32_t m0 = (uint32_t)words[q], m1 = (uint32_t)(words[q] >> 32);
+            int d = -1;
+            std::string c = coef ? bond_code_pb(cls, m0, m1, q, w0, &d) : bond_code(cls, t, m0, m1, w0, &d);
+            if (d >= 0 && std::find(dists.begin(), dists.end(), d) == dists.end()) dists.push_back(d);
+            code.emplace_back(d, c);
+          }
+      std::ostringstream body;
+      for (int d : dists) {
+        body << "{ const u32 z" << d << " = s ^ (s >> " << d << "u);\n    ";
+        for (auto& c : code)
+          if (c.first == d) body << c.second;
+        body << "}\n    ";
+      }
       std::string kern = coef ? kKernelsPB : kKernels;
       const size_t at = kern.find("BONDS");
-      kern.replace(at, 5, bonds.str());
+      kern.replace(at, 5, body.str());
       std::string src = std::string(kPrelude) + "#define W0 " + std::to_string(w0) + "\n#define LOWMASK " +
-                        hex((1u << w0) - 1u) + "\n" + kern;
+                        hex((1u << w0) - 1u) + "\n#define NBC " + std::to_string(std::max(1, seg[6])) + "\n" + kern;
       const char* opts[] = {"-arch=sm_103a", "-std=c++17", "-default-device"};
       const std::string dir = cache_dir();
       char name[40];
@@ -583,8 +632,15 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
             const std::string fname = std::string(k ? "k_hv_jit_dot_" : "k_hv_jit_") + kJitBudgetSuffix[bg] +
                                       (ri ? "_r" : "");
             got = g_drv.get(&jm.fn[bg][k][ri], m, fname.c_str()) == CUDA_SUCCESS;
+            if (got && kJitThreads[bg] > 256) {
+              // a single block per SM needs only its copy of T0: ask for the
+              // smallest shared-memory carveout that holds it (a hint)
+              const int pct = (int)std::min<size_t>(100, ((smem + 1024) * 100 + 228 * 1024 - 1) / (228 * 1024));
+              if (g_drv.set_attr) g_drv.set_attr(jm.fn[bg][k][ri], CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, pct);
+            }
             int ps = 0;
-            if (got && (g_drv.occupancy(&ps, jm.fn[bg][k][ri], 256, smem) != CUDA_SUCCESS || ps < 1)) ps = 1;
+            if (got && (g_drv.occupancy(&ps, jm.fn[bg][k][ri], kJitThreads[bg], smem) != CUDA_SUCCESS || ps < 1))
+              ps = 1;
             jm.per_sm[bg][k][ri] = ps;
           }
       if (!got) {
@@ -599,8 +655,9 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   }
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
   if (budget < 0 || budget >= kJitBudgets) return ed_fail(ED_EINVAL, "unknown register budget");
-  int64_t g = (b->dim + 255) / 256;
   const int bg = budget, kd = dot ? 1 : 0, ri = rio ? 1 : 0;
+  const int nt = kJitThreads[bg];
+  int64_t g = (b->dim + nt - 1) / nt;
   g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)ctx->num_sms * mod->per_sm[bg][kd][ri]));
   const int nblk = (int)g;
   if (dot) ED_TRY(ed_ensure_reduce(ctx, (size_t)3 * nblk + 8));
@@ -614,9 +671,11 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
   void* args_u[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
-  void* args_pb[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &pbexp, &partial};
+  std::vector<long long> pbc(coef ? std::max(1, seg[6]) : 0, 0ll);  // the PBC parameter's bytes
+  if (coef) std::copy(coef, coef + seg[6], pbc.begin());
+  void* args_pb[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &pbexp, &partial, pbc.data(), &coef_dev};
   void** args = coef ? args_pb : args_u;
-  CUresult r = g_drv.launch(mod->fn[bg][kd][ri], (unsigned)nblk, 1, 1, 256, 1, 1, (unsigned)smem,
+  CUresult r = g_drv.launch(mod->fn[bg][kd][ri], (unsigned)nblk, 1, 1, (unsigned)nt, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);
   if (r != CUDA_SUCCESS) return ed_fail(ED_ECUDA, "launch of the compiled H.v failed");
   ctx->kernels++;

@@ -44,7 +44,11 @@ struct ed_lin {
   // per-bond couplings: J_b / 2 of each word as fixed point, value = c * 2^pbexp
   bool per_bond = false;
   std::vector<long long> coef;
+  long long* d_coef = nullptr;  // device copy of coef (ED_MAX_BONDS entries)
   int pbexp = 0;
+  ~ed_lin() {
+    if (d_coef) cudaFree(d_coef);
+  }
 };
 
 static uint64_t binom(int n, int k) {
@@ -147,6 +151,14 @@ static int lin_prepare(ed_ham* h) {
       const int kc = 125 - ed_fx64_sbits(h) - lg;
       for (double v : cf) L->coef.push_back(std::llround(std::ldexp(v, kc - e)));
       L->pbexp = e - kc;
+      if (!L->d_coef && cudaMalloc(&L->d_coef, sizeof(long long) * ED_MAX_BONDS) != cudaSuccess) {
+        cudaGetLastError();
+        L->d_coef = nullptr;
+        return ed_fail(ED_ENOMEM, "per-bond coefficient table does not fit in device memory");
+      }
+      if (!L->coef.empty())
+        ED_CUDA(cudaMemcpyAsync(L->d_coef, L->coef.data(), sizeof(long long) * L->coef.size(), cudaMemcpyHostToDevice,
+                                h->ctx->stream));  // ordered after earlier launches that read it
     }
     L->built_nb = h->bs.nb;
   }
@@ -339,11 +351,11 @@ static const LinVariant kLinVariants[] = {
 };
 static const int kNumLinVariants = (int)(sizeof(kLinVariants) / sizeof(kLinVariants[0]));
 
-// Variants kNumLinVariants + 0, 1, 2 are the run-time specialised kernel
-// (ed_hv_jit.cu) with its three register budgets.
+// Variants kNumLinVariants + 0 .. 4 are the run-time specialised kernel
+// (ed_hv_jit.cu) with its five register budgets and block shapes.
 static const int kJitVariant = kNumLinVariants;
-static const int kNumAllVariants = kNumLinVariants + 3;
-static const char* const kJitNames[3] = {"jit", "jit-b4", "jit-b3"};
+static const int kNumAllVariants = kNumLinVariants + 5;
+static const char* const kJitNames[5] = {"jit", "jit-b4", "jit-b3", "jit-w3", "jit-w4"};
 static uint64_t lin_signature(const ed_ham* h);
 
 static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sbits, int* nblk_out, bool rio) {
@@ -353,7 +365,7 @@ static int lin_launch(ed_ham* h, int v, const void* x, void* y, bool dot, int sb
   if (L->per_bond && v < kJitVariant) v = kJitVariant + 1;  // no static per-bond form
   if (v >= kJitVariant)
     return ed_jit_launch(h, lin_signature(h), v - kJitVariant, x, y, dot, sbits, nblk_out, L->segs.word, L->segs.seg,
-                         L->segs.w0, rio, L->per_bond ? L->coef.data() : nullptr, L->pbexp);
+                         L->segs.w0, rio, L->per_bond ? L->coef.data() : nullptr, L->d_coef, L->pbexp);
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
   LinKernel k = dot ? kLinVariants[v].dot : kLinVariants[v].plain;
   int per_sm = 0;
@@ -385,11 +397,7 @@ static uint64_t lin_signature(const ed_ham* h) {
   mix((uint64_t)sg.w0);
   for (int i = 0; i < 7; ++i) mix((uint64_t)sg.seg[i]);
   for (int i = 0; i < sg.seg[6]; ++i) mix(sg.word[i]);
-  if (h->lin->per_bond) {
-    mix(0x5045524230ull);  // the per-bond form: coefficients are part of the code
-    for (long long c : h->lin->coef) mix((uint64_t)c);
-    mix((uint64_t)(int64_t)h->lin->pbexp);
-  }
+  if (h->lin->per_bond) mix(0x5045524230ull);  // the per-bond form (its couplings are launch parameters)
   return z;
 }
 
@@ -471,7 +479,7 @@ int ed_lin_set_variant(ed_ham* h, const char* name) {
   ED_TRY(lin_prepare(h));
   int v = -2;
   if (strcmp(name, "auto") == 0) v = -1;
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < kNumAllVariants - kJitVariant; ++i)
     if (strcmp(name, kJitNames[i]) == 0) v = kJitVariant + i;
   for (int i = 0; i < kNumLinVariants; ++i)
     if (strcmp(name, kLinVariants[i].name) == 0) v = i;

@@ -190,12 +190,14 @@ bool ed_lin_supported(const ed_ham* h);
 int ed_launch_hv_lin(ed_ham* h, const void* x, void* y, bool dot, int* nblk_out, bool rio);
 // The two-table H.v compiled at run time for one operator's bond words
 // (ed_hv_jit.cu); ED_ENOTSUP where no run-time compiler is available.
-// budget 0, 1, 2: register budget for 2, 4 or 3 blocks of 256 per SM.
-// coef (nullable): per-bond coefficients of the words (the per-bond form);
-// the row sums are then scaled by 2^pbexp.
+// budget 0, 1, 2: register budget for 2, 4 or 3 blocks of 256 per SM; 3, 4:
+// one block of 768 or 1024 per SM.
+// coef (nullable): per-bond coefficients of the words (the per-bond form),
+// on the host (passed as a launch parameter) and in device memory (coef_dev,
+// read by the checked path); the row sums are then scaled by 2^pbexp.
 int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void* y, bool dot, int sbits,
                   int* nblk_out, const unsigned long long* words, const int* seg, int w0, bool rio,
-                  const long long* coef = nullptr, int pbexp = 0);
+                  const long long* coef = nullptr, const long long* coef_dev = nullptr, int pbexp = 0);
 // NVRTC and the driver entry points can be loaded (the run-time compiled
 // kernels can exist at all).
 bool ed_jit_available();

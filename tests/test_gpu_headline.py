@@ -110,7 +110,7 @@ def test_c5_hv_sampled_rows(ed):
     rows_t = torch.from_numpy(rows).cuda()
     y = torch.empty_like(x)
     yd = torch.empty_like(x)
-    for v in ('auto', 'jit-b3', 'jit-b4', 'jit', 'u4-b6'):
+    for v in ('auto', 'jit-b3', 'jit-b4', 'jit', 'jit-w3', 'jit-w4', 'u4-b6'):
         h.set_hv_variant(v)
         h.apply_real(x, out=y)
         err = np.abs(y[rows_t].cpu().numpy() - ref).max()

@@ -299,7 +299,7 @@ def test_hv_real_storage(ed, envs, case):
     xbad = xr.copy()
     xbad[7] = np.nan
     cols = set(M.scipy()[:, 7].nonzero()[0]) | {7}
-    for v in ('auto', 'u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3'):
+    for v in ('auto', 'u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3', 'jit-w3', 'jit-w4'):
         h.set_hv_variant(v)
         y = h.apply_real(xr).cpu().numpy()
         assert np.array_equal(y.view(np.uint64), ref.view(np.uint64)), v
@@ -320,7 +320,7 @@ def test_hv_variants_bit_identical(ed, envs):
     xc = oracle.start_vector(8, b.size)
     xr = xc.real.astype(np.complex128)
     ref = {}
-    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3'):
+    for v in ('u4-b6', 'u4-b4', 'u8-b4', 'u8-b1', 'jit', 'jit-b4', 'jit-b3', 'jit-w3', 'jit-w4'):
         h.set_hv_variant(v)
         for name, x in (('complex', xc), ('real', xr)):
             y = h.apply(x).cpu().numpy()
@@ -712,7 +712,7 @@ def test_hv_per_bond_fixed_point(ed, envs, case):
     xr = x.real.copy()
     ref = M.apply(xr.astype(np.complex128)).real
     first = None
-    for v in ('jit', 'jit-b4', 'jit-b3'):
+    for v in ('jit', 'jit-b4', 'jit-b3', 'jit-w3', 'jit-w4'):
         h.set_hv_variant(v)
         y = h.apply_real(xr).cpu().numpy()
         assert np.abs(y - ref).max() <= 1e-14 * np.linalg.norm(xr), v
