@@ -388,7 +388,7 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     batch_evals = {}
     for mag in sectors:
         bt = ed.DisorderBatch(hams[mag][1], fields)
-        bt.set_restart_arithmetic(restart)
+        bt.set_restart_arithmetic(restart if restart in ('auto', 'fp64', 'pair') else 'auto')
         r = bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
         max_err = max(max_err, float(r['errs'].max()))
         bad += int((r['nconv'] < nev).sum())
@@ -928,9 +928,10 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sisj', action='store_true', help='skip the all-pairs <S_i.S_j> measurement')
     ap.add_argument('--real-input', action='store_true', help='--hv-only with a real input vector')
-    ap.add_argument('--restart', default='auto', choices=('auto', 'fp64', 'pair'),
+    ap.add_argument('--restart', default='auto', choices=('auto', 'fp64', 'pair', 'fixed', 'exact'),
                     help='restart-combination products of the real-storage solve (auto: the fastest form with every '
-                         'product FP64 or better; pair: float pairs on the FP32 units)')
+                         'product FP64 or better; fp64: FP64 beside exact integers; fixed: 56-bit fixed point on the '
+                         'integer units; pair: float pairs on the FP32 units; exact: tensor-core slices)')
     ap.add_argument('--no-extra', action='store_true', help='skip the C3 / C4 sub-objects of the default line')
     ap.add_argument('--probe-rates', action='store_true',
                     help='print the measured FP64 FMA / FP64 mma / FP16-FP32 mma rates and exit')

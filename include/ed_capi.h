@@ -224,12 +224,17 @@ int ed_eps_set_seed(ed_eps* e, uint64_t seed);
  * storage and sums stay FP64), below FP64 accuracy, so only on request.
  * ED_RESTART_EXACT: exact slices on the tensor cores for the restart
  * combination and the Gram-Schmidt projections (ed_bv_mult_real,
- * ed_bv_dot_real; ncv <= 32).  ED_RESTART_AUTO (default): ED_RESTART_FP64.
- * No counterpart in the reference (FP64 throughout). */
+ * ed_bv_dot_real; ncv <= 32).  ED_RESTART_FIXED: the restart combination on
+ * the integer units: each row of V in 56-bit fixed point against the row's
+ * largest entry, each column of Y against its own, exact products of 28-bit
+ * limbs, one rounding per output (error below 2^-51 of max|V row| * max|Y
+ * column|; ncv <= 32, FP64 beyond).  ED_RESTART_AUTO (default):
+ * ED_RESTART_FP64.  No counterpart in the reference (FP64 throughout). */
 #define ED_RESTART_AUTO 0
 #define ED_RESTART_FP64 1
 #define ED_RESTART_PAIR 2
 #define ED_RESTART_EXACT 3
+#define ED_RESTART_FIXED 4
 int ed_eps_set_restart_arithmetic(ed_eps* e, int mode);
 /* The restart combination on its own: out_c = sum_{i<m} V_i Y[i*ldY + c] for
  * c < l, real device vectors of n entries (V_dev and out_dev: host arrays of
@@ -239,7 +244,9 @@ int ed_eps_set_restart_arithmetic(ed_eps* e, int mode);
  * ED_RESTART_EXACT: the products on the tensor cores in exact 8-bit slices of
  * 63-bit fixed point (per 128-row tile of V, per column of Y), level sums
  * combined exactly and rounded once to FP64 (m <= 32, ED_ENOTSUP beyond);
- * ED_RESTART_AUTO picks what the solver would by default (ED_RESTART_FP64).
+ * ED_RESTART_FIXED: 56-bit fixed point per row of V and column of Y, exact
+ * integer products (m <= 32; the FP64 form beyond); ED_RESTART_AUTO picks
+ * what the solver would by default.
  * Synchronises the stream. */
 int ed_bv_mult_real(ed_ctx* ctx, const double* const* V_dev, int m, const double* Y_host, int ldY, int l,
                     double* const* out_dev, int64_t n, int arith);

@@ -16,7 +16,7 @@ ED_OP_SZSZ, ED_OP_SPSM, ED_OP_SMSP, ED_OP_SISJ = 0, 1, 2, 3
 ED_HAM_MATRIX_FREE, ED_HAM_CSR = 0, 1
 ED_ACC_FP64, ED_ACC_EXACT, ED_ACC_FIXED64 = 0, 1, 2
 ED_TERM_XY, ED_TERM_ZZ, ED_TERM_Z, ED_TERM_SISJ = 0, 1, 2, 3
-ED_RESTART_AUTO, ED_RESTART_FP64, ED_RESTART_PAIR, ED_RESTART_EXACT = 0, 1, 2, 3
+ED_RESTART_AUTO, ED_RESTART_FP64, ED_RESTART_PAIR, ED_RESTART_EXACT, ED_RESTART_FIXED = 0, 1, 2, 3, 4
 
 _ERRNAMES = {1: 'EINVAL', 2: 'ECUDA', 3: 'ENOMEM', 4: 'ESTATE', 5: 'ENOTCONV', 6: 'ENOTSUP'}
 

@@ -464,7 +464,8 @@ int ed_bv_mult_real(ed_ctx* ctx, const double* const* V_dev, int m, const double
     for (int c = 0; c < l; ++c)
       if (V_dev[i] == out_dev[c]) return ed_fail(ED_EINVAL, "out must not alias V");
   if (arith == ED_RESTART_AUTO) arith = ED_RESTART_FP64;
-  if (arith != ED_RESTART_FP64 && arith != ED_RESTART_PAIR && arith != ED_RESTART_EXACT)
+  if (arith != ED_RESTART_FP64 && arith != ED_RESTART_PAIR && arith != ED_RESTART_EXACT &&
+      arith != ED_RESTART_FIXED)
     return ed_fail(ED_EINVAL, "unknown restart arithmetic");
   if (arith == ED_RESTART_EXACT && m > 32) return ed_fail(ED_ENOTSUP, "the exact restart takes at most 32 vectors");
   ED_CUDA(cudaSetDevice(ctx->device));

@@ -187,3 +187,46 @@ static inline float2 ed_host_pair(double v) {
   const float hi = (float)v;
   return make_float2(hi, (float)(v - (double)hi));
 }
+
+// 128-bit signed T times 2^X, rounded to nearest even, as an FP64 value,
+// with integer operations only.  Results below 2^-1022 flush to zero.
+__device__ __forceinline__ double ed_fx128_to_double(long long hi, unsigned long long lo, int X) {
+  const bool neg = hi < 0;
+  if (neg) {
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ll : 0ll);
+  }
+  const unsigned long long uh = (unsigned long long)hi;
+  if (uh == 0ull && lo == 0ull) return 0.0;
+  const int L = uh ? 128 - __clzll((long long)uh) : 64 - __clzll((long long)lo);  // bit length
+  unsigned long long m;
+  int bexp = X + L + 1022;
+  if (L <= 53) {
+    m = lo << (53 - L);
+  } else {
+    const int sr = L - 53;  // 1 .. 75
+    unsigned long long rem, half;
+    if (sr < 64) {
+      m = (lo >> sr) | (sr ? (uh << (64 - sr)) : 0ull);
+      rem = lo & ((1ull << sr) - 1ull);
+      half = 1ull << (sr - 1);
+      const bool up = rem > half || (rem == half && (m & 1ull));
+      m += up ? 1ull : 0ull;
+    } else {
+      const int s2 = sr - 64;
+      m = uh >> s2;
+      const unsigned long long remh = uh & ((s2 ? (1ull << s2) : 1ull) - 1ull);
+      const bool gt = s2 ? (remh > (1ull << (s2 - 1)) || (remh == (1ull << (s2 - 1)) && lo != 0ull)) : (lo > (1ull << 63));
+      const bool eq = s2 ? (remh == (1ull << (s2 - 1)) && lo == 0ull) : (lo == (1ull << 63));
+      m += (gt || (eq && (m & 1ull))) ? 1ull : 0ull;
+    }
+    if (m >> 53) {
+      m >>= 1;
+      ++bexp;
+    }
+  }
+  if (bexp <= 0) return 0.0;
+  const unsigned long long bits =
+      ((unsigned long long)neg << 63) | ((unsigned long long)bexp << 52) | (m & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}

@@ -244,7 +244,7 @@ static int orthogonalize_lanczos_r(ed_eps* e, int j, int k, double beta_prev, do
         r2 = ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr);
       ED_TRY(r2);
     }
-    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, wmax));
+    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, wmax, e->restart_mode));
     for (int i = 0; i <= j; ++i) h[i] += c[i];
     *nw = std::sqrt(n2);
     if (n0 < 0.0) {
@@ -270,7 +270,7 @@ static int orthogonalize_r(ed_eps* e, int j, double* nw) {
   for (int pass = 0; pass < 2; ++pass) {
     if (pass == 1)
       ED_TRY(ed_multidot_r(ctx, cols.data(), j + 1, e->w_r, n, nullptr, 0.0, nullptr, 0.0, c.data(), nullptr));
-    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2));
+    ED_TRY(ed_update_r(ctx, cols.data(), j + 1, c.data(), e->w_r, n, &n2, nullptr, e->restart_mode));
     *nw = std::sqrt(n2);
     if (*nw >= 0.7071067811865476 * n0) break;
     n0 = *nw;
@@ -590,7 +590,8 @@ int ed_eps_set_seed(ed_eps* e, uint64_t seed) {
 
 int ed_eps_set_restart_arithmetic(ed_eps* e, int mode) {
   if (!e) return ed_fail(ED_EINVAL, "null solver");
-  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR && mode != ED_RESTART_EXACT)
+  if (mode != ED_RESTART_AUTO && mode != ED_RESTART_FP64 && mode != ED_RESTART_PAIR && mode != ED_RESTART_EXACT &&
+      mode != ED_RESTART_FIXED)
     return ed_fail(ED_EINVAL, "unknown restart arithmetic");
   e->restart_arith = mode;
   return ED_OK;

@@ -242,8 +242,11 @@ int ed_multidot_r(ed_ctx* ctx, const double* const* cols, int nv, double* w, int
                   const double* vjm1, double b, double* h_host, double* wnorm2_host);
 // wmax_host (nullable): max_r |w_r| after the update with its low 32 bits
 // cleared (see ed_fx64_emax_scaled).
+// arith: ED_RESTART_FIXED forms sum_i V_i h_i on the integer units (exact
+// products of 56-bit fixed-point inputs, one rounding per row), otherwise
+// FP64 FMAs.
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
-                double* wnorm2_host, double* wmax_host = nullptr);
+                double* wnorm2_host, double* wmax_host = nullptr, int arith = ED_RESTART_FP64);
 int ed_scale_copy_r(ed_ctx* ctx, const double* src, double* dst, double s, int64_t n);
 // arith: ED_RESTART_FP64 (FP64 FMA beside exact integer products),
 // ED_RESTART_PAIR (float-pair products on the FP32 units, ed_linalg.cu) or

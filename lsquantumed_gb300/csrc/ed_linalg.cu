@@ -5,6 +5,7 @@
 #include "ed_device.cuh"
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #define ED_RED_THREADS 256
 #define ED_GROUP 8
@@ -610,17 +611,42 @@ __global__ void __launch_bounds__(ED_RED_THREADS) k_update_r(const ColPtrsR cp, 
 }
 
 
+template <int MAXM>
+struct UpdLimbs;
+template <int MAXM>
+__global__ void k_update_fx(const ColPtrsR cp, int nv, const __grid_constant__ UpdLimbs<MAXM> H,
+                            double* __restrict__ w, int64_t n, double* __restrict__ partial, int with_max);
+template <int MAXM>
+static int update_fx_launch(ed_ctx* ctx, const ColPtrsR& cp, int nv, const double* h_host, double* w, int64_t n,
+                            int nblk, int with_max);
+
 int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_host, double* w, int64_t n,
-                double* wnorm2_host, double* wmax_host) {
+                double* wnorm2_host, double* wmax_host, int arith) {
   if (nv > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
-  const int nblk = red_blocks(ctx, n);
+  const bool fx = arith == ED_RESTART_FIXED && nv <= 32;
+  int nblk = red_blocks(ctx, n);
+  if (fx) {  // one full wave of the register-heavier integer kernel
+    int per_sm = 0;
+    if (nv <= 16) ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_update_fx<16>, ED_RED_THREADS, 0));
+    else ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_update_fx<32>, ED_RED_THREADS, 0));
+    const int64_t b = (n + ED_RED_THREADS - 1) / ED_RED_THREADS;
+    nblk = (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->num_sms * std::max(1, per_sm)));
+  }
   const int items = wmax_host ? 2 : 1;
   ED_TRY(ed_ensure_reduce(ctx, (size_t)items * nblk + 4 + 128));
   double* h_dev = ctx->d_red + (size_t)items * nblk + 2;
   ED_CUDA(cudaMemcpyAsync(h_dev, h_host, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
   ColPtrsR cp = make_cols_r(cols, nv);
-  k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, wmax_host ? 1 : 0);
-  ED_CHECK_LAUNCH(ctx);
+  int rc = ED_ENOTSUP;
+  if (fx)
+    rc = nv <= 16 ? update_fx_launch<16>(ctx, cp, nv, h_host, w, n, nblk, wmax_host ? 1 : 0)
+                  : update_fx_launch<32>(ctx, cp, nv, h_host, w, n, nblk, wmax_host ? 1 : 0);
+  if (rc == ED_ENOTSUP) {
+    k_update_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, wmax_host ? 1 : 0);
+    ED_CHECK_LAUNCH(ctx);
+  } else {
+    ED_TRY(rc);
+  }
   double out[2];
   ED_TRY(ed_finish_reduce(ctx, items, nblk, out, items - 1));
   if (wnorm2_host) *wnorm2_host = out[0];
@@ -718,6 +744,223 @@ __global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, c
   }
 }
 
+// ---------------------------------------------------------------------------
+// Restart combination on the integer units (ED_RESTART_FIXED).  Row r of
+// output c is sum_i V_i[r] Y[i][c].  Each row's m entries are put in 56-bit
+// fixed point against the row's largest exponent E (q = round(v 2^(1078 - E)),
+// |q| <= 2^56), each coefficient column against its own (y = round(Y 2^(56 -
+// F_c))), and both are split into 28-bit limbs, q = qh 2^28 + ql with
+// ql in [0, 2^28).  The products are then exact sums of four 32 x 32 -> 64
+// bit multiply-adds (mad.wide.s32, full rate on the integer pipe, against
+// 1/64 rate for FP64 on this part); with m <= 32 none of the three partial
+// sums can overflow 64 bits.  The exact 118-bit row sum is rounded once to
+// FP64.  Error: half a unit of each fixed-point input, below 2^-51 of
+// max_i |V_i[r]| * max_i |Y[i][c]| per output (an FP64 FMA chain over 16
+// terms is bounded by 2^-49 of the same product).
+// ---------------------------------------------------------------------------
+template <int MAXM>
+struct RsLimbs {
+  int yh[MAXM * 8];  // [i][c]
+  int yl[MAXM * 8];
+  int z[8];  // output c = T 2^(E - 1078 + z[c])
+};
+
+__device__ __forceinline__ long long ed_mad_wide(int a, int b, long long c) {
+  long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+
+// round(v 2^(1078 - E)) for a row whose largest biased exponent is E
+// (|result| <= 2^56); 0 for zeros and subnormals.
+__device__ __forceinline__ long long ed_fx56_row(double v, int E) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return 0;
+  const unsigned long long mant = (unsigned long long)(b & 0xFFFFFFFFFFFFFll) | 0x10000000000000ull;
+  const int sh = e - E + 3;  // <= 3
+  unsigned long long q;
+  if (sh >= 0) q = mant << sh;
+  else if (sh > -60) q = (mant + (1ull << (-sh - 1))) >> (-sh);
+  else q = 0ull;
+  return b < 0 ? -(long long)q : (long long)q;
+}
+
+template <int MAXM>
+__global__ void __launch_bounds__(256, 2) k_restart_fx(const ColPtrsR cp, int m, int c0, int nc,
+                                                       const __grid_constant__ RsLimbs<MAXM> Y, const ColPtrs outp,
+                                                       int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    double v[MAXM];
+    int E = 0;
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) {
+      v[i] = i < m ? cp.p[i][r] : 0.0;
+      E = max(E, (int)((__double_as_longlong(v[i]) >> 52) & 0x7FF));
+    }
+    long long s1[8], s2[8], s3[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s1[c] = s2[c] = s3[c] = 0ll;
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) {
+      if (i < m) {
+        const long long q = ed_fx56_row(v[i], E);
+        const int qh = (int)(q >> 28), ql = (int)(q & 0xFFFFFFFll);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          s1[c] = ed_mad_wide(qh, Y.yh[i * 8 + c], s1[c]);
+          s2[c] = ed_mad_wide(qh, Y.yl[i * 8 + c], s2[c]);
+          s2[c] = ed_mad_wide(ql, Y.yh[i * 8 + c], s2[c]);
+          s3[c] = ed_mad_wide(ql, Y.yl[i * 8 + c], s3[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (c < nc) {
+        // T = s1 2^56 + s2 2^28 + s3 as a signed 128-bit (hi, lo)
+        unsigned long long lo = (unsigned long long)s3[c];
+        long long hi = s3[c] >> 63;
+        unsigned long long a = (unsigned long long)s2[c] << 28, x = lo + a;
+        hi += (s2[c] >> 36) + (x < lo ? 1ll : 0ll);
+        lo = x;
+        a = (unsigned long long)s1[c] << 56;
+        x = lo + a;
+        hi += (s1[c] >> 8) + (x < lo ? 1ll : 0ll);
+        lo = x;
+        double d = ed_fx128_to_double(hi, lo, E - 1078 + Y.z[c]);
+        if (E == 0x7FF) d = __longlong_as_double(0x7FF8000000000000ll);
+        ((double*)outp.p[c0 + c])[r] = d;
+      }
+    }
+  }
+}
+
+template <int MAXM>
+static int restart_fx_launch(ed_ctx* ctx, const ColPtrsR& cp, int m, const double* Y, int ldY, int l,
+                             const ColPtrs& op, int64_t n) {
+  int per_sm = 0;
+  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_fx<MAXM>, 256, 0));
+  if (per_sm < 1) per_sm = 1;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
+  for (int g0 = 0; g0 < l; g0 += 8) {
+    const int nc = std::min(8, l - g0);
+    RsLimbs<MAXM> P;
+    std::memset(&P, 0, sizeof(P));
+    for (int c = 0; c < nc; ++c) {
+      double mx = 0.0;
+      for (int i = 0; i < m; ++i) {
+        const double y = Y[(size_t)i * ldY + g0 + c];
+        if (!std::isfinite(y)) return ed_fail(ED_EINVAL, "non-finite restart coefficient");
+        mx = std::max(mx, std::fabs(y));
+      }
+      int F = 0;
+      if (mx > 0.0) std::frexp(mx, &F);  // mx < 2^F
+      P.z[c] = F - 56;
+      for (int i = 0; i < m; ++i) {
+        const long long y = std::llround(std::ldexp(Y[(size_t)i * ldY + g0 + c], 56 - F));  // |y| <= 2^56
+        P.yh[i * 8 + c] = (int)(y >> 28);
+        P.yl[i * 8 + c] = (int)(y & 0xFFFFFFFll);
+      }
+    }
+    k_restart_fx<MAXM><<<g, 256, 0, ctx->stream>>>(cp, m, g0, nc, P, op, n);
+    ED_CHECK_LAUNCH(ctx);
+  }
+  return ED_OK;
+}
+
+// w <- w - sum_i V_i h_i on the integer units (ED_RESTART_FIXED): row r's
+// entries V_i[r] in 56-bit fixed point against the row's largest exponent,
+// h in 56-bit fixed point against max|h_i|, exact products of 28-bit limbs,
+// the row's sum rounded once to FP64 and subtracted (one FP64 add per row
+// instead of nv FP64 FMAs).  Partial ||w||^2 and the high word of max |w|
+// as k_update_r.
+template <int MAXM>
+struct UpdLimbs {
+  int hh[MAXM];
+  int hl[MAXM];
+  int z;  // sum = T 2^(E - 1078 + z)
+};
+
+template <int MAXM>
+__global__ void __launch_bounds__(ED_RED_THREADS) k_update_fx(const ColPtrsR cp, int nv,
+                                                              const __grid_constant__ UpdLimbs<MAXM> H,
+                                                              double* __restrict__ w, int64_t n,
+                                                              double* __restrict__ partial, int with_max) {
+  double acc[1] = {0.0};
+  unsigned int amax = 0u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    double v[MAXM];
+    int E = 0;
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) {
+      v[i] = i < nv ? cp.p[i][r] : 0.0;
+      E = max(E, (int)((__double_as_longlong(v[i]) >> 52) & 0x7FF));
+    }
+    long long s1 = 0, s2 = 0, s3 = 0;
+#pragma unroll
+    for (int i = 0; i < MAXM; ++i) {
+      if (i < nv) {
+        const long long q = ed_fx56_row(v[i], E);
+        const int qh = (int)(q >> 28), ql = (int)(q & 0xFFFFFFFll);
+        s1 = ed_mad_wide(qh, H.hh[i], s1);
+        s2 = ed_mad_wide(qh, H.hl[i], s2);
+        s2 = ed_mad_wide(ql, H.hh[i], s2);
+        s3 = ed_mad_wide(ql, H.hl[i], s3);
+      }
+    }
+    unsigned long long lo = (unsigned long long)s3;
+    long long hi = s3 >> 63;
+    unsigned long long a = (unsigned long long)s2 << 28, x = lo + a;
+    hi += (s2 >> 36) + (x < lo ? 1ll : 0ll);
+    lo = x;
+    a = (unsigned long long)s1 << 56;
+    x = lo + a;
+    hi += (s1 >> 8) + (x < lo ? 1ll : 0ll);
+    lo = x;
+    double d = ed_fx128_to_double(hi, lo, E - 1078 + H.z);
+    if (E == 0x7FF) d = __longlong_as_double(0x7FF8000000000000ll);
+    const double wv = w[r] - d;
+    w[r] = wv;
+    acc[0] = fma(wv, wv, acc[0]);
+    if (with_max) amax = ed_absmax_hi(amax, wv);
+  }
+  __shared__ double shr[32];
+  ed_block_reduce<1>(acc, shr);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
+  if (with_max) {
+    __syncthreads();  // shr reused
+    double am = ed_absmax_hi_value(amax);
+    ed_block_max(am, shr);
+    if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = am;
+  }
+}
+
+template <int MAXM>
+static int update_fx_launch(ed_ctx* ctx, const ColPtrsR& cp, int nv, const double* h_host, double* w, int64_t n,
+                            int nblk, int with_max) {
+  UpdLimbs<MAXM> P;
+  std::memset(&P, 0, sizeof(P));
+  double mx = 0.0;
+  for (int i = 0; i < nv; ++i) {
+    if (!std::isfinite(h_host[i])) return ED_ENOTSUP;  // the FP64 form propagates it
+    mx = std::max(mx, std::fabs(h_host[i]));
+  }
+  int F = 0;
+  if (mx > 0.0) std::frexp(mx, &F);  // mx < 2^F
+  P.z = F - 56;
+  for (int i = 0; i < nv; ++i) {
+    const long long y = std::llround(std::ldexp(h_host[i], 56 - F));  // |y| <= 2^56
+    P.hh[i] = (int)(y >> 28);
+    P.hl[i] = (int)(y & 0xFFFFFFFll);
+  }
+  k_update_fx<MAXM><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, P, w, n, ctx->d_red, with_max);
+  ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
 int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const double* Y, int ldY, int l,
                          double* const* out, int64_t n, int arith) {
   if (m > 127) return ed_fail(ED_ENOTSUP, "at most 127 basis vectors");
@@ -727,6 +970,10 @@ int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const do
   ColPtrs op;
   for (int i = 0; i < 128; ++i) op.p[i] = nullptr;
   for (int i = 0; i < l && i < 128; ++i) op.p[i] = (const double2*)out[i];
+  if (arith == ED_RESTART_FIXED && m <= 32) {
+    if (m <= 16) return restart_fx_launch<16>(ctx, cp, m, Y, ldY, l, op, n);
+    return restart_fx_launch<32>(ctx, cp, m, Y, ldY, l, op, n);
+  }
   const int ngroups = (l + 7) / 8;
   const size_t per = (size_t)m * 8;
   if (pair) {

@@ -37,6 +37,7 @@
 // waits (again bounded) for its own MMAs, frees its TMEM and returns; the
 // host turns the flag into ED_ECUDA.
 #include "ed_internal.h"
+#include "ed_device.cuh"
 #include <cuda_fp16.h>
 #include <algorithm>
 #include <cmath>
@@ -99,49 +100,6 @@ __device__ __forceinline__ uint32_t slice_pair(uint32_t w, uint32_t sel, __half2
   asm("prmt.b32 %0, %1, %2, %3;" : "=r"(x) : "r"(w), "r"(0x64646464u), "r"(sel));
   __half2 h = __hfma2(*reinterpret_cast<__half2*>(&x), sgn, off);
   return *reinterpret_cast<uint32_t*>(&h);
-}
-
-// 128-bit signed T times 2^X, rounded to nearest even, as an FP64 value,
-// with integer operations only.  Results below 2^-1022 flush to zero.
-__device__ __forceinline__ double fx128_to_double(long long hi, unsigned long long lo, int X) {
-  const bool neg = hi < 0;
-  if (neg) {
-    lo = ~lo + 1ull;
-    hi = ~hi + (lo == 0ull ? 1ll : 0ll);
-  }
-  const unsigned long long uh = (unsigned long long)hi;
-  if (uh == 0ull && lo == 0ull) return 0.0;
-  const int L = uh ? 128 - __clzll((long long)uh) : 64 - __clzll((long long)lo);  // bit length
-  unsigned long long m;
-  int bexp = X + L + 1022;
-  if (L <= 53) {
-    m = lo << (53 - L);
-  } else {
-    const int sr = L - 53;  // 1 .. 75
-    unsigned long long rem, half;
-    if (sr < 64) {
-      m = (lo >> sr) | (sr ? (uh << (64 - sr)) : 0ull);
-      rem = lo & ((1ull << sr) - 1ull);
-      half = 1ull << (sr - 1);
-      const bool up = rem > half || (rem == half && (m & 1ull));
-      m += up ? 1ull : 0ull;
-    } else {
-      const int s2 = sr - 64;
-      m = uh >> s2;
-      const unsigned long long remh = uh & ((s2 ? (1ull << s2) : 1ull) - 1ull);
-      const bool gt = s2 ? (remh > (1ull << (s2 - 1)) || (remh == (1ull << (s2 - 1)) && lo != 0ull)) : (lo > (1ull << 63));
-      const bool eq = s2 ? (remh == (1ull << (s2 - 1)) && lo == 0ull) : (lo == (1ull << 63));
-      m += (gt || (eq && (m & 1ull))) ? 1ull : 0ull;
-    }
-    if (m >> 53) {
-      m >>= 1;
-      ++bexp;
-    }
-  }
-  if (bexp <= 0) return 0.0;
-  const unsigned long long bits =
-      ((unsigned long long)neg << 63) | ((unsigned long long)bexp << 52) | (m & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
 }
 
 // q = round(|v| 2^(63 - P)) for a tile whose largest biased exponent is E
@@ -373,7 +331,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_restart_tc(const TcCols cols, in
             unsigned long long lo = (unsigned long long)Ah[c] << 40;
             const unsigned long long lo2 = lo + (unsigned long long)Bl[c];
             hi += (Bl[c] >> 63) + (lo2 < lo ? 1ll : 0ll);
-            double x = fx128_to_double(hi, lo2, P + out.F[c] - 78);
+            double x = ed_fx128_to_double(hi, lo2, P + out.F[c] - 78);
             if (bad) x = __longlong_as_double(0x7FF8000000000000ll);
             out.p[c][row] = x;
           }

@@ -46,7 +46,7 @@ def as_device_vector(x, n=None):
 
 def restart_code(mode):
     m = {'auto': capi.ED_RESTART_AUTO, 'fp64': capi.ED_RESTART_FP64, 'pair': capi.ED_RESTART_PAIR,
-         'exact': capi.ED_RESTART_EXACT}.get(mode)
+         'exact': capi.ED_RESTART_EXACT, 'fixed': capi.ED_RESTART_FIXED}.get(mode)
     if m is None:
         raise InvalidArgument(capi.ED_EINVAL, 'unknown restart arithmetic %r' % (mode,))
     return m
@@ -480,8 +480,9 @@ class EPS:
         """Products of the restart combination V Y in a real-storage solve:
         'fp64', 'pair' (float pairs on the FP32 units, storage and sums FP64;
         below FP64 accuracy), 'exact' (exact slices on the tensor cores for
-        the restart and the Gram-Schmidt projections, ncv <= 32) or 'auto'
-        (fp64)."""
+        the restart and the Gram-Schmidt projections, ncv <= 32), 'fixed'
+        (the restart on the integer units: 56-bit fixed point per row and
+        column, exact products, one rounding) or 'auto'."""
         call('ed_eps_set_restart_arithmetic', self._h, restart_code(mode))
 
     def set_initial_vector(self, v):
