@@ -155,12 +155,14 @@ __global__ void k_batch_quantize_r(const double* __restrict__ x, int64_t n, cons
 }
 
 // Batched H.v over a [dim][B] block.  A CTA takes a tile of BH_ROWS rows:
-// first its threads resolve every (row, bond) pair of the tile at once (the
-// antiparallel test and the two-table rank of the flipped state, written to
-// shared memory; non-flippable pairs get an invalid target), then each
-// thread owns realisation columns b and gathers the B contiguous values of
-// every target row, four bonds at a time so several loads are in flight.
-// Exact int64 sums of the fixed-point input per coupling type, rounded once.
+// first one warp per row resolves the row's bonds (the antiparallel test and
+// the two-table rank of the flipped state) and writes only the flipping
+// ones to shared memory, compacted with warp ballots: first-type targets
+// from the front of the row's list, second-type ones from the back.  Then
+// each thread owns realisation columns b and gathers the B contiguous values
+// of every listed target, four at a time so several loads are in flight,
+// with no test or select per bond.  Exact int64 sums of the fixed-point
+// input per coupling type, rounded once.
 #define BH_ROWS 8
 #define BH_NONE 0xFFFFFFFFu
 
@@ -198,60 +200,78 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
   const long long kNaN = (long long)0x8000000000000000ull;
   const uint32_t low = (1u << w0) - 1u;
   const int nb = bb.nb;
+  __shared__ int cnt[BH_ROWS][2];  // flipping bonds of each type in the tile's rows
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
   for (int64_t r0 = (int64_t)blockIdx.x * BH_ROWS; r0 < dim; r0 += (int64_t)gridDim.x * BH_ROWS) {
     __syncthreads();  // t0s ready / previous tile's targets consumed
-    for (int it = threadIdx.x; it < BH_ROWS * nb; it += blockDim.x) {
-      const int rr = it / nb, q = it % nb;
-      uint32_t c = BH_NONE;
-      if (r0 + rr < dim) {
-        const uint32_t s = states[r0 + rr], m = bb.mask[q], t = s & m;
-        if (t != 0u && t != m) {
-          const uint32_t f = s ^ m;
-          c = (uint32_t)t0s[f & low] + __ldg(&t1[f >> w0]);
+    for (int rr = warp; rr < BH_ROWS; rr += nwarp) {
+      uint32_t* tl = tgt + rr * nb;
+      int n0 = 0, n1 = 0;
+      const bool valid = r0 + rr < dim;
+      const uint32_t s = valid ? states[r0 + rr] : 0u;
+      for (int q0 = 0; q0 < nb; q0 += 32) {
+        const int q = q0 + lane;
+        bool on = false;
+        uint32_t c = 0u;
+        int ty = 0;
+        if (valid && q < nb) {
+          const uint32_t m = bb.mask[q], t = s & m;
+          if (t != 0u && t != m) {
+            const uint32_t f = s ^ m;
+            c = (uint32_t)t0s[f & low] + __ldg(&t1[f >> w0]);
+            on = true;
+            ty = bb.type[q];
+          }
         }
+        const unsigned b0 = __ballot_sync(0xffffffffu, on && ty == 0);
+        const unsigned b1 = __ballot_sync(0xffffffffu, on && ty != 0);
+        const unsigned below = (1u << lane) - 1u;
+        if (on && ty == 0) tl[n0 + __popc(b0 & below)] = c;
+        if (on && ty != 0) tl[nb - 1 - (n1 + __popc(b1 & below))] = c;
+        n0 += __popc(b0);
+        n1 += __popc(b1);
       }
-      tgt[it] = c;
+      if (lane == 0) {
+        cnt[rr][0] = n0;
+        cnt[rr][1] = n1;
+      }
     }
     __syncthreads();
     const int nrows = (int)(dim - r0 < BH_ROWS ? dim - r0 : BH_ROWS);
     for (int rr = 0; rr < nrows; ++rr) {
       const uint32_t* tr = tgt + rr * nb;
+      const int n0 = cnt[rr][0], n1 = cnt[rr][1];
       for (int b = threadIdx.x; b < B; b += blockDim.x) {
         long long a[4] = {0, 0, 0, 0};
         bool bad = false;
-        for (int q0 = 0; q0 < nb; q0 += 4) {
-          if (RS) {
-            long long v[4];
+        // type 0: tr[0 .. n0), accumulators a[0], a[1]; type 1: tr[nb - n1 .. nb), a[2], a[3]
+        for (int ty = 0; ty < 2; ++ty) {
+          const int qb = ty ? nb - n1 : 0, qe = ty ? nb : n0;
+          long long ar = 0, ai = 0;
+          for (int q0 = qb; q0 < qe; q0 += 4) {
+            if (RS) {
+              long long v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
-              v[u] = c != BH_NONE ? __ldg(&xqr[(size_t)c * B + b]) : 0ll;
-            }
+              for (int u = 0; u < 4; ++u) v[u] = q0 + u < qe ? __ldg(&xqr[(size_t)tr[q0 + u] * B + b]) : 0ll;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              bad |= v[u] == kNaN;
-              const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
-              // selects, not a runtime index: a[] must stay in registers
-              a[0] += t1b ? 0ll : v[u];
-              a[2] += t1b ? v[u] : 0ll;
-            }
-          } else {
-            longlong2 v[4];
+              for (int u = 0; u < 4; ++u) {
+                bad |= v[u] == kNaN;
+                ar += v[u];
+              }
+            } else {
+              longlong2 v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const uint32_t c = (q0 + u < nb) ? tr[q0 + u] : BH_NONE;
-              v[u] = c != BH_NONE ? __ldg(&xq[(size_t)c * B + b]) : make_longlong2(0, 0);
-            }
+              for (int u = 0; u < 4; ++u)
+                v[u] = q0 + u < qe ? __ldg(&xq[(size_t)tr[q0 + u] * B + b]) : make_longlong2(0, 0);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              bad |= (v[u].x == kNaN) | (v[u].y == kNaN);
-              const bool t1b = (q0 + u < nb) && bb.type[q0 + u];
-              a[0] += t1b ? 0ll : v[u].x;
-              a[1] += t1b ? 0ll : v[u].y;
-              a[2] += t1b ? v[u].x : 0ll;
-              a[3] += t1b ? v[u].y : 0ll;
+              for (int u = 0; u < 4; ++u) {
+                bad |= (v[u].x == kNaN) | (v[u].y == kNaN);
+                ar += v[u].x;
+                ai += v[u].y;
+              }
             }
           }
+          if (ty) { a[2] = ar; a[3] = ai; } else { a[0] = ar; a[1] = ai; }
         }
         const size_t k = (size_t)(r0 + rr) * B + b;
         const double d = diag[k];
