@@ -360,44 +360,58 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     """C3: disorder sweep, chain N=20 (J1=1, J2=0.2, Delta=1), h_i ~ U[-2, 2]
     from mt19937_64(seed) (RandomDisorder::hi_init with srand_seq[k] = seed),
     Sz = 0, 1, 2, lowest 2 pairs at eps_tol 1e-9.  Batched: one batch per
-    sector over all `seeds`, timed on the host around the three solves (each
-    returns its results to the host).  Plain: the same solves one at a time
+    sector over all `seeds`, the three sectors solved at once (solve_batches:
+    one environment, host thread and stream per sector), timed on the host
+    around the call; the same batches one sector after another are timed
+    beside it.  Plain: the same solves one at a time
     for `plain_sample` seeds per sector spread over the whole seed range
     (every restart tile of the batch), timed per solve, eigenvalues checked
     against the batch at 1e-8."""
     import numpy as np
     import torch
     N, J1, J2, W, nev, ncv, tol = (C3[k] for k in ('N', 'J1', 'J2', 'W', 'nev', 'ncv', 'tol'))
-    env = ed.Environment(nspins=N, device=torch.cuda.current_device())
     fields = np.stack([ed.random_fields(sd, N, -W, W) for sd in seeds])
     sectors = (0, 1, 2)
-    hams = {}
-    for mag in sectors:
+    hams, envs = {}, {}
+    for mag in sectors:  # one environment (stream) per sector: the sectors can run at once
+        env = envs[mag] = ed.Environment(nspins=N, device=torch.cuda.current_device())
         b = ed.Basis(env, mag)
         h = ed.Hamiltonian(env, b, ed.chain1D(env), J1, 1.0, J2, J2)
         h.build_diag(env)
         h.build_off_diag(env)
         hams[mag] = (b, h)
-    bt = ed.DisorderBatch(hams[0][1], fields[:8])  # warm-up on a small batch
-    bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
-    del bt
-    torch.cuda.synchronize()
-    k0 = env.kernel_count()
-    t0 = time.perf_counter()
-    max_err, its, bad = 0.0, [], 0
-    batch_evals = {}
-    for mag in sectors:
-        bt = ed.DisorderBatch(hams[mag][1], fields)
-        bt.set_restart_arithmetic(restart if restart in ('auto', 'fp64', 'pair') else 'auto')
-        r = bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
-        max_err = max(max_err, float(r['errs'].max()))
-        bad += int((r['nconv'] < nev).sum())
-        its.append(r['its'])
-        batch_evals[mag] = r['evals']
+    for mag in sectors:  # warm-up on a small batch per sector
+        bt = ed.DisorderBatch(hams[mag][1], fields[:8])
+        bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0)
         del bt
     torch.cuda.synchronize()
-    t_batch = time.perf_counter() - t0
-    launches = env.kernel_count() - k0
+    brestart = restart if restart in ('auto', 'fp64', 'pair') else 'auto'
+    kcount = lambda: sum(e.kernel_count() for e in envs.values())
+
+    def batched(concurrent):
+        bts = []
+        for mag in sectors:
+            bt = ed.DisorderBatch(hams[mag][1], fields)
+            bt.set_restart_arithmetic(brestart)
+            bts.append(bt)
+        torch.cuda.synchronize()
+        k0 = kcount()
+        t0 = time.perf_counter()
+        if concurrent:  # the three sectors at once, one host thread and stream each
+            rs = ed.solve_batches(bts, nev=nev, ncv=ncv, tol=tol, seed=0)
+        else:
+            rs = [bt.solve(nev=nev, ncv=ncv, tol=tol, seed=0) for bt in bts]
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        return t, kcount() - k0, rs, [list(bt.hv_tile()) for bt in bts]
+
+    t_seq, _, rs_seq, _ = batched(False)
+    t_batch, launches, rs, tiles = batched(True)
+    max_err = max(float(r['errs'].max()) for r in rs)
+    bad = sum(int((r['nconv'] < nev).sum()) for r in rs)
+    its = [r['its'] for r in rs]
+    batch_evals = {mag: r['evals'] for mag, r in zip(sectors, rs)}
+    same_seq = all(np.allclose(a['evals'], b['evals'], rtol=1e-12, atol=0) for a, b in zip(rs, rs_seq))
     nplain = min(plain_sample, len(seeds))
     pick = sorted(set(np.linspace(0, len(seeds) - 1, nplain).round().astype(int).tolist()))
     t0 = time.perf_counter()
@@ -405,6 +419,7 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     perr = 0.0
     for mag in sectors:
         b, _ = hams[mag]
+        env = envs[mag]
         for k in pick:
             h = ed.Hamiltonian(env, b, ed.chain1D(env), J1, 1.0, J2, J2)
             h.build_diag(env)
@@ -424,8 +439,11 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     nsolve = len(seeds) * len(sectors)
     return {'batched_samples_per_s': nsolve / t_batch, 'plain_samples_per_s': 1.0 / t_plain,
             'batched_over_plain': (nsolve / t_batch) * t_plain, 'batched_seconds': t_batch, 'solves': nsolve,
+            'sectors_at_once': True, 'batched_one_sector_at_a_time_samples_per_s': nsolve / t_seq,
+            'eigenvalues_agree_with_one_sector_at_a_time_1e-12': bool(same_seq),
             'max_rel_residual': max_err, 'plain_max_rel_residual': perr, 'unconverged': bad,
             'restarts_per_sector': its, 'gpu_launches': launches, 'restart_arithmetic': restart,
+            'hv_tile_per_sector': tiles,
             'plain_sample': '%d seeds per sector (indices %s), one solve at a time' % (len(pick), pick),
             'eigenvalues_agree_1e-8': bool(agree), 'fields': fields, 'batch_evals': batch_evals,
             'config': 'chain1D N=20 J1=1 J2=0.2 Delta=1, h_i~U[-2,2] seeds %d..%d, Sz=0,1,2, nev=2, ncv=16, '

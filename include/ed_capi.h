@@ -295,6 +295,25 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
 /* Eigenvector i of realisation b into a contiguous device vector. */
 int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev);
 int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv);
+/* Several batched sweeps at once (e.g. the Sz sectors of one disorder
+ * sweep): bts[i] is solved as by ed_batch_solve into evals_host[i] /
+ * errs_host[i] / nconv_host[i], each on its own host thread.  Every batch
+ * must belong to a different environment (its own stream), so that the
+ * device overlaps them.  Returns the first error, prefixed with the batch's
+ * index.  No counterpart in the reference (its sectors run one after
+ * another). */
+int ed_batch_solve_many(ed_batch* const* bts, int count, int nev, int ncv, double tol, int max_it, uint64_t seed,
+                        double* const* evals_host, double* const* errs_host, int* const* nconv_host);
+/* Tile of the batched H.v: rows of the basis per CTA tile (4, 8, 16, 32)
+ * and threads per CTA (128, 256; the realisation columns are spread over
+ * them).  (0, 0) re-enables the autotuner, which times every tile once at the
+ * batch's first real-storage H.v and keeps the fastest.  All tiles give
+ * bit-identical H.v results; the x^T y and ||y||^2 fused into the solve's
+ * H.v are summed per tile, so a solve's last bits can depend on the tile.
+ * No counterpart in the reference. */
+int ed_batch_set_hv_tile(ed_batch* bt, int rows, int threads);
+/* The tile in use ((0, 0) before the autotuner has run). */
+int ed_batch_hv_tile(const ed_batch* bt, int* rows, int* threads);
 /* Products of the restart combination, as ed_eps_set_restart_arithmetic. */
 int ed_batch_set_restart_arithmetic(ed_batch* bt, int mode);
 

@@ -8,7 +8,8 @@ from . import capi  # noqa: F401
 from .capi import EDError, InvalidArgument  # noqa: F401
 from .ed import (AF, Adjoint, DSF_data, EPS, DisorderBatch, PETSC_DECIDE, PETSC_DEFAULT, Basis, Environment, Hamiltonian,  # noqa: F401
                  Phys, RandomDisorder, SiSj, SmSp, Solver, SpSm, Striped, SzSz, chain1D, honeycomb2D,
-                 bv_dot_real, bv_mult_real, ground_state_energy, random_fields, random_normal, square2D)
+                 bv_dot_real, bv_mult_real, ground_state_energy, random_fields, random_normal, solve_batches,
+                 square2D)
 
 
 def build(force=False):

@@ -88,6 +88,8 @@ SIGNATURES = {
     'ed_bv_mult_real': [vp, vp, i32, vp, i32, i32, vp, i64, i32],
     'ed_bv_dot_real': [vp, vp, i32, vp, i64, i32, vp],
     'ed_batch_set_restart_arithmetic': [vp, i32],
+    'ed_batch_set_hv_tile': [vp, i32, i32],
+    'ed_batch_hv_tile': [vp, P(i32), P(i32)],
     'ed_eps_set_initial_vector': [vp, vp, i32],
     'ed_eps_solve': [vp, P(i32)],
     'ed_eps_get_eigenpair': [vp, i32, P(dbl), P(dbl), vp],
@@ -99,6 +101,7 @@ SIGNATURES = {
     'ed_batch_apply': [vp, vp, vp],
     'ed_batch_diag_host': [vp, vp],
     'ed_batch_solve': [vp, i32, i32, dbl, i32, u64, vp, vp, vp],
+    'ed_batch_solve_many': [vp, i32, i32, i32, dbl, i32, u64, vp, vp, vp],
     'ed_batch_get_eigenvector': [vp, i32, i32, vp],
     'ed_batch_stats': [vp, P(i32), P(i64)],
     'ed_expect_pairs': [vp, i32, vp, vp, i64, vp],

@@ -11,8 +11,10 @@
 #include "ed_internal.h"
 #include "ed_device.cuh"
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 struct ed_batch {
@@ -36,6 +38,8 @@ struct ed_batch {
   // (k_batch_scale_quantize); the next batched H.v of it uses them once
   const void* xq_src = nullptr;
   int xq_b = 0;
+  int hv_variant = -1;  // batched H.v launch variant (-1: autotune at the next real-storage H.v)
+  bool hv_forced = false;
 };
 
 // Per-realisation diagonal, exactly as build_disorder computes it:
@@ -163,8 +167,12 @@ __global__ void k_batch_quantize_r(const double* __restrict__ x, int64_t n, cons
 // of every listed target, four at a time so several loads are in flight,
 // with no test or select per bond.  Exact int64 sums of the fixed-point
 // input per coupling type, rounded once.
-#define BH_ROWS 8
 #define BH_NONE 0xFFFFFFFFu
+// launch variants of the batched H.v: rows per tile x threads per block (the
+// autotuner times each once per batch; all give bit-identical results)
+static const int kBhRows[4] = {4, 8, 16, 32};
+static const int kBhThreads[2] = {128, 256};
+static const int kBhVariants = 8;  // v: rows kBhRows[v / 2], threads kBhThreads[v % 2]
 
 struct BatchBonds {
   int nb;
@@ -174,7 +182,7 @@ struct BatchBonds {
 
 // RS: real storage (x, y double[dim][B], fixed-point copy int64[dim][B]);
 // else complex128 blocks with (re, im) fixed-point pairs.
-template <bool RS>
+template <bool RS, int BH_ROWS>
 __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ states, const double* __restrict__ diag,
                                                   const void* __restrict__ xv_, const void* __restrict__ xq_,
                                                   const int* __restrict__ gmax_p, int sbits, void* __restrict__ y_,
@@ -712,32 +720,88 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
     bb.type[bb.nb] = (uint8_t)(h->bs.type[q] & 1);
     ++bb.nb;
   }
-  size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)BH_ROWS * std::max(bb.nb, 1));
-  if (dot) smem = ((smem + 7) & ~(size_t)7) + sizeof(double) * 2 * (size_t)B + 8;
-  if (smem > 96 * 1024) return ed_fail(ED_ENOTSUP, "batch too wide for the batched H.v");
-  static bool attr = false;
-  if (!attr) {
-    ED_CUDA(cudaFuncSetAttribute(k_batch_hv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-    ED_CUDA(cudaFuncSetAttribute(k_batch_hv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-    attr = true;
+  // one launch of variant v; partial (real storage only): fused x^T y, ||y||^2
+  auto launch = [&](int v, double* partial, int* grid_out) -> int {
+    const int rows = kBhRows[v / 2];
+    size_t smem = sizeof(uint32_t) * ((((size_t)1 << b->lin_w0) + 1) / 2 + (size_t)rows * std::max(bb.nb, 1));
+    if (partial) smem = ((smem + 7) & ~(size_t)7) + sizeof(double) * 2 * (size_t)B + 8;
+    if (smem > 96 * 1024) return ED_ENOTSUP;
+    const int threads = std::min(kBhThreads[v % 2], ((B + 31) / 32) * 32);
+    const void* fn = nullptr;
+#define ED_BH_FN(R)                                                                  \
+  case R:                                                                            \
+    fn = rs ? (const void*)k_batch_hv<true, R> : (const void*)k_batch_hv<false, R>; \
+    break;
+    switch (rows) { ED_BH_FN(4) ED_BH_FN(8) ED_BH_FN(16) ED_BH_FN(32) }
+#undef ED_BH_FN
+    static std::atomic<bool> attr_set[2][4] = {};  // several host threads may launch (ed_batch_solve_many)
+    std::atomic<bool>& done = attr_set[rs ? 1 : 0][v / 2];
+    if (!done.load()) {
+      ED_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+      done.store(true);
+    }
+    int per_sm = 0;
+    ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int64_t tiles = (bt->dim + rows - 1) / rows;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
+    if (grid_out) *grid_out = grid;
+    if (partial) ED_TRY(batch_reduce_buf(bt, (size_t)2 * B * grid + (size_t)2 * B));
+    double* part = partial ? bt->d_red : nullptr;
+#define ED_BH_LAUNCH(R)                                                                                             \
+  case R:                                                                                                           \
+    if (rs)                                                                                                         \
+      k_batch_hv<true, R><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, \
+                                                                y, bt->dim, B, b->d_lin_t0, b->d_lin_t1,            \
+                                                                b->lin_w0, bb, h->bs.chalf[0], h->bs.chalf[1],      \
+                                                                part);                                              \
+    else                                                                                                            \
+      k_batch_hv<false, R><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax,       \
+                                                                 sbits, y, bt->dim, B, b->d_lin_t0, b->d_lin_t1,   \
+                                                                 b->lin_w0, bb, h->bs.chalf[0], h->bs.chalf[1],    \
+                                                                 nullptr);                                          \
+    break;
+    switch (rows) { ED_BH_LAUNCH(4) ED_BH_LAUNCH(8) ED_BH_LAUNCH(16) ED_BH_LAUNCH(32) }
+#undef ED_BH_LAUNCH
+    ED_CHECK_LAUNCH(ctx);
+    return ED_OK;
+  };
+  if (bt->hv_variant < 0 && rs) {
+    // time every variant once on this input (plain H.v; the result is the same
+    // for all of them) and keep the fastest for the rest of the batch's life
+    cudaEvent_t e0, e1;
+    ED_CUDA(cudaEventCreate(&e0));
+    ED_CUDA(cudaEventCreate(&e1));
+    float best = 0.0f;
+    bool have = false;
+    int vbest = 3;  // 8 rows x 256 threads
+    for (int v = 0; v < kBhVariants; ++v) {
+      int r = launch(v, nullptr, nullptr);  // warm-up (and the T0 fill of a new shape)
+      if (r == ED_ENOTSUP) continue;
+      ED_TRY(r);
+      ED_CUDA(cudaEventRecord(e0, ctx->stream));
+      ED_TRY(launch(v, nullptr, nullptr));
+      ED_CUDA(cudaEventRecord(e1, ctx->stream));
+      ED_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (!have || ms < best) {
+        have = true;
+        best = ms;
+        vbest = v;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    bt->hv_variant = vbest;
   }
-  int per_sm = 0;
-  const int threads = std::min(256, ((B + 31) / 32) * 32);
-  if (rs) ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<true>, threads, smem));
-  else ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_hv<false>, threads, smem));
-  if (per_sm < 1) per_sm = 1;
-  const int64_t tiles = (bt->dim + BH_ROWS - 1) / BH_ROWS;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)ctx->num_sms * per_sm));
-  if (dot) ED_TRY(batch_reduce_buf(bt, (size_t)2 * B * grid + (size_t)2 * B));
-  if (rs)
-    k_batch_hv<true><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y, bt->dim,
-                                                           B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb, h->bs.chalf[0],
-                                                           h->bs.chalf[1], dot ? bt->d_red : nullptr);
-  else
-    k_batch_hv<false><<<grid, threads, smem, ctx->stream>>>(b->d_states, diag, x, bt->d_xq, bt->d_gmax, sbits, y,
-                                                            bt->dim, B, b->d_lin_t0, b->d_lin_t1, b->lin_w0, bb,
-                                                            h->bs.chalf[0], h->bs.chalf[1], nullptr);
-  ED_CHECK_LAUNCH(ctx);
+  const int v = bt->hv_variant < 0 ? 3 : bt->hv_variant;
+  int grid = 0;
+  {
+    const int r = launch(v, dot ? bt->d_red : nullptr, &grid);
+    if (r == ED_ENOTSUP) return ed_fail(ED_ENOTSUP, "batch too wide for the batched H.v");
+    ED_TRY(r);
+  }
   if (dot) {
     const int64_t items = 2 * (int64_t)B;
     double* res = bt->d_red + (size_t)items * grid;
@@ -1188,6 +1252,42 @@ cleanup:
   return rc;
 }
 
+int ed_batch_solve_many(ed_batch* const* bts, int count, int nev, int ncv, double tol, int max_it, uint64_t seed,
+                        double* const* evals_host, double* const* errs_host, int* const* nconv_host) {
+  if (!bts || count < 1 || !evals_host || !errs_host || !nconv_host) return ed_fail(ED_EINVAL, "null argument");
+  for (int i = 0; i < count; ++i) {
+    if (!bts[i] || !evals_host[i] || !errs_host[i] || !nconv_host[i]) return ed_fail(ED_EINVAL, "null argument");
+    for (int j = 0; j < i; ++j)
+      if (bts[j]->h->ctx == bts[i]->h->ctx)
+        return ed_fail(ED_EINVAL, "each batch of ed_batch_solve_many needs its own environment (stream)");
+  }
+  // one host thread per batch; every batch issues to its own context's
+  // stream, so the device overlaps them (the gathers of one sector's H.v on
+  // the L1 path beside another's FP64-bound Gram-Schmidt)
+  std::vector<int> rc(count, ED_OK);
+  std::vector<std::string> msg(count);
+  auto run = [&](int i) {
+    ed_batch* bt = bts[i];
+    if (cudaSetDevice(bt->h->ctx->device) != cudaSuccess) {
+      rc[i] = ed_cuda_fail(cudaGetLastError(), "cudaSetDevice", __FILE__, __LINE__);
+    } else {
+      rc[i] = ed_batch_solve(bt, nev, ncv, tol, max_it, seed, evals_host[i], errs_host[i], nconv_host[i]);
+    }
+    if (rc[i] != ED_OK) {
+      char buf[512];
+      ed_last_error(buf, sizeof(buf));
+      msg[i] = buf;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int i = 1; i < count; ++i) th.emplace_back(run, i);
+  run(0);
+  for (auto& t : th) t.join();
+  for (int i = 0; i < count; ++i)
+    if (rc[i] != ED_OK) return ed_fail(rc[i], "batch " + std::to_string(i) + ": " + msg[i]);
+  return ED_OK;
+}
+
 int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev) {
   if (!bt || !vec_dev) return ed_fail(ED_EINVAL, "null argument");
   if (!bt->d_vecs || i < 0 || i >= bt->nrep || b < 0 || b >= bt->B) return ed_fail(ED_EINVAL, "index out of range");
@@ -1195,6 +1295,29 @@ int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev) {
   k_batch_extract<<<grid_n(ctx, bt->dim), 256, 0, ctx->stream>>>(bt->d_vecs + (size_t)i * bt->dim * bt->B, bt->dim,
                                                                 bt->B, b, (double2*)vec_dev);
   ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+int ed_batch_set_hv_tile(ed_batch* bt, int rows, int threads) {
+  if (!bt) return ed_fail(ED_EINVAL, "null batch");
+  if (rows == 0 && threads == 0) {
+    bt->hv_variant = -1;
+    bt->hv_forced = false;
+    return ED_OK;
+  }
+  for (int v = 0; v < kBhVariants; ++v)
+    if (kBhRows[v / 2] == rows && kBhThreads[v % 2] == threads) {
+      bt->hv_variant = v;
+      bt->hv_forced = true;
+      return ED_OK;
+    }
+  return ed_fail(ED_EINVAL, "unknown batched H.v tile (rows 4/8/16/32, threads 128/256)");
+}
+
+int ed_batch_hv_tile(const ed_batch* bt, int* rows, int* threads) {
+  if (!bt || !rows || !threads) return ed_fail(ED_EINVAL, "null argument");
+  *rows = bt->hv_variant < 0 ? 0 : kBhRows[bt->hv_variant / 2];
+  *threads = bt->hv_variant < 0 ? 0 : kBhThreads[bt->hv_variant % 2];
   return ED_OK;
 }
 

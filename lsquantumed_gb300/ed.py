@@ -612,6 +612,18 @@ class DisorderBatch:
             raise InvalidArgument(capi.ED_EINVAL, "the batched sweep has no 'exact' restart")
         call('ed_batch_set_restart_arithmetic', self._h, restart_code(mode))
 
+    def set_hv_tile(self, rows, threads):
+        """Force the batched H.v tile: rows per CTA tile (4, 8, 16, 32) and
+        threads per CTA (128, 256); (0, 0) re-enables the autotuner."""
+        call('ed_batch_set_hv_tile', self._h, int(rows), int(threads))
+
+    def hv_tile(self):
+        """(rows, threads) of the batched H.v tile in use; (0, 0) before the
+        autotuner has run."""
+        r, t = ctypes.c_int32(), ctypes.c_int32()
+        call('ed_batch_hv_tile', self._h, ctypes.byref(r), ctypes.byref(t))
+        return r.value, t.value
+
     def solve(self, nev=1, ncv=0, tol=1e-8, max_it=0, seed=0):
         ev = np.zeros((self.B, nev))
         er = np.zeros((self.B, nev))
@@ -635,6 +647,28 @@ class DisorderBatch:
             except Exception:
                 pass
             self._h = None
+
+
+def solve_batches(batches, nev=1, ncv=0, tol=1e-8, max_it=0, seed=0):
+    """Solve several DisorderBatch objects at once (ed_batch_solve_many): each
+    on its own host thread and stream, so the device overlaps them.  Every
+    batch must come from a different Environment.  Returns one result dict
+    per batch, as DisorderBatch.solve."""
+    k = len(batches)
+    evs = [np.zeros((bt.B, nev)) for bt in batches]
+    ers = [np.zeros((bt.B, nev)) for bt in batches]
+    ncs = [np.zeros(bt.B, dtype=np.int32) for bt in batches]
+    hp = (ctypes.c_void_p * k)(*[bt._h for bt in batches])
+    ep = (ctypes.c_void_p * k)(*[a.ctypes.data for a in evs])
+    rp = (ctypes.c_void_p * k)(*[a.ctypes.data for a in ers])
+    np_ = (ctypes.c_void_p * k)(*[a.ctypes.data for a in ncs])
+    call('ed_batch_solve_many', hp, k, int(nev), int(ncv), float(tol), int(max_it), int(seed), ep, rp, np_)
+    out = []
+    for bt, ev, er, nc in zip(batches, evs, ers, ncs):
+        its, nhv = ctypes.c_int(), ctypes.c_int64()
+        call('ed_batch_stats', bt._h, ctypes.byref(its), ctypes.byref(nhv))
+        out.append({'evals': ev, 'errs': er, 'nconv': nc, 'its': its.value, 'nhv': nhv.value})
+    return out
 
 
 # ---------------------------------------------------------------------------
