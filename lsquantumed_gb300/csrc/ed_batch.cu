@@ -120,7 +120,9 @@ __global__ void k_batch_quantize(const double2* __restrict__ x, int64_t n, const
 }
 
 // The same two passes for the real-storage block of the batched solve.
-__global__ void k_batch_maxexp_r(const double* __restrict__ x, int64_t n, int* __restrict__ gmax) {
+__global__ void k_batch_maxexp_r(const double* __restrict__ x, int64_t n, int* __restrict__ gmax,
+                                 const int* __restrict__ skip = nullptr) {
+  if (skip && *skip) return;  // the fixed-point copy was made with x already
   int m = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
@@ -151,7 +153,8 @@ __device__ __forceinline__ long long batch_fx64_entry(double v, int emax, int sb
 }
 
 __global__ void k_batch_quantize_r(const double* __restrict__ x, int64_t n, const int* __restrict__ gmax_p, int sbits,
-                                   long long* __restrict__ xq) {
+                                   long long* __restrict__ xq, const int* __restrict__ skip = nullptr) {
+  if (skip && *skip) return;
   const int emax = *gmax_p;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
@@ -330,7 +333,8 @@ struct BCols {
 __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, double* __restrict__ w, int64_t dim,
                                                     int B, int with_norm, double* __restrict__ partial, int nblk,
                                                     const double* __restrict__ vj, const double* __restrict__ vjm1,
-                                                    const double* __restrict__ coef) {
+                                                    const double* __restrict__ coef, const int* __restrict__ pred) {
+  if (pred && *pred == 0) return;  // a pass the device decided to skip (uniform over the grid)
   __shared__ double sh[256 * (BD_MAXV + 1)];
   const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
   const int S = 256 / Bp;  // row lanes
@@ -385,7 +389,8 @@ __global__ void __launch_bounds__(256) k_batch_dots(const BCols V, int nv, doubl
 // (coalesced), a fixed shuffle tree (the same order every run).
 // Items below nsum are summed over the blocks, the others maximised.
 __global__ void k_batch_reduce(const double* __restrict__ partial, int nblk, int64_t items, double* __restrict__ out,
-                               int64_t nsum) {
+                               int64_t nsum, const int* __restrict__ pred = nullptr) {
+  if (pred && *pred == 0) return;
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t it = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
@@ -424,7 +429,9 @@ __global__ void __launch_bounds__(256) k_batch_update(const BCols V, int nv, con
 template <bool REG>
 __global__ void __launch_bounds__(256) k_batch_update_norm(const BCols V, int nv, const double* __restrict__ h,
                                                            double* __restrict__ w, int64_t dim, int B,
-                                                           double* __restrict__ partial, int nblk) {
+                                                           double* __restrict__ partial, int nblk,
+                                                           const int* __restrict__ pred = nullptr) {
+  if (pred && *pred == 0) return;
   __shared__ double sh[256], shm[256];
   const int Bp = B >= 256 ? 256 : ((B + 31) / 32) * 32;
   const int S = 256 / Bp;
@@ -513,6 +520,130 @@ __global__ void k_batch_scale_quantize(const double* __restrict__ src, double* _
     dst[k] = v;
     xq[k] = batch_fx64_entry(v, emax, sbits);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Device-side steps of the batched expansion: the per-realisation
+// coefficients (the local Lanczos pair, the Gram-Schmidt dots, the norms, the
+// refinement decision and the scale of the new vector) stay in device memory
+// between the kernels, so an expansion sweep has no host round trip; alpha
+// and beta ([b][m + 1], as on the host) go back once per restart.
+// ---------------------------------------------------------------------------
+struct BxState {
+  double* alpha;  // [B][m1]
+  double* beta;   // [B][m1]
+  double* prevn;  // [B] norm before the pass (DGKS test)
+  double* wmax;   // [B] high word of max |w[:, b]| after the last pass
+  int* again;     // any realisation needs the refinement pass
+  int* emax;      // largest exponent of the scaled block
+  int* finite;    // emax determined for every realisation
+  int* xq_valid;  // the fixed-point copy was made with the new vector
+};
+
+// res_hv[b] = v_j^T w: alpha_j and the local coefficients (a_b, beta_{j-1,b})
+__global__ void k_bx_local(const double* __restrict__ res_hv, int A, int j, int m1, int three, BxState st,
+                           double* __restrict__ coefL) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b == 0) *st.again = 0;
+  if (b >= A) return;
+  const double a = res_hv[b];
+  st.alpha[(size_t)b * m1 + j] = a;
+  coefL[b] = a;
+  coefL[A + b] = three ? st.beta[(size_t)b * m1 + j - 1] : 0.0;
+}
+
+// After an update pass: res_upd = [||w||^2 per b, high word of max |w| per b],
+// dots = [(j + 1)][A] the pass's coefficients.  The first pass's norm before
+// the update is sqrt(||w||^2 + sum_i dots_i^2) (Pythagoras against the
+// orthonormal basis).
+__global__ void k_bx_post(const double* __restrict__ res_upd, const double* __restrict__ dots, int A, int j, int m1,
+                          int first, BxState st, const int* __restrict__ pred) {
+  if (pred && *pred == 0) return;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= A) return;
+  st.alpha[(size_t)b * m1 + j] += dots[(size_t)j * A + b];
+  const double n2 = res_upd[b];
+  const double nw = sqrt(n2);
+  st.beta[(size_t)b * m1 + j] = nw;
+  double pv = st.prevn[b];
+  if (first) {
+    double s2 = n2;
+    for (int i = 0; i <= j; ++i) {
+      const double c = dots[(size_t)i * A + b];
+      s2 += c * c;
+    }
+    pv = sqrt(s2);
+  }
+  if (nw < 0.7071067811865476 * pv) atomicOr(st.again, 1);
+  st.prevn[b] = nw;
+  st.wmax[b] = res_upd[A + b];
+}
+
+// ed_fx64_emax_scaled on the device: the biased exponent of fl(max |w| * s)
+// where the high word of max |w| determines it, else -1.
+__device__ __forceinline__ int bx_emax_scaled(double absmax_hi, double s) {
+  const unsigned long long lb = (unsigned long long)__double_as_longlong(absmax_hi);
+  const double u = __longlong_as_double((long long)(lb | 0xFFFFFFFFull));
+  const double ml = absmax_hi * s, mu = u * s;
+  if (!isfinite(ml) || !isfinite(mu) || !(s > 0.0)) return -1;
+  const int el = (int)(((unsigned long long)__double_as_longlong(ml) >> 52) & 0x7FF);
+  const int eu = (int)(((unsigned long long)__double_as_longlong(mu) >> 52) & 0x7FF);
+  return el == eu ? el : -1;
+}
+
+// scale factors 1 / beta_j (0 keeps a zero column zero) and the largest
+// exponent of the scaled block; one block
+__global__ void __launch_bounds__(256) k_bx_scale(int A, int j, int m1, BxState st, double* __restrict__ sc) {
+  __shared__ int sh_e[256], sh_f[256];
+  int e = 0, f = 1;
+  for (int b = threadIdx.x; b < A; b += blockDim.x) {
+    const double nb = st.beta[(size_t)b * m1 + j];
+    const double s = nb > 1e-300 ? 1.0 / nb : 0.0;
+    sc[b] = s;
+    if (s == 0.0) continue;
+    const int eb = bx_emax_scaled(st.wmax[b], s);
+    if (eb < 0) f = 0;
+    else e = max(e, eb);
+  }
+  sh_e[threadIdx.x] = e;
+  sh_f[threadIdx.x] = f;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh_e[threadIdx.x] = max(sh_e[threadIdx.x], sh_e[threadIdx.x + o]);
+      sh_f[threadIdx.x] = min(sh_f[threadIdx.x], sh_f[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *st.emax = sh_e[0];
+    *st.finite = sh_f[0];
+  }
+}
+
+// k_batch_scale_quantize with emax and its validity from the device: where
+// the exponent is not determined, only the scaled vector is written and the
+// next batched H.v quantizes it itself.
+__global__ void k_bx_scale_quantize(const double* __restrict__ src, double* __restrict__ dst,
+                                    const double* __restrict__ s, int64_t dim, int B, int sbits,
+                                    long long* __restrict__ xq, int* __restrict__ gmax, BxState st) {
+  const int finite = *st.finite, emax = *st.emax;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (finite) gmax[0] = emax;
+    *st.xq_valid = finite;
+  }
+  const int64_t n = dim * B;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const double v = src[k] * s[k % B];
+    dst[k] = v;
+    if (finite) xq[k] = batch_fx64_entry(v, emax, sbits);
+  }
+}
+
+// before a quantization the next H.v may need: reset the exponent maximum
+__global__ void k_bx_prequant(int* __restrict__ gmax, const int* __restrict__ xq_valid) {
+  if (!*xq_valid) gmax[0] = 0;
 }
 
 // out_c[:, b] = sum_i V_i[:, b] Y[b][i][c]   (Y real, m x l per realisation),
@@ -662,7 +793,8 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
   BCols vc;
   memset(&vc, 0, sizeof(vc));
   for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
-  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk, vj, vjm1, coef);
+  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, norm ? 1 : 0, bt->d_red, nblk, vj, vjm1, coef,
+                                              nullptr);
   ED_CHECK_LAUNCH(ctx);
   double* res = bt->d_red + (size_t)items * nblk;
   k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, res, items);
@@ -670,6 +802,26 @@ static int batch_dots(ed_batch* bt, int B, const std::vector<const double*>& V, 
   ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   out.assign(bt->h_red, bt->h_red + items);
+  return ED_OK;
+}
+
+// The dots V_i^T w of a pass, reduced straight into out_dev ([nv][B], the
+// update's coefficient layout), without a host round trip; pred (device):
+// skip the pass when it reads 0.
+static int batch_dots_dev(ed_batch* bt, int B, const std::vector<const double*>& V, double* w, double* out_dev,
+                          const double* vj, const double* vjm1, const double* coef, const int* pred) {
+  ed_ctx* ctx = bt->h->ctx;
+  const int nv = (int)V.size();
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(bt->dim / 64 + 1, (int64_t)ctx->num_sms * 4));
+  const int64_t items = (int64_t)nv * B;
+  ED_TRY(batch_reduce_buf(bt, (size_t)(items + B) * nblk + (size_t)items));
+  BCols vc;
+  memset(&vc, 0, sizeof(vc));
+  for (int i = 0; i < nv && i < 64; ++i) vc.p[i] = V[i];
+  k_batch_dots<<<nblk, 256, 0, ctx->stream>>>(vc, nv, w, bt->dim, B, 0, bt->d_red, nblk, vj, vjm1, coef, pred);
+  ED_CHECK_LAUNCH(ctx);
+  k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, items, out_dev, items, pred);
+  ED_CHECK_LAUNCH(ctx);
   return ED_OK;
 }
 
@@ -686,14 +838,28 @@ static int batch_sbits(const ed_batch* bt) {
 // y = H_b x for the B (active) realisation columns of x, whose diagonals are
 // the columns of diag ([dim][B]).  rs: x, y are real storage double[dim][B]
 // (the solve), else complex128 blocks (ed_batch_apply).
+// dev (real storage only): the expansion's device state; the fixed-point copy
+// is then made here only where the previous step could not (xq_valid), and
+// with res_dev the fused x^T y / ||y||^2 stay on the device (*res_dev, in the
+// reduce buffer, valid until its next use) instead of coming back to *dot.
 static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void* y, bool rs,
-                    std::vector<double>* dot = nullptr) {
+                    std::vector<double>* dot = nullptr, const BxState* dev = nullptr,
+                    const double** res_dev = nullptr) {
   ed_ham* h = bt->h;
   ed_ctx* ctx = h->ctx;
   const ed_basis* b = h->basis;
   const int64_t n = bt->dim * B;
   const int sbits = batch_sbits(bt);
-  if (rs && bt->xq_src == x && bt->xq_b == B) {
+  if (rs && dev) {
+    bt->xq_src = nullptr;
+    k_bx_prequant<<<1, 1, 0, ctx->stream>>>(bt->d_gmax, dev->xq_valid);
+    ED_CHECK_LAUNCH(ctx);
+    k_batch_maxexp_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, dev->xq_valid);
+    ED_CHECK_LAUNCH(ctx);
+    k_batch_quantize_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, sbits,
+                                                                 (long long*)bt->d_xq, dev->xq_valid);
+    ED_CHECK_LAUNCH(ctx);
+  } else if (rs && bt->xq_src == x && bt->xq_b == B) {
     // made with x by k_batch_scale_quantize: use it once
     bt->xq_src = nullptr;
   } else if (rs) {
@@ -798,18 +964,22 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   const int v = bt->hv_variant < 0 ? 3 : bt->hv_variant;
   int grid = 0;
   {
-    const int r = launch(v, dot ? bt->d_red : nullptr, &grid);
+    const int r = launch(v, (dot || res_dev) ? bt->d_red : nullptr, &grid);
     if (r == ED_ENOTSUP) return ed_fail(ED_ENOTSUP, "batch too wide for the batched H.v");
     ED_TRY(r);
   }
-  if (dot) {
+  if (dot || res_dev) {
     const int64_t items = 2 * (int64_t)B;
     double* res = bt->d_red + (size_t)items * grid;
     k_batch_reduce<<<grid_n(ctx, items * 32, 8), 256, 0, ctx->stream>>>(bt->d_red, grid, items, res, items);
     ED_CHECK_LAUNCH(ctx);
+    if (res_dev) {
+      *res_dev = res;
+      return ED_OK;
+    }
     ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * (size_t)items, cudaMemcpyDeviceToHost, ctx->stream));
     ED_CUDA(cudaStreamSynchronize(ctx->stream));
-    dot->assign(bt->h_red, bt->h_red + items);
+    if (dot) dot->assign(bt->h_red, bt->h_red + items);
   }
   return ED_OK;
 }
@@ -935,6 +1105,28 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     cudaFree(pool); cudaFree(w); cudaFree(dg[0]); cudaFree(dg[1]); cudaFree(d_coef); cudaFree(d_idx); cudaFree(dY);
     return ed_fail(ED_ENOMEM, "batched eigenvectors do not fit in device memory");
   }
+  // device state of the expansion sweeps
+  BxState st;
+  double* st_buf = nullptr;
+  int* st_int = nullptr;
+  const size_t m1 = (size_t)m + 1;
+  if (cudaMalloc(&st_buf, sizeof(double) * (2 * m1 + 2) * (size_t)B) != cudaSuccess ||
+      cudaMalloc(&st_int, sizeof(int) * 8) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(st_buf);
+    cudaFree(pool); cudaFree(w); cudaFree(dg[0]); cudaFree(dg[1]); cudaFree(d_coef); cudaFree(d_idx); cudaFree(dY);
+    return ed_fail(ED_ENOMEM, "batched solver state does not fit in device memory");
+  }
+  st.alpha = st_buf;
+  st.beta = st_buf + m1 * B;
+  st.prevn = st_buf + 2 * m1 * B;
+  st.wmax = st_buf + (2 * m1 + 1) * B;
+  st.again = st_int;
+  st.emax = st_int + 1;
+  st.finite = st_int + 2;
+  st.xq_valid = st_int + 3;
+  ED_CUDA(cudaMemsetAsync(st_int, 0, sizeof(int) * 8, ctx->stream));
+  std::vector<double> st_host(2 * m1 * (size_t)B);
   std::vector<double*> col(m + 1), freel;
   for (int i = 0; i < pool_cols; ++i) {
     double* p = pool + (size_t)i * colB;
@@ -967,106 +1159,71 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   while (A > 0 && its < max_it) {
     ++its;
     const int64_t colA = dim * (int64_t)A;
+    // the expansion sweep runs without a host round trip: the coefficients
+    // live in the device state (st), alpha and beta come back after it
     for (int j = k; j < m; ++j) {
-      // H.v with the local projection coefficient a_b = v_j^T w (and ||w||^2)
-      // reduced in the same pass
-      if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true, &out)) != ED_OK) goto cleanup;
+      const double* res_hv = nullptr;
+      if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true, nullptr, &st, &res_hv)) != ED_OK) goto cleanup;
       bt->nhv++;
-      const double* local_vj = nullptr;
-      const double* local_vjm1 = nullptr;
-      {
-        std::vector<double> hc((size_t)2 * A);
-        const bool three = j > k && j > 0;
-        for (int b = 0; b < A; ++b) {
-          const double a = out[b];
-          alpha[(size_t)b * (m + 1) + j] = a;
-          hc[b] = a;
-          hc[(size_t)A + b] = three ? beta[(size_t)b * (m + 1) + j - 1] : 0.0;
-        }
-        // the local coefficients go to the upper half of d_coef; the first
-        // CGS pass applies them in its own pass over w
-        cudaMemcpyAsync(d_coef + (size_t)64 * A, hc.data(), sizeof(double) * 2 * A, cudaMemcpyHostToDevice,
-                        ctx->stream);
-        local_vj = col[j];
-        local_vjm1 = three ? col[j - 1] : nullptr;
-      }
-      // full CGS pass (+ DGKS refinement when any realisation needs it)
-      std::vector<const double*> vs(col.begin(), col.begin() + j + 1);
-      // norms before each pass for the DGKS test: no norm in the dot pass (one
-      // FP64 FMA per entry less); before the first pass it is
-      // sqrt(||w_after||^2 + sum_i c_i^2) (Pythagoras), before the second the
-      // norm after the first
-      std::vector<double> prevn(A, -1.0);
-      for (int pass = 0; pass < 2; ++pass) {
-        if ((rc = batch_dots(bt, A, vs, w, false, out, pass == 0 ? local_vj : nullptr, local_vjm1,
-                             d_coef + (size_t)64 * A)) != ED_OK)
-          goto cleanup;
-        std::vector<double> hc(out.begin(), out.begin() + (size_t)(j + 1) * A);
-        cudaMemcpyAsync(d_coef, hc.data(), sizeof(double) * hc.size(), cudaMemcpyHostToDevice, ctx->stream);
-        BCols vc;
-        memset(&vc, 0, sizeof(vc));
-        for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
-        // update and the new norms in one pass
-        {
-          const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
-          // items: A norms, then A maxima
-          if ((rc = batch_reduce_buf(bt, (size_t)2 * A * nblk + 2 * (size_t)A)) != ED_OK) goto cleanup;
-          if (j + 1 <= BU_REG)
-            k_batch_update_norm<true><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
-          else
-            k_batch_update_norm<false><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk);
-          ctx->kernels++;
-          double* res = bt->d_red + (size_t)2 * A * nblk;
-          k_batch_reduce<<<grid_n(ctx, (int64_t)A * 64, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, 2 * (int64_t)A,
-                                                                                    res, A);
-          ctx->kernels++;
-          ED_CUDA(cudaMemcpyAsync(bt->h_red, res, sizeof(double) * 2 * (size_t)A, cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-          ED_CUDA(cudaStreamSynchronize(ctx->stream));
-          out.assign(bt->h_red, bt->h_red + A);
-          wmax.assign(bt->h_red + A, bt->h_red + 2 * A);
-        }
-        for (int b = 0; b < A; ++b) alpha[(size_t)b * (m + 1) + j] += hc[(size_t)j * A + b];
-        bool again = false;
-        for (int b = 0; b < A; ++b) {
-          const double nw = std::sqrt(out[b]);
-          beta[(size_t)b * (m + 1) + j] = nw;
-          if (prevn[b] < 0.0) {
-            double s2 = out[b];
-            for (int i = 0; i <= j; ++i) s2 += hc[(size_t)i * A + b] * hc[(size_t)i * A + b];
-            prevn[b] = std::sqrt(s2);
-          }
-          if (nw < 0.7071067811865476 * prevn[b]) again = true;
-          prevn[b] = nw;
-        }
-        if (!again) break;
-      }
-      // normalise into col[j+1]; its fixed-point copy for the next H.v in
-      // the same pass: the largest exponent of the scaled block is the largest
-      // of fl(max_r |w[r, b]| * s_b) over b (rounding is monotonic); where
-      // one is not determined by the high words, scale only
-      std::vector<double> sc(A);
-      int emax = 0;
-      bool finite = true;
-      for (int b = 0; b < A; ++b) {
-        const double nb = beta[(size_t)b * (m + 1) + j];
-        sc[b] = nb > 1e-300 ? 1.0 / nb : 0.0;
-        if (sc[b] == 0.0) continue;  // a zero column stays zero
-        const int eb = ed_fx64_emax_scaled(wmax[b], sc[b]);
-        if (eb < 0) { finite = false; continue; }
-        emax = std::max(emax, eb);
-      }
-      cudaMemcpyAsync(d_coef, sc.data(), sizeof(double) * A, cudaMemcpyHostToDevice, ctx->stream);
-      if (finite) {
-        k_batch_scale_quantize<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A, emax,
-                                                                           batch_sbits(bt), (long long*)bt->d_xq,
-                                                                           bt->d_gmax);
-        bt->xq_src = col[j + 1];
-        bt->xq_b = A;
-      } else {
-        k_batch_scale<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A);
-      }
+      const bool three = j > k && j > 0;
+      k_bx_local<<<(A + 255) / 256, 256, 0, ctx->stream>>>(res_hv, A, j, m + 1, three ? 1 : 0, st,
+                                                           d_coef + (size_t)64 * A);
       ctx->kernels++;
+      std::vector<const double*> vs(col.begin(), col.begin() + j + 1);
+      BCols vc;
+      memset(&vc, 0, sizeof(vc));
+      for (int i = 0; i <= j; ++i) vc.p[i] = col[i];
+      const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
+      {
+        // room for the dots' and the update's partials at once, so that no
+        // call below moves the reduce buffer while res_upd points into it
+        const size_t nd = (size_t)(j + 1) * A;
+        const size_t need = std::max((nd + A) * nblk + nd, (size_t)2 * A * nblk + 2 * (size_t)A);
+        if ((rc = batch_reduce_buf(bt, need)) != ED_OK) goto cleanup;
+      }
+      double* res_upd = bt->d_red + (size_t)2 * A * nblk;
+      // first pass: the local step, the dots, the update; the second (DGKS
+      // refinement) runs where the device found a realisation that needs it
+      for (int pass = 0; pass < 2; ++pass) {
+        const int* pred = pass ? st.again : nullptr;
+        if ((rc = batch_dots_dev(bt, A, vs, w, d_coef, pass == 0 ? col[j] : nullptr,
+                                 pass == 0 && three ? col[j - 1] : nullptr, d_coef + (size_t)64 * A, pred)) != ED_OK)
+          goto cleanup;
+        if (j + 1 <= BU_REG)
+          k_batch_update_norm<true><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk,
+                                                                   pred);
+        else
+          k_batch_update_norm<false><<<nblk, 256, 0, ctx->stream>>>(vc, j + 1, d_coef, w, dim, A, bt->d_red, nblk,
+                                                                    pred);
+        ctx->kernels++;
+        k_batch_reduce<<<grid_n(ctx, (int64_t)A * 64, 8), 256, 0, ctx->stream>>>(bt->d_red, nblk, 2 * (int64_t)A,
+                                                                                  res_upd, A, pred);
+        ctx->kernels++;
+        k_bx_post<<<(A + 255) / 256, 256, 0, ctx->stream>>>(res_upd, d_coef, A, j, m + 1, pass == 0 ? 1 : 0, st,
+                                                            pred);
+        ctx->kernels++;
+      }
+      // normalise into col[j+1] with its fixed-point copy for the next H.v
+      // in the same pass (the largest exponent of the scaled block from the
+      // per-realisation maxima; where it is not determined, scale only)
+      k_bx_scale<<<1, 256, 0, ctx->stream>>>(A, j, m + 1, st, d_coef);
+      ctx->kernels++;
+      k_bx_scale_quantize<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A, batch_sbits(bt),
+                                                                     (long long*)bt->d_xq, bt->d_gmax, st);
+      ED_CHECK_LAUNCH(ctx);
+    }
+    {
+      // alpha and beta of this sweep's steps back to the host
+      const size_t na = (size_t)A * (m + 1);
+      ED_CUDA(cudaMemcpyAsync(st_host.data(), st.alpha, sizeof(double) * na, cudaMemcpyDeviceToHost, ctx->stream));
+      ED_CUDA(cudaMemcpyAsync(st_host.data() + na, st.beta, sizeof(double) * na, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+      ED_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int b = 0; b < A; ++b)
+        for (int jj = k; jj < m; ++jj) {
+          alpha[(size_t)b * (m + 1) + jj] = st_host[(size_t)b * (m + 1) + jj];
+          beta[(size_t)b * (m + 1) + jj] = st_host[(size_t)A * (m + 1) + (size_t)b * (m + 1) + jj];
+        }
     }
     // projected problems, convergence and restart, per active realisation
     // (independent small eigenproblems: one host thread each)
@@ -1182,6 +1339,8 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
                                                                                    d_idx);
       ctx->kernels++;
       cur = 1 - cur;
+      // the fixed-point copy was made for the unpacked block
+      ED_CUDA(cudaMemsetAsync(st.xq_valid, 0, sizeof(int), ctx->stream));
       std::vector<double> a2((size_t)A2 * (m + 1)), b2((size_t)A2 * (m + 1)), r2((size_t)A2 * (m + 1));
       std::vector<int> act2(A2);
       for (int t = 0; t < A2; ++t) {
@@ -1242,6 +1401,8 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
 cleanup:
   cudaStreamSynchronize(ctx->stream);
   bt->xq_src = nullptr;  // made with a column of the pool freed here
+  cudaFree(st_buf);
+  cudaFree(st_int);
   cudaFree(pool);
   cudaFree(w);
   cudaFree(dg[0]);
