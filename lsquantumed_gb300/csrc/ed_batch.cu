@@ -208,6 +208,11 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
   const int e_unit = *gmax_p - 1022 - sbits;
   const double s1 = __longlong_as_double((long long)(e_unit / 2 + 1023) << 52);
   const double s2 = __longlong_as_double((long long)(e_unit - e_unit / 2 + 1023) << 52);
+  // real storage: the couplings carry the fixed-point scale 2^e_unit (a power
+  // of two, so c * 2^e is exact where it stays normal and the results are
+  // bit-identical): one conversion and one product per sum
+  const bool fold = RS && e_unit > -900 && e_unit < 900;
+  const double c0s = c0 * s1 * s2, c1s = c1 * s1 * s2;
   const long long kNaN = (long long)0x8000000000000000ull;
   const uint32_t low = (1u << w0) - 1u;
   const int nb = bb.nb;
@@ -287,10 +292,17 @@ __global__ void __launch_bounds__(256) k_batch_hv(const uint32_t* __restrict__ s
         const size_t k = (size_t)(r0 + rr) * B + b;
         const double d = diag[k];
         const double2 xv = RS ? make_double2(xr[k], 0.0) : x[k];
-        const double s0r = (double)a[0] * s1 * s2, s0i = (double)a[1] * s1 * s2;
-        const double t1r = (double)a[2] * s1 * s2, t1i = (double)a[3] * s1 * s2;
-        double yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
-        double yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
+        double yr, yi = 0.0;
+        if (fold) {
+          yr = fma(d, xv.x, fma(c0s, (double)a[0], c1s * (double)a[2]));
+        } else {
+          const double s0r = (double)a[0] * s1 * s2, t1r = (double)a[2] * s1 * s2;
+          yr = fma(d, xv.x, fma(c0, s0r, c1 * t1r));
+          if (!RS) {
+            const double s0i = (double)a[1] * s1 * s2, t1i = (double)a[3] * s1 * s2;
+            yi = fma(d, xv.y, fma(c0, s0i, c1 * t1i));
+          }
+        }
         if (bad) { yr = __longlong_as_double(0x7FF8000000000000ll); yi = yr; }
         if (RS) {
           ((double*)y_)[k] = yr;
@@ -933,8 +945,14 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
     return ED_OK;
   };
   if (bt->hv_variant < 0 && rs) {
-    // time every variant once on this input (plain H.v; the result is the same
-    // for all of them) and keep the fastest for the rest of the batch's life
+    // a batch of this width on this operator was tuned before: reuse
+    for (const auto& t : h->batch_tile)
+      if (t.first == B) bt->hv_variant = t.second;
+  }
+  if (bt->hv_variant < 0 && rs) {
+    // time every variant on this input (plain H.v; the result is the same for
+    // all of them), best of three launches each, and keep the fastest for
+    // the batch's life and for later batches of this width on this operator
     cudaEvent_t e0, e1;
     ED_CUDA(cudaEventCreate(&e0));
     ED_CUDA(cudaEventCreate(&e1));
@@ -945,12 +963,16 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
       int r = launch(v, nullptr, nullptr);  // warm-up (and the T0 fill of a new shape)
       if (r == ED_ENOTSUP) continue;
       ED_TRY(r);
-      ED_CUDA(cudaEventRecord(e0, ctx->stream));
-      ED_TRY(launch(v, nullptr, nullptr));
-      ED_CUDA(cudaEventRecord(e1, ctx->stream));
-      ED_CUDA(cudaEventSynchronize(e1));
       float ms = 0.0f;
-      ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      for (int rep = 0; rep < 3; ++rep) {
+        ED_CUDA(cudaEventRecord(e0, ctx->stream));
+        ED_TRY(launch(v, nullptr, nullptr));
+        ED_CUDA(cudaEventRecord(e1, ctx->stream));
+        ED_CUDA(cudaEventSynchronize(e1));
+        float t = 0.0f;
+        ED_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        if (rep == 0 || t < ms) ms = t;
+      }
       if (!have || ms < best) {
         have = true;
         best = ms;
@@ -960,6 +982,7 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     bt->hv_variant = vbest;
+    h->batch_tile.emplace_back(B, vbest);
   }
   const int v = bt->hv_variant < 0 ? 3 : bt->hv_variant;
   int grid = 0;

@@ -116,6 +116,8 @@ struct ed_lin;  // two-table fixed-point H.v state (ed_hv_lin.cu)
 struct ed_ham {
   ed_ctx* ctx = nullptr;
   const ed_basis* basis = nullptr;
+  // batched H.v tile chosen by the autotuner, per batch width (ed_batch.cu)
+  std::vector<std::pair<int, int>> batch_tile;
   // reference parameters (uniform mode)
   bool per_bond = false;
   double J1 = 0, D1 = 0, J2 = 0, D2 = 0;
