@@ -768,17 +768,25 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         phases = {}
+
+        def mark(key, t_prev):
+            torch.cuda.synchronize()
+            t_now = time.perf_counter()
+            phases[key] = t_now - t_prev
+            return t_now
         b2 = ed.Basis(env, mag)
+        tm = mark('basis_s', t0)
         lat2 = ed.square2D(env, lx, ly) if ltype == 'square2D' else ed.chain1D(env)
         H2 = ed.Hamiltonian(env, b2, lat2, J1, D1, J2, D2)
         H2.build_diag(env)
         H2.build_off_diag(env)
+        tm = mark('hamiltonian_s', tm)
         eps2 = ed.Solver.SolverInit(H2, nev, ncv if ncv else ed.PETSC_DEFAULT)
         ed.Solver.EPSSetTolerances(eps2, tol, 0)
         eps2.set_restart_arithmetic(args.restart)
         eps2.set_initial_vector(start_host)
-        torch.cuda.synchronize()
-        phases['setup_and_upload_s'] = time.perf_counter() - t0
+        tm = mark('solver_init_and_upload_s', tm)
+        phases['setup_and_upload_s'] = tm - t0
         ed.Solver.solve(env, eps2)
         torch.cuda.synchronize()
         phases['solve_s'] = time.perf_counter() - t0 - phases['setup_and_upload_s']

@@ -642,7 +642,8 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host) {
   const int64_t n = e->h->basis->dim;
   if (e->real_storage) {
     // expand to complex128 in halves through a basis column that holds no
-    // Ritz vector (col_r[m], n doubles = n/2 complex entries): no allocation
+    // Ritz vector (col_r[m], n doubles = n/2 complex entries) and the work
+    // vector: no allocation
     const int m = (int)e->col_r.size() - 1;
     if (n < 2) {  // one state: a column cannot hold one complex entry
       double v = 0.0;
@@ -652,14 +653,19 @@ int ed_eps_get_eigenvector_host(ed_eps* e, int i, ed_cplx* vec_host) {
       std::memset((char*)vec_host + sizeof(double), 0, sizeof(double));
       return ED_OK;
     }
-    double2* stage = (double2*)e->col_r[m];
-    const int64_t half = n / 2;
-    for (int64_t r0 = 0; r0 < n; r0 += half) {
+    // two stages (that column and the work vector, both free after the
+    // solve): both halves are expanded and copied back with one wait
+    double2* stage[2] = {(double2*)e->col_r[m], (double2*)e->w_r};
+    const int64_t half = n / 2;  // complex entries a stage holds
+    int q = 0;
+    for (int64_t r0 = 0; r0 < n; r0 += half, ++q) {
+      if (q >= 2) ED_CUDA(cudaStreamSynchronize(ctx->stream));  // odd n: a third chunk reuses a stage
       const int64_t c = std::min(half, n - r0);
-      ED_TRY(ed_real_to_complex(ctx, e->col_r[i] + r0, stage, c));
-      ED_CUDA(cudaMemcpyAsync(vec_host + r0, stage, sizeof(double2) * (size_t)c, cudaMemcpyDeviceToHost, ctx->stream));
-      ED_CUDA(cudaStreamSynchronize(ctx->stream));
+      ED_TRY(ed_real_to_complex(ctx, e->col_r[i] + r0, stage[q & 1], c));
+      ED_CUDA(cudaMemcpyAsync(vec_host + r0, stage[q & 1], sizeof(double2) * (size_t)c, cudaMemcpyDeviceToHost,
+                              ctx->stream));
     }
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));
     return ED_OK;
   }
   ED_CUDA(cudaMemcpyAsync(vec_host, e->col[i], sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -423,8 +423,9 @@ def test_real_storage_matches_complex_path(ed, envs):
 @pytest.mark.parametrize('case', [(18, 7), (8, 4), (16, 0)])
 def test_host_eigenvector_real_storage(ed, envs, case):
     """solution_host of a real-storage solve (staged in halves through a spare
-    basis column) equals the device eigenvector bit for bit, for an odd
-    dimension (C(18,16) = 153), the one-state sector and an even one."""
+    basis column and the work vector) equals the device eigenvector bit for
+    bit, for an odd dimension (C(18,16) = 153: a third chunk reuses a stage),
+    the one-state sector and an even one."""
     N, mag = case
     env, b, h, M = make_pair(ed, envs, 0, N, 1, N, mag, 1.0, 1.0, 0.3, 0.3)
     nev = 1 if b.size == 1 else 2
@@ -439,8 +440,8 @@ def test_host_eigenvector_real_storage(ed, envs, case):
 
 
 def test_restart_pair_arithmetic(ed, envs, golden):
-    """Float-pair products in the restart combination (forced here; the
-    default from 2^22 basis states up): every golden solver case at 1e-12 as
+    """Float-pair products in the restart combination (forced here; opt-in,
+    the default keeps FP64): every golden solver case at 1e-12 as
     with FP64 products, and on the 4x6 lattice (2.7M states) the same lowest
     levels as the FP64 products at 1e-12 relative, residuals within tol and
     orthonormal Ritz vectors."""
