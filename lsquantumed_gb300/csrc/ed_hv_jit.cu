@@ -109,6 +109,12 @@ struct alignas(16) D2 { double x, y; };
 struct alignas(16) L2 { i64 x, y; };
 #define NAN_Q ((i64)0x8000000000000000ull)
 #define T0B(off) ((u32)*(const unsigned short*)((const char*)t0s + (off)))
+// T0 sits in shared memory permuted by SWZ (an involution, linear over XOR):
+// bits 6..10 of the index are folded into bits 1..5, which pick the bank of
+// a 16-bit entry, so lanes whose indices differ only above bit 5 no longer
+// meet in one bank.  T0[c ^ m] = t0s[SWZ(c) ^ SWZ(m)]: one XOR per row, and
+// SWZ(m) is each bond's immediate.
+#define SWZ(i) ((i) ^ ((((i) >> 6) & 31u) << 1))
 // element of the fixed-point input: real parts only (RX) or (re, im) pairs
 template <bool RX> struct XEt { typedef L2 T; };
 template <> struct XEt<true> { typedef i64 T; };
@@ -143,8 +149,9 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 s = states[r];
     const u32 c0 = s & LOWMASK, c1 = s >> W0;
     const u32 rr = (u32)r;
-    const u32 rb0 = rr - (u32)t0s[c0];
-    const u32 c0b = c0 << 1;  // byte offset of T0[c0]; T0[c0 ^ m] is at c0b ^ (m << 1)
+    const u32 c0s = SWZ(c0);
+    const u32 rb0 = rr - (u32)t0s[c0s];
+    const u32 c0b = c0s << 1;  // byte offset of T0[c0]; T0[c0 ^ m] is at c0b ^ (SWZ(m) << 1)
     const u32 rb1 = rr - t1[c1];
     const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     i64 a0 = 0, a1 = 0, a2 = 0, a3 = 0;
@@ -194,7 +201,7 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
                                      const unsigned short* __restrict__ t0, const u32* __restrict__ t1, double c0c,
                                      double c1c, double* __restrict__ partial) {
   extern __shared__ unsigned short t0s[];
-  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
+  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[SWZ((u32)i)];
   __syncthreads();
   const int e_unit = gmax_p[0] - 1022 - sbits;
   const double s1 = __longlong_as_double((i64)(e_unit / 2 + 1023) << 52);
@@ -339,8 +346,9 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 s = states[r];
     const u32 c0 = s & LOWMASK, c1 = s >> W0;
     const u32 rr = (u32)r;
-    const u32 rb0 = rr - (u32)t0s[c0];
-    const u32 c0b = c0 << 1;
+    const u32 c0s = SWZ(c0);
+    const u32 rb0 = rr - (u32)t0s[c0s];
+    const u32 c0b = c0s << 1;
     const u32 rb1 = rr - t1[c1];
     const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     A128 ar = {0ull, 0ll}, ai = {0ull, 0ll};
@@ -383,7 +391,7 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
                                      const unsigned short* __restrict__ t0, const u32* __restrict__ t1, int pbexp,
                                      double* __restrict__ partial, const PBC& pbc, const i64* __restrict__ gcf) {
   extern __shared__ unsigned short t0s[];
-  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[i];
+  for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[SWZ((u32)i)];
   __syncthreads();
   const int xexp = gmax_p[0] - 1022 - sbits + pbexp;
   double dacc[3] = {0.0, 0.0, 0.0};
@@ -528,10 +536,13 @@ std::string flip_test(uint32_t m0, uint32_t m1, int w0, int* d_out) {
 
 // Address of a bond's target entry, rank(s ^ m): class 0 (both sites in the
 // low half), 1 (both in the high half), 2 (across).
+// the shared-memory T0's permutation (SWZ in the generated source)
+uint32_t swz(uint32_t i) { return i ^ (((i >> 6) & 31u) << 1); }
+
 std::string target(int cls, uint32_t m0, uint32_t m1) {
-  if (cls == 0) return "xe + (rb0 + T0B(c0b ^ " + hex(m0 << 1) + "))";
+  if (cls == 0) return "xe + (rb0 + T0B(c0b ^ " + hex(swz(m0) << 1) + "))";
   if (cls == 1) return "xe + (rb1 + t1[c1 ^ " + hex(m1) + "])";
-  return "xe + (T0B(c0b ^ " + hex(m0 << 1) + ") + t1[c1 ^ " + hex(m1) + "])";
+  return "xe + (T0B(c0b ^ " + hex(swz(m0) << 1) + ") + t1[c1 ^ " + hex(m1) + "])";
 }
 
 // One bond's code; type selects the accumulators (nn: a0/a1, nnn: a2/a3).
