@@ -412,6 +412,7 @@ int ed_ham_destroy(ed_ham* h) {
   if (h->d_x) cudaFree(h->d_x);
   if (h->d_y) cudaFree(h->d_y);
   if (h->d_xq) cudaFree(h->d_xq);
+  if (h->jit_t1n) cudaFree(h->jit_t1n);
   if (h->d_xe) cudaFree(h->d_xe);
   if (h->d_gmax) cudaFree(h->d_gmax);
   ed_lin_free(h->lin);

@@ -142,7 +142,7 @@ __device__ __forceinline__ void gather(const XE<RX>* p, bool on, i64& ar, i64& a
 template <bool CHECK, bool RX, bool DOT, bool RIO>
 __device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
-                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
+                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1, const uint4* __restrict__ t1n,
                                      double c0c, double c1c, double s1, double s2, double* dacc) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
@@ -153,6 +153,7 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 rb0 = rr - (u32)t0s[c0s];
     const u32 c0b = c0s << 1;  // byte offset of T0[c0]; T0[c0 ^ m] is at c0b ^ (SWZ(m) << 1)
     const u32 rb1 = rr - t1[c1];
+    const uint4* __restrict__ tn = t1n + (size_t)c1 * NQ;  // t1[c1 ^ m1] of the bonds, in order
     const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     i64 a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     bool bad = false;
@@ -186,9 +187,9 @@ template <bool RX, bool DOT, bool RIO>
 __device__ __noinline__ void rows_checked(const u32* __restrict__ states, const double* __restrict__ diag,
                                           const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                           i64 dim, const unsigned short* __restrict__ t0s,
-                                          const u32* __restrict__ t1, double c0c, double c1c, double s1, double s2,
+                                          const u32* __restrict__ t1, const uint4* __restrict__ t1n, double c0c, double c1c, double s1, double s2,
                                           double* dacc) {
-  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, c0c, c1c, s1, s2, dacc);
 }
 
 // RIO: x and y are real storage (double[dim]); the input is then real, and
@@ -198,7 +199,7 @@ template <bool DOT, bool RIO>
 __device__ __forceinline__ void body(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq,
                                      const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
-                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, double c0c,
+                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, const uint4* __restrict__ t1n, double c0c,
                                      double c1c, double* __restrict__ partial) {
   extern __shared__ unsigned short t0s[];
   for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[SWZ((u32)i)];
@@ -209,11 +210,11 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   double dacc[3] = {0.0, 0.0, 0.0};
   const bool rx = RIO || gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
-    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, c0c, c1c, s1, s2, dacc);
+    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, t1n, c0c, c1c, s1, s2, dacc);
   } else {
-    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
-    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, c0c, c1c, s1, s2, dacc);
+    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, c0c, c1c, s1, s2, dacc);
+    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, t1n, c0c, c1c, s1, s2, dacc);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -237,8 +238,8 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
 #define JIT_KERNEL(NAME, DOT, RIO, NT, MINB)                                                              \
   extern "C" __global__ void __launch_bounds__(NT, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
-      const u32* t1, double c0c, double c1c, double* partial) {                                             \
-    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, c0c, c1c, partial);                  \
+      const u32* t1, const uint4* t1n, double c0c, double c1c, double* partial) {                                             \
+    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, t1n, c0c, c1c, partial);                  \
   }
 // register budgets: 2, 3 or 4 blocks of 256 per SM (128, 80 or 64 registers);
 // _r: real storage of x and y
@@ -339,7 +340,7 @@ __device__ __forceinline__ double a128_to_double(A128 a, int X) {
 template <bool CHECK, bool RX, bool DOT, bool RIO, typename CF>
 __device__ __forceinline__ void rows(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
-                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1,
+                                     i64 dim, const unsigned short* __restrict__ t0s, const u32* __restrict__ t1, const uint4* __restrict__ t1n,
                                      int xexp, double* dacc, const CF& cf) {
   const i64 stride = (i64)gridDim.x * blockDim.x;
   for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
@@ -350,6 +351,7 @@ __device__ __forceinline__ void rows(const u32* __restrict__ states, const doubl
     const u32 rb0 = rr - (u32)t0s[c0s];
     const u32 c0b = c0s << 1;
     const u32 rb1 = rr - t1[c1];
+    const uint4* __restrict__ tn = t1n + (size_t)c1 * NQ;  // t1[c1 ^ m1] of the bonds, in order
     const XE<RX>* xe = (const XE<RX>*)xq;  // rank(s) = t1[c1] + T0[c0]
     A128 ar = {0ull, 0ll}, ai = {0ull, 0ll};
     bool bad = false;
@@ -379,16 +381,16 @@ template <bool RX, bool DOT, bool RIO>
 __device__ __noinline__ void rows_checked(const u32* __restrict__ states, const double* __restrict__ diag,
                                           const D2* __restrict__ x, const L2* __restrict__ xq, D2* __restrict__ y,
                                           i64 dim, const unsigned short* __restrict__ t0s,
-                                          const u32* __restrict__ t1, int xexp, double* dacc,
+                                          const u32* __restrict__ t1, const uint4* __restrict__ t1n, int xexp, double* dacc,
                                           const i64* __restrict__ gcf) {
-  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
+  rows<true, RX, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, xexp, dacc, gcf);
 }
 
 template <bool DOT, bool RIO>
 __device__ __forceinline__ void body(const u32* __restrict__ states, const double* __restrict__ diag,
                                      const D2* __restrict__ x, const L2* __restrict__ xq,
                                      const int* __restrict__ gmax_p, int sbits, D2* __restrict__ y, i64 dim,
-                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, int pbexp,
+                                     const unsigned short* __restrict__ t0, const u32* __restrict__ t1, const uint4* __restrict__ t1n, int pbexp,
                                      double* __restrict__ partial, const PBC& pbc, const i64* __restrict__ gcf) {
   extern __shared__ unsigned short t0s[];
   for (int i = threadIdx.x; i < (1 << W0); i += blockDim.x) t0s[i] = t0[SWZ((u32)i)];
@@ -397,11 +399,11 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
   double dacc[3] = {0.0, 0.0, 0.0};
   const bool rx = RIO || gmax_p[2] == 0;
   if (gmax_p[1]) {
-    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
-    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, gcf);
+    if (rx) rows_checked<true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, xexp, dacc, gcf);
+    else rows_checked<false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, t1n, xexp, dacc, gcf);
   } else {
-    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, pbc);
-    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, xexp, dacc, pbc);
+    if (rx) rows<false, true, DOT, RIO>(states, diag, x, xq, y, dim, t0s, t1, t1n, xexp, dacc, pbc);
+    else if (!RIO) rows<false, false, DOT, false>(states, diag, x, xq, y, dim, t0s, t1, t1n, xexp, dacc, pbc);
   }
   if (DOT) {
     __shared__ double sh[3 * 32];
@@ -425,8 +427,8 @@ __device__ __forceinline__ void body(const u32* __restrict__ states, const doubl
 #define JIT_KERNEL(NAME, DOT, RIO, NT, MINB)                                                              \
   extern "C" __global__ void __launch_bounds__(NT, MINB) NAME(const u32* states, const double* diag,        \
       const D2* x, const L2* xq, const int* gmax_p, int sbits, D2* y, i64 dim, const unsigned short* t0,     \
-      const u32* t1, int pbexp, double* partial, const __grid_constant__ PBC pbc, const i64* gcf) {         \
-    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, pbexp, partial, pbc, gcf);           \
+      const u32* t1, const uint4* t1n, int pbexp, double* partial, const __grid_constant__ PBC pbc, const i64* gcf) {         \
+    body<DOT, RIO>(states, diag, x, xq, gmax_p, sbits, y, dim, t0, t1, t1n, pbexp, partial, pbc, gcf);           \
   }
 JIT_KERNEL(k_hv_jit_b2, false, false, 256, 2)
 JIT_KERNEL(k_hv_jit_dot_b2, true, false, 256, 2)
@@ -464,6 +466,8 @@ struct JitModule {
   bool ok = false;
   CUfunction fn[kJitBudgets][2][2] = {};  // [budget][dot][real storage]
   int per_sm[kJitBudgets][2][2] = {};
+  std::vector<uint32_t> slots;  // high-half mask of each neighbour-table slot
+  int nq = 1;                   // 16-byte loads per row of the neighbour table
 };
 
 std::map<std::tuple<int, uint64_t>, JitModule> g_modules;
@@ -539,25 +543,39 @@ std::string flip_test(uint32_t m0, uint32_t m1, int w0, int* d_out) {
 // the shared-memory T0's permutation (SWZ in the generated source)
 uint32_t swz(uint32_t i) { return i ^ (((i >> 6) & 31u) << 1); }
 
-std::string target(int cls, uint32_t m0, uint32_t m1) {
+// t1v: the expression of t1[c1 ^ m1] (a component of a 16-byte load from
+// the row's neighbour table)
+std::string target(int cls, uint32_t m0, const std::string& t1v) {
   if (cls == 0) return "xe + (rb0 + T0B(c0b ^ " + hex(swz(m0) << 1) + "))";
-  if (cls == 1) return "xe + (rb1 + t1[c1 ^ " + hex(m1) + "])";
-  return "xe + (T0B(c0b ^ " + hex(swz(m0) << 1) + ") + t1[c1 ^ " + hex(m1) + "])";
+  if (cls == 1) return "xe + (rb1 + " + t1v + ")";
+  return "xe + (T0B(c0b ^ " + hex(swz(m0) << 1) + ") + " + t1v + ")";
 }
 
 // One bond's code; type selects the accumulators (nn: a0/a1, nnn: a2/a3).
-std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1, int w0, int* d) {
+std::string bond_code(int cls, int type, uint32_t m0, uint32_t m1, const std::string& t1v, int w0, int* d) {
   const char* ar = type ? "a2" : "a0";
   const char* ai = type ? "a3" : "a1";
   const std::string on = flip_test(m0, m1, w0, d);
-  return "gather<CHECK, RX>(" + target(cls, m0, m1) + ", " + on + ", " + ar + ", " + ai + ", bad);\n    ";
+  return "gather<CHECK, RX>(" + target(cls, m0, t1v) + ", " + on + ", " + ar + ", " + ai + ", bad);\n    ";
 }
 
 // Per-bond form: the bond's own coefficient (entry q of the kernel's
 // coefficient parameter) instead of a type accumulator.
-std::string bond_code_pb(int cls, uint32_t m0, uint32_t m1, int q, int w0, int* d) {
+std::string bond_code_pb(int cls, uint32_t m0, uint32_t m1, const std::string& t1v, int q, int w0, int* d) {
   const std::string on = flip_test(m0, m1, w0, d);
-  return "gatherw<CHECK, RX>(" + target(cls, m0, m1) + ", " + on + ", cf[" + std::to_string(q) + "], ar, ai, bad);\n    ";
+  return "gatherw<CHECK, RX>(" + target(cls, m0, t1v) + ", " + on + ", cf[" + std::to_string(q) + "], ar, ai, bad);\n    ";
+}
+
+// out[c1][k] = t1[c1 ^ slots[k]] (0 past the last slot), nq * 4 entries per c1
+__global__ void k_build_t1n(const uint32_t* __restrict__ t1, int64_t nc1, const uint32_t* __restrict__ slots, int K,
+                            int nq, uint32_t* __restrict__ out) {
+  const int64_t per = (int64_t)nq * 4, n = nc1 * per;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t c1 = i / per;
+    const int k = (int)(i - c1 * per);
+    out[i] = k < K ? t1[(uint32_t)c1 ^ slots[k]] : 0u;
+  }
 }
 
 }  // namespace
@@ -583,29 +601,61 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
     auto it = g_modules.find(key);
     if (it == g_modules.end()) {
       JitModule jm;
-      std::vector<std::pair<int, std::string>> code;  // (d, bond code)
+      // the bonds grouped by d, each group after its z_d; t1[c1 ^ m1] of the
+      // high-half and crossing bonds come from the row's neighbour table, in
+      // slots numbered in emission order (crossing bonds of one m1 share a
+      // slot), four per 16-byte load, each load emitted before its first use
+      struct Bond { int cls, t, q, d; uint32_t m0, m1; };
+      std::vector<Bond> bonds;
       std::vector<int> dists;
       for (int cls = 0; cls < 3; ++cls)
         for (int t = 0; t < 2; ++t)
           for (int q = seg[cls * 2 + t]; q < seg[cls * 2 + t + 1]; ++q) {
-            const uint32_t m0 = (uint32_t)words[q], m1 = (uint32_t)(words[q] >> 32);
-            int d = -1;
-            std::string c = coef ? bond_code_pb(cls, m0, m1, q, w0, &d) : bond_code(cls, t, m0, m1, w0, &d);
-            if (d >= 0 && std::find(dists.begin(), dists.end(), d) == dists.end()) dists.push_back(d);
-            code.emplace_back(d, c);
+            Bond bd{cls, t, q, -1, (uint32_t)words[q], (uint32_t)(words[q] >> 32)};
+            flip_test(bd.m0, bd.m1, w0, &bd.d);
+            if (bd.d < 0) continue;  // never flips
+            if (std::find(dists.begin(), dists.end(), bd.d) == dists.end()) dists.push_back(bd.d);
+            bonds.push_back(bd);
           }
+      std::vector<uint32_t> slot_m1;
+      std::map<uint32_t, int> cross_slot;
       std::ostringstream body;
+      std::ostringstream decl;
       for (int d : dists) {
         body << "{ const u32 z" << d << " = s ^ (s >> " << d << "u);\n    ";
-        for (auto& c : code)
-          if (c.first == d) body << c.second;
+        for (const Bond& bd : bonds) {
+          if (bd.d != d) continue;
+          std::string t1v;
+          if (bd.cls != 0) {
+            int k;
+            auto it = bd.cls == 2 ? cross_slot.find(bd.m1) : cross_slot.end();
+            if (it != cross_slot.end()) {
+              k = it->second;
+            } else {
+              k = (int)slot_m1.size();
+              slot_m1.push_back(bd.m1);
+              if (bd.cls == 2) cross_slot[bd.m1] = k;
+              if (k % 4 == 0) body << "Q" << k / 4 << " = tn[" << k / 4 << "];\n    ";
+            }
+            static const char* comp[4] = {".x", ".y", ".z", ".w"};
+            t1v = "Q" + std::to_string(k / 4) + comp[k % 4];
+          }
+          int dd = -1;
+          body << (coef ? bond_code_pb(bd.cls, bd.m0, bd.m1, t1v, bd.q, w0, &dd)
+                        : bond_code(bd.cls, bd.t, bd.m0, bd.m1, t1v, w0, &dd));
+        }
         body << "}\n    ";
       }
+      const int nq = std::max(1, ((int)slot_m1.size() + 3) / 4);
+      for (int k = 0; k < (int)(slot_m1.size() + 3) / 4; ++k) decl << "uint4 Q" << k << ";\n    ";
+      jm.slots = slot_m1;
+      jm.nq = nq;
       std::string kern = coef ? kKernelsPB : kKernels;
       const size_t at = kern.find("BONDS");
-      kern.replace(at, 5, body.str());
+      kern.replace(at, 5, decl.str() + body.str());
       std::string src = std::string(kPrelude) + "#define W0 " + std::to_string(w0) + "\n#define LOWMASK " +
-                        hex((1u << w0) - 1u) + "\n#define NBC " + std::to_string(std::max(1, seg[6])) + "\n" + kern;
+                        hex((1u << w0) - 1u) + "\n#define NBC " + std::to_string(std::max(1, seg[6])) +
+                        "\n#define NQ " + std::to_string(nq) + "\n" + kern;
       const char* opts[] = {"-arch=sm_103a", "-std=c++17", "-default-device"};
       const std::string dir = cache_dir();
       char name[40];
@@ -666,6 +716,29 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   }
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << w0);
   if (budget < 0 || budget >= kJitBudgets) return ed_fail(ED_EINVAL, "unknown register budget");
+  if (h->jit_t1n_key != (const void*)mod) {
+    // this operator's neighbour table for the module's slot order
+    const int K = (int)mod->slots.size();
+    const int64_t nc1 = (int64_t)1 << (b->nspins - w0);
+    const size_t bytes = sizeof(uint32_t) * ((size_t)nc1 * mod->nq * 4 + (size_t)std::max(K, 1));
+    if (h->jit_t1n) cudaFree(h->jit_t1n);
+    h->jit_t1n = nullptr;
+    h->jit_t1n_key = nullptr;
+    if (cudaMalloc(&h->jit_t1n, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      h->jit_t1n = nullptr;
+      return ed_fail(ED_ENOMEM, "neighbour table of the run-time compiled H.v does not fit in device memory");
+    }
+    uint32_t* tab = (uint32_t*)h->jit_t1n;
+    uint32_t* dslots = tab + (size_t)nc1 * mod->nq * 4;
+    if (K > 0)
+      ED_CUDA(cudaMemcpyAsync(dslots, mod->slots.data(), sizeof(uint32_t) * K, cudaMemcpyHostToDevice, ctx->stream));
+    const int gb = (int)std::max<int64_t>(1, std::min<int64_t>(nc1 * mod->nq * 4 / 256 + 1, (int64_t)ctx->num_sms * 8));
+    k_build_t1n<<<gb, 256, 0, ctx->stream>>>(b->d_lin_t1, nc1, dslots, K, mod->nq, tab);
+    ED_CHECK_LAUNCH(ctx);
+    ED_CUDA(cudaStreamSynchronize(ctx->stream));  // the slot list is pageable host memory
+    h->jit_t1n_key = (const void*)mod;
+  }
   const int bg = budget, kd = dot ? 1 : 0, ri = rio ? 1 : 0;
   const int nt = kJitThreads[bg];
   int64_t g = (b->dim + nt - 1) / nt;
@@ -681,10 +754,12 @@ int ed_jit_launch(ed_ham* h, uint64_t signature, int budget, const void* x, void
   const uint32_t* t1 = b->d_lin_t1;
   double c0c = h->bs.chalf[0], c1c = h->bs.chalf[1];
   double* partial = dot ? ctx->d_red : nullptr;
-  void* args_u[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &c0c, &c1c, &partial};
+  const void* t1n = h->jit_t1n;
+  void* args_u[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &t1n, &c0c, &c1c, &partial};
   std::vector<long long> pbc(coef ? std::max(1, seg[6]) : 0, 0ll);  // the PBC parameter's bytes
   if (coef) std::copy(coef, coef + seg[6], pbc.begin());
-  void* args_pb[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &pbexp, &partial, pbc.data(), &coef_dev};
+  void* args_pb[] = {&states, &diag, &x, &xq, &gmax, &sbits, &y, &dim, &t0, &t1, &t1n, &pbexp, &partial, pbc.data(),
+                     &coef_dev};
   void** args = coef ? args_pb : args_u;
   CUresult r = g_drv.launch(mod->fn[bg][kd][ri], (unsigned)nblk, 1, 1, (unsigned)nt, 1, 1, (unsigned)smem,
                             (CUstream)ctx->stream, args, nullptr);

@@ -118,6 +118,10 @@ struct ed_ham {
   const ed_basis* basis = nullptr;
   // batched H.v tile chosen by the autotuner, per batch width (ed_batch.cu)
   std::vector<std::pair<int, int>> batch_tile;
+  // neighbour table of the run-time compiled H.v (ed_hv_jit.cu): t1[c1 ^ m1]
+  // per high half c1 in the module's slot order; jit_t1n_key is the module
+  void* jit_t1n = nullptr;
+  const void* jit_t1n_key = nullptr;
   // reference parameters (uniform mode)
   bool per_bond = false;
   double J1 = 0, D1 = 0, J2 = 0, D2 = 0;
