@@ -305,7 +305,7 @@ int ed_minres(ed_ham* h, double shift, const ed_cplx* rhs_dev, const ed_cplx* q_
   };
   double beta1 = 0.0, t = 0.0;
   int itn = 0;
-  double oldb = 0.0, beta, dbar = 0.0, epsln = 0.0, phibar, cs = -1.0, sn = 0.0, rnorm;
+  double oldb = 0.0, beta, dbar = 0.0, epsln = 0.0, phibar, cs = -1.0, sn = 0.0, rnorm = 0.0;
   MR_CUDA(cudaMemcpyAsync(r1, rhs_dev, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToDevice, ctx->stream));
   if ((rc = project(r1)) != ED_OK) goto done;
   if ((rc = nrm(r1, &t)) != ED_OK) goto done;

@@ -323,7 +323,7 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
       double pre_y2 = 0.0;
       ED_TRY(ed_launch_hv_dot_any(H, e->col_r[j], e->w_r, true, &pre_a, &pre_y2));
       e->nhv++;
-      double nw, norig, wmax;
+      double nw = 0.0, norig = 0.0, wmax = 0.0;
       ED_TRY(orthogonalize_lanczos_r(e, j, k, j > 0 ? beta[j - 1] : 0.0, pre_a.x, pre_y2, h, &nw, &norig, &wmax));
       alpha[j] = h[j];
       if (nw <= 1e-13 * norig) {
@@ -331,7 +331,7 @@ static int eps_solve_real(ed_eps* e, int* nconv_out, int m, int nev, double tol,
         beta[j] = 0.0;
         if (j + 1 < m) {
           ED_TRY(ed_start_vector_r(ctx, rseed++, n, e->w_r));
-          double nw2;
+          double nw2 = 0.0;
           ED_TRY(orthogonalize_r(e, j, &nw2));
           ED_TRY(ed_scale_copy_r(ctx, e->w_r, e->col_r[j + 1], 1.0 / nw2, n));
         } else {
@@ -470,7 +470,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
         ED_TRY(ed_launch_hv(H, e->col[j], e->w));
       }
       e->nhv++;
-      double nw, norig;
+      double nw = 0.0, norig = 0.0;
       ED_TRY(orthogonalize_lanczos(e, j, k, j > 0 ? beta[j - 1] : 0.0, h, &nw, &norig, fused ? &pre_a : nullptr,
                                    pre_y2));
       alpha[j] = h[j].x;
@@ -480,7 +480,7 @@ static int eps_solve_impl(ed_eps* e, int* nconv_out) {
         if (j + 1 < m) {
           ED_TRY(ed_start_vector(ctx, rseed++, n, e->w, e->real_coeffs));
           std::vector<double2> h2;
-          double nw2, no2;
+          double nw2 = 0.0, no2 = 0.0;
           ED_TRY(orthogonalize(e, j, h2, &nw2, &no2));
           ED_TRY(ed_scale_copy(ctx, e->w, e->col[j + 1], 1.0 / nw2, n));
         } else {

@@ -281,7 +281,7 @@ int ed_update(ed_ctx* ctx, const double2* const* cols, int nv, const double2* h_
   if (real) k_update<true><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, nblk);
   else k_update<false><<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(cp, nv, h_dev, w, n, ctx->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
-  double out;
+  double out = 0.0;
   ED_TRY(ed_finish_reduce(ctx, 1, nblk, &out));
   if (wnorm2_host) *wnorm2_host = out;
   return ED_OK;
@@ -381,7 +381,7 @@ int ed_residual_norm2(ed_ctx* ctx, const double2* hx, const double2* x, double t
   ED_TRY(ed_ensure_reduce(ctx, (size_t)2 * nblk + 2));
   k_residual<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(hx, x, theta, n, ctx->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
-  double out[2];
+  double out[2] = {0.0, 0.0};
   ED_TRY(ed_finish_reduce(ctx, 2, nblk, out));
   *r2_host = out[0];
   *x2_host = out[1];
@@ -647,7 +647,7 @@ int ed_update_r(ed_ctx* ctx, const double* const* cols, int nv, const double* h_
   } else {
     ED_TRY(rc);
   }
-  double out[2];
+  double out[2] = {0.0, 0.0};
   ED_TRY(ed_finish_reduce(ctx, items, nblk, out, items - 1));
   if (wnorm2_host) *wnorm2_host = out[0];
   if (wmax_host) *wmax_host = out[1];
@@ -1049,7 +1049,7 @@ int ed_residual_norm2_r(ed_ctx* ctx, const double* hx, const double* x, double t
   ED_TRY(ed_ensure_reduce(ctx, (size_t)2 * nblk + 2));
   k_residual_r<<<nblk, ED_RED_THREADS, 0, ctx->stream>>>(hx, x, theta, n, ctx->d_red, nblk);
   ED_CHECK_LAUNCH(ctx);
-  double out[2];
+  double out[2] = {0.0, 0.0};
   ED_TRY(ed_finish_reduce(ctx, 2, nblk, out));
   *r2_host = out[0];
   *x2_host = out[1];
