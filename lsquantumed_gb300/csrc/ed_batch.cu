@@ -34,10 +34,6 @@ struct ed_batch {
   size_t red_cap = 0;
   double* h_red = nullptr;
   int restart_arith = ED_RESTART_AUTO;  // ed_batch_set_restart_arithmetic
-  // d_xq / d_gmax already hold the fixed-point copy of this [dim][xq_b] block
-  // (k_batch_scale_quantize); the next batched H.v of it uses them once
-  const void* xq_src = nullptr;
-  int xq_b = 0;
   int hv_variant = -1;  // batched H.v launch variant (-1: autotune at the next real-storage H.v)
   bool hv_forced = false;
 };
@@ -518,22 +514,6 @@ __global__ void k_batch_scale(const double* __restrict__ src, double* __restrict
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k] * s[k % B];
 }
 
-// The same scaling and, in the same pass, the fixed-point copy of dst for the
-// next batched H.v (k_batch_quantize_r's values) with the largest exponent
-// emax found on the host from the per-realisation maxima.
-__global__ void k_batch_scale_quantize(const double* __restrict__ src, double* __restrict__ dst,
-                                       const double* __restrict__ s, int64_t dim, int B, int emax, int sbits,
-                                       long long* __restrict__ xq, int* __restrict__ gmax) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) gmax[0] = emax;
-  const int64_t n = dim * B;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    const double v = src[k] * s[k % B];
-    dst[k] = v;
-    xq[k] = batch_fx64_entry(v, emax, sbits);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Device-side steps of the batched expansion: the per-realisation
 // coefficients (the local Lanczos pair, the Gram-Schmidt dots, the norms, the
@@ -633,9 +613,11 @@ __global__ void __launch_bounds__(256) k_bx_scale(int A, int j, int m1, BxState 
   }
 }
 
-// k_batch_scale_quantize with emax and its validity from the device: where
-// the exponent is not determined, only the scaled vector is written and the
-// next batched H.v quantizes it itself.
+// dst = src * s per realisation and, in the same pass, the fixed-point copy
+// of dst for the next batched H.v (k_batch_quantize_r's values) with the
+// largest exponent from the device (k_bx_scale): where that exponent is not
+// determined, only the scaled vector is written and the next batched H.v
+// quantizes it itself.
 __global__ void k_bx_scale_quantize(const double* __restrict__ src, double* __restrict__ dst,
                                     const double* __restrict__ s, int64_t dim, int B, int sbits,
                                     long long* __restrict__ xq, int* __restrict__ gmax, BxState st) {
@@ -863,7 +845,6 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
   const int64_t n = bt->dim * B;
   const int sbits = batch_sbits(bt);
   if (rs && dev) {
-    bt->xq_src = nullptr;
     k_bx_prequant<<<1, 1, 0, ctx->stream>>>(bt->d_gmax, dev->xq_valid);
     ED_CHECK_LAUNCH(ctx);
     k_batch_maxexp_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, dev->xq_valid);
@@ -871,11 +852,7 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
     k_batch_quantize_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax, sbits,
                                                                  (long long*)bt->d_xq, dev->xq_valid);
     ED_CHECK_LAUNCH(ctx);
-  } else if (rs && bt->xq_src == x && bt->xq_b == B) {
-    // made with x by k_batch_scale_quantize: use it once
-    bt->xq_src = nullptr;
   } else if (rs) {
-    bt->xq_src = nullptr;
     ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
     k_batch_maxexp_r<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double*)x, n, bt->d_gmax);
     ED_CHECK_LAUNCH(ctx);
@@ -883,7 +860,6 @@ static int batch_hv(ed_batch* bt, int B, const double* diag, const void* x, void
                                                                  (long long*)bt->d_xq);
     ED_CHECK_LAUNCH(ctx);
   } else {
-    bt->xq_src = nullptr;
     ED_CUDA(cudaMemsetAsync(bt->d_gmax, 0, sizeof(int), ctx->stream));
     k_batch_maxexp<<<grid_n(ctx, n), 256, 0, ctx->stream>>>((const double2*)x, n, bt->d_gmax);
     ED_CHECK_LAUNCH(ctx);
@@ -1157,7 +1133,7 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
   int cur = 0;  // dg[cur] holds the active realisations' diagonals
   int rc = ED_OK;
-  std::vector<double> out, wmax;
+  std::vector<double> out;
   std::vector<double> alpha((size_t)B * (m + 1)), beta((size_t)B * (m + 1)), arrow((size_t)B * (m + 1));
   std::vector<int> act(B), nconv(B, 0);
   for (int b = 0; b < B; ++b) act[b] = b;
@@ -1423,7 +1399,6 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
 cleanup:
   cudaStreamSynchronize(ctx->stream);
-  bt->xq_src = nullptr;  // made with a column of the pool freed here
   cudaFree(st_buf);
   cudaFree(st_int);
   cudaFree(pool);
