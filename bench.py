@@ -361,9 +361,10 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     from mt19937_64(seed) (RandomDisorder::hi_init with srand_seq[k] = seed),
     Sz = 0, 1, 2, lowest 2 pairs at eps_tol 1e-9.  Batched: one batch per
     sector over all `seeds`, the three sectors solved at once (solve_batches:
-    one environment, host thread and stream per sector), timed on the host
-    around the call; the same batches one sector after another are timed
-    beside it.  Plain: the same solves one at a time
+    one environment, host thread and stream per sector; expansion sweeps
+    replayed from CUDA graphs), timed on the host around the call; the same
+    batches one sector after another, and at once with direct launches, are
+    timed beside it.  Plain: the same solves one at a time
     for `plain_sample` seeds per sector spread over the whole seed range
     (every restart tile of the batch), timed per solve, eigenvalues checked
     against the batch at 1e-8."""
@@ -388,11 +389,12 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     brestart = restart if restart in ('auto', 'fp64', 'pair') else 'auto'
     kcount = lambda: sum(e.kernel_count() for e in envs.values())
 
-    def batched(concurrent):
+    def batched(concurrent, graphs=False):
         bts = []
         for mag in sectors:
             bt = ed.DisorderBatch(hams[mag][1], fields)
             bt.set_restart_arithmetic(brestart)
+            bt.set_graphs(graphs)
             bts.append(bt)
         torch.cuda.synchronize()
         k0 = kcount()
@@ -405,8 +407,9 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
         t = time.perf_counter() - t0
         return t, kcount() - k0, rs, [list(bt.hv_tile()) for bt in bts]
 
-    t_seq, _, rs_seq, _ = batched(False)
-    t_batch, launches, rs, tiles = batched(True)
+    t_seq, _, rs_seq, _ = batched(False, graphs=True)
+    t_direct, _, rs_direct, _ = batched(True, graphs=False)
+    t_batch, launches, rs, tiles = batched(True, graphs=True)
     max_err = max(float(r['errs'].max()) for r in rs)
     bad = sum(int((r['nconv'] < nev).sum()) for r in rs)
     its = [r['its'] for r in rs]
@@ -440,6 +443,9 @@ def disorder_sweep(ed, env, seeds, restart='auto', plain_sample=16):
     return {'batched_samples_per_s': nsolve / t_batch, 'plain_samples_per_s': 1.0 / t_plain,
             'batched_over_plain': (nsolve / t_batch) * t_plain, 'batched_seconds': t_batch, 'solves': nsolve,
             'sectors_at_once': True, 'batched_one_sector_at_a_time_samples_per_s': nsolve / t_seq,
+            'cuda_graphs': True, 'batched_direct_launches_samples_per_s': nsolve / t_direct,
+            'direct_launches_eigenvalues_agree_1e-12': bool(all(np.allclose(a['evals'], b['evals'], rtol=1e-12, atol=0)
+                                                              for a, b in zip(rs, rs_direct))),
             'eigenvalues_agree_with_one_sector_at_a_time_1e-12': bool(same_seq),
             'max_rel_residual': max_err, 'plain_max_rel_residual': perr, 'unconverged': bad,
             'restarts_per_sector': its, 'gpu_launches': launches, 'restart_arithmetic': restart,

@@ -304,6 +304,17 @@ int ed_batch_stats(ed_batch* bt, int* its, int64_t* n_hv);
  * another). */
 int ed_batch_solve_many(ed_batch* const* bts, int count, int nev, int ncv, double tol, int max_it, uint64_t seed,
                         double* const* evals_host, double* const* errs_host, int* const* nconv_host);
+/* CUDA graphs for the batched solve: with on != 0 (the default), every
+ * expansion sweep after the first (which tunes the batched H.v and sizes the
+ * buffers) is captured from the batch's stream into a CUDA graph and
+ * launched from it.  The sweep has no host round trip, so the graph holds
+ * all of its kernels; the results are those of direct launches bit for bit.
+ * A sweep's columns change at every restart, so each graph is captured and
+ * instantiated once.  on = 0 launches the kernels directly.
+ * ed_batch_graph_sweeps reports how many sweeps of the last solve ran from
+ * a graph.  No counterpart in the reference. */
+int ed_batch_set_graphs(ed_batch* bt, int on);
+int ed_batch_graph_sweeps(const ed_batch* bt, int64_t* n);
 /* Tile of the batched H.v: rows of the basis per CTA tile (4, 8, 16, 32)
  * and threads per CTA (128, 256; the realisation columns are spread over
  * them).  (0, 0) re-enables the autotuner, which times every tile once at the

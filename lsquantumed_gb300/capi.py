@@ -89,6 +89,8 @@ SIGNATURES = {
     'ed_bv_dot_real': [vp, vp, i32, vp, i64, i32, vp],
     'ed_batch_set_restart_arithmetic': [vp, i32],
     'ed_batch_set_hv_tile': [vp, i32, i32],
+    'ed_batch_set_graphs': [vp, i32],
+    'ed_batch_graph_sweeps': [vp, P(i64)],
     'ed_batch_hv_tile': [vp, P(i32), P(i32)],
     'ed_eps_set_initial_vector': [vp, vp, i32],
     'ed_eps_solve': [vp, P(i32)],

@@ -36,6 +36,9 @@ struct ed_batch {
   int restart_arith = ED_RESTART_AUTO;  // ed_batch_set_restart_arithmetic
   int hv_variant = -1;  // batched H.v launch variant (-1: autotune at the next real-storage H.v)
   bool hv_forced = false;
+  bool graphs = true;  // capture each expansion sweep after the first in a CUDA graph
+  cudaStream_t stream = nullptr;  // the solve's own stream (ordered with the context's by events)
+  int64_t graph_sweeps = 0;  // sweeps run from a captured graph in the last solve
 };
 
 // Per-realisation diagonal, exactly as build_disorder computes it:
@@ -1039,6 +1042,7 @@ int ed_batch_destroy(ed_batch* bt) {
   if (bt->d_vecs) cudaFree(bt->d_vecs);
   if (bt->d_red) cudaFree(bt->d_red);
   if (bt->h_red) cudaFreeHost(bt->h_red);
+  if (bt->stream) cudaStreamDestroy(bt->stream);
   delete bt;
   return ED_OK;
 }
@@ -1064,9 +1068,43 @@ int ed_batch_diag_host(ed_batch* bt, double* out_host) {
 // realisations whose nev pairs converged save their Ritz vectors and leave
 // the active block, which is packed to the remaining A columns, so the work
 // follows the sum of the realisations' iterations, not B times the slowest.
+static int batch_solve_impl(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed,
+                            double* evals_host, double* errs_host, int* nconv_host);
+
+// The solve runs on the batch's own non-blocking stream, ordered after the
+// context stream's earlier work and before its later work by events: batches
+// of different environments then overlap on the device even when the
+// environments use the legacy default stream, and a sweep can be captured in
+// a CUDA graph (the legacy stream cannot be captured).
 int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed, double* evals_host,
                    double* errs_host, int* nconv_host) {
   if (!bt || !evals_host || !errs_host || !nconv_host) return ed_fail(ED_EINVAL, "null argument");
+  ed_ctx* ctx = bt->h->ctx;
+  if (!bt->stream) ED_CUDA(cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking));
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  ED_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+  if (cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess) {
+    cudaEventDestroy(ev_in);
+    return ed_cuda_fail(cudaGetLastError(), "cudaEventCreate", __FILE__, __LINE__);
+  }
+  cudaStream_t outer = ctx->stream;
+  int rc = ED_OK;
+  if (cudaEventRecord(ev_in, outer) != cudaSuccess || cudaStreamWaitEvent(bt->stream, ev_in, 0) != cudaSuccess) {
+    rc = ed_cuda_fail(cudaGetLastError(), "stream ordering", __FILE__, __LINE__);
+  } else {
+    ctx->stream = bt->stream;
+    rc = batch_solve_impl(bt, nev, ncv, tol, max_it, seed, evals_host, errs_host, nconv_host);
+    ctx->stream = outer;
+    if (cudaEventRecord(ev_out, bt->stream) != cudaSuccess || cudaStreamWaitEvent(outer, ev_out, 0) != cudaSuccess)
+      if (rc == ED_OK) rc = ed_cuda_fail(cudaGetLastError(), "stream ordering", __FILE__, __LINE__);
+  }
+  cudaEventDestroy(ev_in);
+  cudaEventDestroy(ev_out);
+  return rc;
+}
+
+static int batch_solve_impl(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint64_t seed,
+                            double* evals_host, double* errs_host, int* nconv_host) {
   ed_ctx* ctx = bt->h->ctx;
   const int64_t dim = bt->dim;
   const int B = bt->B;
@@ -1133,6 +1171,8 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
   }
   int cur = 0;  // dg[cur] holds the active realisations' diagonals
   int rc = ED_OK;
+  bool capturing = false;  // the stream is capturing an expansion sweep
+  bt->graph_sweeps = 0;
   std::vector<double> out;
   std::vector<double> alpha((size_t)B * (m + 1)), beta((size_t)B * (m + 1)), arrow((size_t)B * (m + 1));
   std::vector<int> act(B), nconv(B, 0);
@@ -1159,7 +1199,23 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     ++its;
     const int64_t colA = dim * (int64_t)A;
     // the expansion sweep runs without a host round trip: the coefficients
-    // live in the device state (st), alpha and beta come back after it
+    // live in the device state (st), alpha and beta come back after it.
+    // With graphs on, the sweeps after the first (which tunes the H.v and
+    // sizes the buffers) are captured in a CUDA graph and replayed once.
+    bool capture = bt->graphs && its > 1;
+    if (capture) {
+      const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(dim / 64 + 1, (int64_t)ctx->num_sms * 4));
+      const size_t nd = (size_t)m * A;
+      const size_t need = std::max({(nd + A) * nblk + nd, (size_t)2 * A * nblk + 2 * (size_t)A,
+                                    (size_t)2 * A * ((size_t)ctx->num_sms * 64) + 2 * (size_t)A});
+      if ((rc = batch_reduce_buf(bt, need)) != ED_OK) goto cleanup;
+      if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        capture = false;  // run this sweep directly
+      } else {
+        capturing = true;
+      }
+    }
     for (int j = k; j < m; ++j) {
       const double* res_hv = nullptr;
       if ((rc = batch_hv(bt, A, dg[cur], col[j], w, true, nullptr, &st, &res_hv)) != ED_OK) goto cleanup;
@@ -1210,6 +1266,22 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
       k_bx_scale_quantize<<<grid_n(ctx, colA), 256, 0, ctx->stream>>>(w, col[j + 1], d_coef, dim, A, batch_sbits(bt),
                                                                      (long long*)bt->d_xq, bt->d_gmax, st);
       ED_CHECK_LAUNCH(ctx);
+    }
+    if (capture) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      capturing = false;
+      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+      if (ce == cudaSuccess) ce = cudaGraphLaunch(exec, ctx->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        rc = ed_cuda_fail(ce, "CUDA graph of an expansion sweep", __FILE__, __LINE__);
+        goto cleanup;
+      }
+      bt->graph_sweeps++;
     }
     {
       // alpha and beta of this sweep's steps back to the host
@@ -1398,6 +1470,12 @@ int ed_batch_solve(ed_batch* bt, int nev, int ncv, double tol, int max_it, uint6
     }
   }
 cleanup:
+  if (capturing) {  // an error inside a captured sweep: close the capture
+    cudaGraph_t graph = nullptr;
+    cudaStreamEndCapture(ctx->stream, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+  }
   cudaStreamSynchronize(ctx->stream);
   cudaFree(st_buf);
   cudaFree(st_int);
@@ -1454,6 +1532,18 @@ int ed_batch_get_eigenvector(ed_batch* bt, int b, int i, ed_cplx* vec_dev) {
   k_batch_extract<<<grid_n(ctx, bt->dim), 256, 0, ctx->stream>>>(bt->d_vecs + (size_t)i * bt->dim * bt->B, bt->dim,
                                                                 bt->B, b, (double2*)vec_dev);
   ED_CHECK_LAUNCH(ctx);
+  return ED_OK;
+}
+
+int ed_batch_set_graphs(ed_batch* bt, int on) {
+  if (!bt) return ed_fail(ED_EINVAL, "null batch");
+  bt->graphs = on != 0;
+  return ED_OK;
+}
+
+int ed_batch_graph_sweeps(const ed_batch* bt, int64_t* n) {
+  if (!bt || !n) return ed_fail(ED_EINVAL, "null argument");
+  *n = bt->graph_sweeps;
   return ED_OK;
 }
 

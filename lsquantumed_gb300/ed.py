@@ -617,6 +617,17 @@ class DisorderBatch:
         threads per CTA (128, 256); (0, 0) re-enables the autotuner."""
         call('ed_batch_set_hv_tile', self._h, int(rows), int(threads))
 
+    def set_graphs(self, on=True):
+        """Capture every expansion sweep after the first in a CUDA graph
+        (ed_batch_set_graphs; on by default, False launches directly)."""
+        call('ed_batch_set_graphs', self._h, 1 if on else 0)
+
+    def graph_sweeps(self):
+        """Sweeps of the last solve that ran from a CUDA graph."""
+        n = ctypes.c_int64()
+        call('ed_batch_graph_sweeps', self._h, ctypes.byref(n))
+        return n.value
+
     def hv_tile(self):
         """(rows, threads) of the batched H.v tile in use; (0, 0) before the
         autotuner has run."""

@@ -166,6 +166,26 @@ def test_solve_batches_concurrent(ed):
         ed.solve_batches([bts[0], ed.DisorderBatch(bts[0].hamilt, fields)], nev=nev)
 
 
+def test_batch_cuda_graphs(ed):
+    """Expansion sweeps replayed from CUDA graphs (ed_batch_set_graphs, the
+    default) give the results of direct launches bit for bit with the same
+    H.v tile, and the sweeps after the first run from graphs."""
+    N, mag, B, nev = 14, 1, 40, 2
+    env, b, h, fields = _setup(ed, N, mag, B, seed0=90)
+    res = {}
+    for g in (False, True):
+        bt = ed.DisorderBatch(h, fields)
+        bt.set_hv_tile(8, 256)
+        bt.set_graphs(g)
+        r = bt.solve(nev=nev, ncv=12, tol=1e-10, seed=3)
+        assert np.all(r['nconv'] >= nev) and np.all(r['errs'] <= 1e-10)
+        res[g] = (r, bt.graph_sweeps())
+    assert res[False][1] == 0 and res[True][1] >= 1, (res[False][1], res[True][1])
+    assert res[True][1] == res[True][0]['its'] - 1
+    assert np.array_equal(res[True][0]['evals'].view(np.uint64), res[False][0]['evals'].view(np.uint64))
+    assert res[True][0]['its'] == res[False][0]['its'] and res[True][0]['nhv'] == res[False][0]['nhv']
+
+
 def test_batch_rejects_bad_input(ed):
     env, b, h, fields = _setup(ed, 8, 0, 2)
     with pytest.raises(ValueError):
