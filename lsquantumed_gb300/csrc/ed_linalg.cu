@@ -692,11 +692,17 @@ __device__ __forceinline__ long long ed_fx62(double v, bool& bad) {
   return (bits >> 63) ? -(long long)a : (long long)a;
 }
 
-#define RS_NF 4  // outputs per group formed in FP64; the other 8 - RS_NF in integers
-
+// NF outputs of a group in FP64 and the next NI in integers (NF + NI <= 8).
+// A full group of eight takes 4 + 4, which keeps both units busy (3 + 5 and
+// 4 + 4 measured the same; 2 + 6 and fewer FP64 outputs were slower).  A
+// partial last group computes only the outputs it stores: one or two in FP64
+// alone (an integer output of its own would pay the conversion of every input
+// for one product), three or more split as evenly as the FP64 side allows.
+template <int NF, int NI>
 __global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, const double* __restrict__ Yd,
-                                                     const long long* __restrict__ Yq, int c0, int nc,
+                                                     const long long* __restrict__ Yq, int c0,
                                                      const ColPtrs outp, int64_t n) {
+  static_assert(NF >= 1 && NI >= 0 && NF + NI <= 8, "group of at most eight outputs");
   __shared__ double shY[128 * 8];     // m x 8 coefficients of this group (FP64 columns)
   __shared__ long long shQ[128 * 8];  // the same, 62-bit fixed point (integer columns)
   for (int k = threadIdx.x; k < m * 8; k += blockDim.x) {
@@ -706,41 +712,65 @@ __global__ void __launch_bounds__(256) k_restart_mix(const ColPtrsR cp, int m, c
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    double a[RS_NF];
-    unsigned long long lo[8 - RS_NF];
-    long long hi[8 - RS_NF];
+    double a[NF];
+    unsigned long long lo[NI > 0 ? NI : 1];
+    long long hi[NI > 0 ? NI : 1];
 #pragma unroll
-    for (int c = 0; c < RS_NF; ++c) a[c] = 0.0;
+    for (int c = 0; c < NF; ++c) a[c] = 0.0;
 #pragma unroll
-    for (int c = 0; c < 8 - RS_NF; ++c) { lo[c] = 0ull; hi[c] = 0ll; }
+    for (int c = 0; c < NI; ++c) { lo[c] = 0ull; hi[c] = 0ll; }
     bool bad = false;
     for (int i = 0; i < m; ++i) {
       const double vd = cp.p[i][r];
-      const long long v = ed_fx62(vd, bad);
 #pragma unroll
-      for (int c = 0; c < RS_NF; ++c) a[c] = fma(vd, shY[i * 8 + c], a[c]);
+      for (int c = 0; c < NF; ++c) a[c] = fma(vd, shY[i * 8 + c], a[c]);
+      if (NI > 0) {
+        const long long v = ed_fx62(vd, bad);
 #pragma unroll
-      for (int c = 0; c < 8 - RS_NF; ++c) {
-        const long long y = shQ[i * 8 + RS_NF + c];
-        const unsigned long long pl = (unsigned long long)v * (unsigned long long)y;
-        const long long ph = __mul64hi(v, y);
-        const unsigned long long s = lo[c] + pl;
-        hi[c] += ph + (s < pl ? 1 : 0);
-        lo[c] = s;
+        for (int c = 0; c < NI; ++c) {
+          const long long y = shQ[i * 8 + NF + c];
+          const unsigned long long pl = (unsigned long long)v * (unsigned long long)y;
+          const long long ph = __mul64hi(v, y);
+          const unsigned long long s = lo[c] + pl;
+          hi[c] += ph + (s < pl ? 1 : 0);
+          lo[c] = s;
+        }
       }
     }
 #pragma unroll
-    for (int c = 0; c < RS_NF; ++c)
-      if (c < nc) ((double*)outp.p[c0 + c])[r] = a[c];
+    for (int c = 0; c < NF; ++c) ((double*)outp.p[c0 + c])[r] = a[c];
 #pragma unroll
-    for (int c = 0; c < 8 - RS_NF; ++c) {
-      if (RS_NF + c < nc) {
-        // (hi * 2^64 + lo) * 2^-124
-        double d = fma((double)hi[c], 0x1p-60, (double)lo[c] * 0x1p-124);
-        if (bad) d = __longlong_as_double(0x7FF8000000000000ll);
-        ((double*)outp.p[c0 + RS_NF + c])[r] = d;
-      }
+    for (int c = 0; c < NI; ++c) {
+      // (hi * 2^64 + lo) * 2^-124
+      double d = fma((double)hi[c], 0x1p-60, (double)lo[c] * 0x1p-124);
+      if (bad) d = __longlong_as_double(0x7FF8000000000000ll);
+      ((double*)outp.p[c0 + NF + c])[r] = d;
     }
+  }
+}
+
+// One group of nc outputs (1..8) with the split above.
+static int restart_mix_launch(ed_ctx* ctx, const ColPtrsR& cp, int m, const double* dYd, const long long* dYq, int c0,
+                              int nc, const ColPtrs& op, int64_t n) {
+  auto go = [&](auto kern) -> int {
+    int per_sm = 0;
+    ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    if (per_sm < 1) per_sm = 1;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
+    kern<<<g, 256, 0, ctx->stream>>>(cp, m, dYd, dYq, c0, op, n);
+    ED_CHECK_LAUNCH(ctx);
+    return ED_OK;
+  };
+  switch (nc) {
+    case 1: return go(k_restart_mix<1, 0>);
+    case 2: return go(k_restart_mix<2, 0>);
+    case 3: return go(k_restart_mix<2, 1>);
+    case 4: return go(k_restart_mix<2, 2>);
+    case 5: return go(k_restart_mix<3, 2>);
+    case 6: return go(k_restart_mix<3, 3>);
+    case 7: return go(k_restart_mix<4, 3>);
+    case 8: return go(k_restart_mix<4, 4>);
+    default: return ed_fail(ED_EINVAL, "restart group of " + std::to_string(nc) + " outputs");
   }
 }
 
@@ -1014,15 +1044,8 @@ int ed_restart_combine_r(ed_ctx* ctx, const double* const* cols, int m, const do
   long long* dYq = (long long*)(ctx->d_red + ngroups * per);
   ED_CUDA(cudaMemcpyAsync(dYd, yd.data(), sizeof(double) * yd.size(), cudaMemcpyHostToDevice, ctx->stream));
   ED_CUDA(cudaMemcpyAsync(dYq, yq.data(), sizeof(long long) * yq.size(), cudaMemcpyHostToDevice, ctx->stream));
-  int per_sm = 0;
-  ED_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_restart_mix, 256, 0));
-  if (per_sm < 1) per_sm = 1;
-  int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * per_sm));
-  for (int gi = 0; gi < ngroups; ++gi) {
-    const int nc = std::min(8, l - gi * 8);
-    k_restart_mix<<<g, 256, 0, ctx->stream>>>(cp, m, dYd + gi * per, dYq + gi * per, gi * 8, nc, op, n);
-    ED_CHECK_LAUNCH(ctx);
-  }
+  for (int gi = 0; gi < ngroups; ++gi)
+    ED_TRY(restart_mix_launch(ctx, cp, m, dYd + gi * per, dYq + gi * per, gi * 8, std::min(8, l - gi * 8), op, n));
   // the host coefficients must outlive the copies
   ED_CUDA(cudaStreamSynchronize(ctx->stream));
   return ED_OK;

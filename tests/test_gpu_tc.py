@@ -7,7 +7,8 @@ restatement of its arithmetic in exact integers (quantisation per 128-row
 tile, slice levels, one rounding); against FP64 (numpy) within 2^-52 of the
 largest output norm-wise; and inside the eigensolve against the FP64 restart
 (eigenvalues 1e-12 relative, residuals <= tol, orthonormal Ritz vectors) and
-the reference's golden eigenvalues (1e-12).
+the reference's golden eigenvalues (1e-12).  The default FP64 restart is
+checked beside them for every size of a partial last group of outputs.
 """
 import numpy as np
 import pytest
@@ -68,6 +69,26 @@ def test_exact_restart_bit_exact(ed, env, n, m, l):
     got = _check(ed, env, V, Y)
     ref = Y.T @ V
     assert np.linalg.norm(got - ref) <= 2.0 ** -52 * max(1.0, np.linalg.norm(ref)), (n, m, l)
+
+
+@pytest.mark.parametrize('m', [16, 5])
+@pytest.mark.parametrize('l', [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16, 17])
+def test_fp64_restart_groups(ed, env, m, l):
+    """The default restart combination (FP64 FMA beside exact integer
+    products, arith='fp64') for every size of the last group of eight
+    outputs: each output within an FMA chain's bound of the exact value,
+    2^-49 sum_i |V_i Y_ic|, plus the 62-bit quantisation of the integer
+    columns, m 2^-62 (orthonormal V and Y, so every entry is at most 1)."""
+    rng = np.random.default_rng(100 * m + l)
+    n = 3001
+    V = _orth(rng, n, m).T.copy()
+    Y = _orth(rng, m, m)[:, :min(l, m)]
+    Y = np.hstack([Y] * ((l + m - 1) // m))[:, :l].copy()
+    got = _run(ed, env, V, Y, arith='fp64')
+    ref = (Y.T.astype(np.longdouble) @ V.astype(np.longdouble))
+    scale = np.abs(Y.T) @ np.abs(V)
+    err = np.abs(got.astype(np.longdouble) - ref).astype(np.float64)
+    assert (err <= 2.0 ** -49 * scale + m * 2.0 ** -62).all(), (np.argwhere(err > 2.0 ** -49 * scale)[:5], err.max())
 
 
 def test_exact_restart_dynamic_range_zeros_nan(ed, env):
