@@ -665,6 +665,46 @@ def run_hv_only(args):
     return 0
 
 
+def run_sisj_only(args):
+    """Time the all-pairs <S_i.S_j> and <S^z_i S^z_j> measurements alone on a
+    seeded random real state of the workload's sector (the solver's
+    eigenvectors are real): K calls after W warm-up calls, each call all N^2
+    pairs (N (N + 1) / 2 evaluated, the rest mirrored)."""
+    import numpy as np
+    import torch
+    from lsquantumed_gb300.build import build
+    build()
+    import lsquantumed_gb300 as ed
+    wl = args.workload
+    ltype, N, lx, ly, J1, D1, J2, D2, mag, nev, ncv, tol = WORKLOADS[wl]
+    env = ed.Environment(nspins=N)
+    b = ed.Basis(env, mag)
+    g = torch.Generator(device='cuda')
+    g.manual_seed(5)
+    psi = torch.randn(b.size, dtype=torch.float64, device='cuda', generator=g)
+    psi /= torch.linalg.vector_norm(psi)
+    psi = psi.to(torch.complex128)
+    out = {'mode': 'sisj-only', 'workload': wl, 'dim': b.size, 'pairs': N * N, 'evaluated': N * (N + 1) // 2}
+    for name, cls in (('SiSj', ed.SiSj), ('SzSz', ed.SzSz)):
+        corr = cls(env, b)
+        for _ in range(args.warmup):
+            corr.AllPairs(psi)
+        torch.cuda.synchronize()
+        k0 = env.kernel_count()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            C = corr.AllPairs(psi)
+        torch.cuda.synchronize()
+        sec = (time.perf_counter() - t0) / args.steps
+        out[name] = {'s_per_all_pairs': sec, 'launches_per_call': (env.kernel_count() - k0) / args.steps,
+                     'trace': float(np.real(np.trace(C))), 'c01': float(np.real(C[0, 1]))}
+    # one FP64 FMA per evaluated off-diagonal pair and basis state (the flip part)
+    offd = N * (N - 1) // 2
+    out['SiSj']['fp64_fma_per_s'] = offd * b.size / out['SiSj']['s_per_all_pairs']
+    print(json.dumps(out))
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -991,6 +1031,8 @@ def main():
                     help='--hv-only on real vectors in real storage (float64, as inside the solve)')
     ap.add_argument('--variant', default='auto', help='--hv-only: force an H.v launch variant (default: autotuner)')
     ap.add_argument('--hv-only', action='store_true', help='time the H.v kernel alone')
+    ap.add_argument('--sisj-only', action='store_true',
+                    help='time the all-pairs <S_i.S_j> / <S^z_i S^z_j> measurements alone on a random real state')
     ap.add_argument('--seeds', type=int, default=512, help='disorder seeds (c3)')
     ap.add_argument('--cpu-seeds', type=int, default=4, help='seeds of the C3 CPU baseline sample (x 3 sectors)')
     ap.add_argument('--plain-sample', type=int, default=16, help='seeds per sector solved one at a time (c3)')
@@ -1002,6 +1044,8 @@ def main():
         return run_reference(args)
     if args.hv_only:
         return run_hv_only(args)
+    if args.sisj_only:
+        return run_sisj_only(args)
     if args.probe_rates:
         from lsquantumed_gb300.build import build
         build()

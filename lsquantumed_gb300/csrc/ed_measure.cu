@@ -10,6 +10,7 @@
 #include "ed_internal.h"
 #include "ed_device.cuh"
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #define MEAS_G 8
@@ -136,10 +137,255 @@ static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t
   return ED_OK;
 }
 
+// Real psi and a symmetric operator (S^z_i S^z_j or S_i.S_j): the solver's
+// eigenvectors and the all-pairs measurement.  The general kernel above spends
+// about four FP64 operations per pair and row, and GB300 runs FP64 at a small
+// fraction of its other rates: at N=30 that pass is FP64-bound.  Here
+//  * the S^z S^z part, 0.25 sum_r w_r sigma_i sigma_j with w_r = psi_r^2, is
+//    summed in 64-bit integers: w_r in fixed point once per call (scale
+//    2^(60 - e) with sum_r w_r < 2^e, so no sum can overflow), then one
+//    integer add or subtract per pair and row; each sum is exact and rounded
+//    once;
+//  * the flip part (S+_i S-_j + S-_i S+_j) / 2 pairs every antiparallel row
+//    with its partner r' = rank(s ^ m) (an involution), so it equals
+//    sum over the rows with bit i set and bit j clear of psi_r psi_r': one
+//    FP64 FMA per pair and row, half the gathers;
+//  * psi is read as 8-byte real parts from a compact copy;
+//  * the row's own rank r = T0[s_lo] + T1[s_hi] gives both halves, so a flip
+//    inside the low bits needs no T1 load and one inside the high bits no T0
+//    lookup;
+//  * a row's gathers are issued together: each is predicated on its own
+//    condition, with no branch between them, and a row that does not
+//    contribute adds zero.
+struct PairMasks {
+  int n;
+  uint32_t diag;         // bit g: pair g has i == j
+  uint32_t m[MEAS_GR];   // (1 << i) | (1 << j)
+  uint32_t bi[MEAS_GR];  // 1 << i
+  uint32_t ml[MEAS_GR];  // m & (2^w0 - 1)
+  uint32_t mh[MEAS_GR];  // m >> w0
+};
+
+template <int NV>
+__device__ __forceinline__ void ed_block_reduce_i64(long long (&v)[NV], long long* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    long long a = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) sh[k * 32 + wid] = a;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      long long a = lane < nw ? sh[k * 32 + lane] : 0ll;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      v[k] = a;
+    }
+  }
+}
+
+// partial[(2 g) nblk + blk]: flip sum of pair g (FP64); partial[(2 g + 1)
+// nblk + blk]: its S^z S^z sum in fixed point (int64 bits), times 4 in the
+// units of the final result.
+template <int OP>
+__global__ void __launch_bounds__(256, 2) k_expect_sym_r(const uint32_t* __restrict__ states,
+                                                      const double* __restrict__ pr,
+                                                      const long long* __restrict__ wqv, int64_t dim,
+                                                      const uint16_t* __restrict__ t0,
+                                                      const uint32_t* __restrict__ t1, int w0, const PairMasks pm,
+                                                      double* __restrict__ partial, int nblk) {
+  extern __shared__ uint16_t t0s[];
+  for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
+  __syncthreads();
+  double fl[MEAS_GR];
+  long long zz[MEAS_GR];
+#pragma unroll
+  for (int k = 0; k < MEAS_GR; ++k) { fl[k] = 0.0; zz[k] = 0ll; }
+  const uint32_t low = (1u << w0) - 1u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const uint32_t s = states[r];
+    const long long wq = wqv[r];
+    if (OP == ED_OP_SISJ) {
+      const double x = pr[r];
+      const uint32_t r0 = t0s[s & low];        // rank(s) = r0 + T1[s_hi]
+      const uint32_t r1 = (uint32_t)r - r0;  // = T1[s_hi]
+      double q[MEAS_GR];
+#pragma unroll
+      for (int g = 0; g < MEAS_GR; ++g) {
+        q[g] = 0.0;
+        if (g < pm.n && !((pm.diag >> g) & 1u)) {
+          const uint32_t m = pm.m[g];
+          if ((s & m) == pm.bi[g]) {  // bit i set, bit j clear: predicated, no memory request otherwise
+            const uint32_t f = s ^ m;
+            const uint32_t c = (pm.ml[g] ? (uint32_t)t0s[f & low] : r0) + (pm.mh[g] ? __ldg(&t1[f >> w0]) : r1);
+            q[g] = __ldg(&pr[c]);
+          }
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < MEAS_GR; ++g)
+        if (g < pm.n && !((pm.diag >> g) & 1u)) fl[g] = fma(x, q[g], fl[g]);
+    }
+#pragma unroll
+    for (int g = 0; g < MEAS_GR; ++g) {
+      if (g < pm.n) {
+        if ((pm.diag >> g) & 1u) {
+          zz[g] += OP == ED_OP_SISJ ? 3 * wq : wq;  // S_i.S_i = 3/4, S^z_i S^z_i = 1/4
+        } else {
+          const uint32_t m = pm.m[g], bits = s & m;
+          zz[g] += (bits != 0u && bits != m) ? -wq : wq;  // antiparallel: -1/4
+        }
+      }
+    }
+  }
+  __shared__ double shd[MEAS_GR * 32];
+  __shared__ long long shi[MEAS_GR * 32];
+  ed_block_reduce<MEAS_GR>(fl, shd);
+  ed_block_reduce_i64<MEAS_GR>(zz, shi);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < MEAS_GR; ++k) {
+      partial[(size_t)(2 * k) * nblk + blockIdx.x] = fl[k];
+      partial[(size_t)(2 * k + 1) * nblk + blockIdx.x] = __longlong_as_double(zz[k]);
+    }
+  }
+}
+
+// out[g] = 0.25 zz_g / wscale + flip_g, the block partials summed in a fixed
+// order (the integer sums exactly).  One block per pair.
+__global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk, int n, double wscale,
+                                    double* __restrict__ out) {
+  const int g = blockIdx.x;
+  if (g >= n) return;
+  __shared__ double shd[256];
+  __shared__ long long shi[256];
+  double a = 0.0;
+  long long z = 0ll;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    a += partial[(size_t)(2 * g) * nblk + b];
+    z += __double_as_longlong(partial[(size_t)(2 * g + 1) * nblk + b]);
+  }
+  shd[threadIdx.x] = a;
+  shi[threadIdx.x] = z;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      shd[threadIdx.x] += shd[threadIdx.x + s];
+      shi[threadIdx.x] += shi[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[g] = 0.25 * ((double)shi[0] / wscale) + shd[0];
+}
+
+__global__ void k_real_parts(const double2* __restrict__ src, double* __restrict__ dst, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) dst[r] = src[r].x;
+}
+
+// w_r = psi_r^2 in fixed point, once per call (the passes then run no FP64
+// operation per row for it)
+__global__ void k_weights_fx(const double* __restrict__ pr, long long* __restrict__ wq, int64_t n, double wscale) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+    wq[r] = __double2ll_rn(pr[r] * pr[r] * wscale);
+}
+
+// ED_ENOMEM (nothing launched) when the compact copy does not fit, ED_ENOTSUP
+// when psi is not finite: the general kernel then runs instead.
+template <int OP>
+static int expect_sym_r(const ed_basis* b, const double2* psi, const int32_t* pairs, int64_t np, double2* out) {
+  ed_ctx* ctx = b->ctx;
+  const int64_t dim = b->dim;
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 4));
+  const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
+  // the real parts and their squares in fixed point, side by side
+  double* pr = nullptr;
+  if (cudaMalloc(&pr, 2 * sizeof(double) * (size_t)dim) != cudaSuccess) {
+    cudaGetLastError();  // clear the allocation failure
+    return ED_ENOMEM;
+  }
+  long long* wqv = (long long*)(pr + dim);
+  const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 8));
+  int rc = ED_OK;
+  {
+    k_real_parts<<<gs, 256, 0, ctx->stream>>>(psi, pr, dim);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) rc = ed_cuda_fail(le, "k_real_parts launch", __FILE__, __LINE__);
+    else ctx->kernels++;
+  }
+  // sum_r psi_r^2 = W < 2^e: every fixed-point w_r is below 2^60 and every
+  // integer sum (at most 3 sum_r w_r) below 2^62 (the rounding of W moves it
+  // by far less than the two spare bits)
+  double W = 0.0;
+  if (rc == ED_OK) rc = ed_multidot_r(ctx, nullptr, 0, pr, dim, nullptr, 0.0, nullptr, 0.0, nullptr, &W);
+  if (rc == ED_OK && !std::isfinite(W)) rc = ED_ENOTSUP;
+  int e = 0;
+  if (rc == ED_OK && W > 0.0) std::frexp(W, &e);
+  const double wscale = std::ldexp(1.0, 60 - e);
+  if (rc == ED_OK) {
+    k_weights_fx<<<gs, 256, 0, ctx->stream>>>(pr, wqv, dim, wscale);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) rc = ed_cuda_fail(le, "k_weights_fx launch", __FILE__, __LINE__);
+    else ctx->kernels++;
+  }
+  if (rc == ED_OK) rc = ed_ensure_reduce(ctx, (size_t)2 * MEAS_GR * nblk + MEAS_GR + 8);
+  double* out_dev = ctx->d_red + (size_t)2 * MEAS_GR * nblk;
+  const uint32_t low = (1u << b->lin_w0) - 1u;
+  for (int64_t p0 = 0; p0 < np && rc == ED_OK; p0 += MEAS_GR) {
+    PairMasks pm;
+    memset(&pm, 0, sizeof(pm));
+    pm.n = (int)std::min<int64_t>(MEAS_GR, np - p0);
+    for (int g = 0; g < pm.n; ++g) {
+      const int i = pairs[2 * (p0 + g)], j = pairs[2 * (p0 + g) + 1];
+      const uint32_t m = (1u << i) | (1u << j);
+      if (i == j) pm.diag |= 1u << g;
+      pm.m[g] = m;
+      pm.bi[g] = 1u << i;
+      pm.ml[g] = m & low;
+      pm.mh[g] = m >> b->lin_w0;
+    }
+    k_expect_sym_r<OP><<<nblk, 256, smem, ctx->stream>>>(b->d_states, pr, wqv, dim, b->d_lin_t0, b->d_lin_t1,
+                                                          b->lin_w0, pm, ctx->d_red, nblk);
+    cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess) {
+      ctx->kernels++;
+      k_expect_sym_finish<<<pm.n, 256, 0, ctx->stream>>>(ctx->d_red, nblk, pm.n, wscale, out_dev);
+      le = cudaGetLastError();
+    }
+    if (le == cudaSuccess) {
+      ctx->kernels++;
+      le = cudaMemcpyAsync(ctx->h_red, out_dev, sizeof(double) * pm.n, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    if (le == cudaSuccess) le = cudaStreamSynchronize(ctx->stream);
+    if (le != cudaSuccess) {
+      rc = ed_cuda_fail(le, "expectation pass", __FILE__, __LINE__);
+      break;
+    }
+    for (int g = 0; g < pm.n; ++g) {
+      out[p0 + g].x = ctx->h_red[g];
+      out[p0 + g].y = 0.0;
+    }
+  }
+  const cudaError_t fe = cudaFree(pr);
+  if (fe != cudaSuccess && rc == ED_OK) rc = ed_cuda_fail(fe, "cudaFree", __FILE__, __LINE__);
+  return rc;
+}
+
 int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const int32_t* pairs, int64_t np,
                            double2* out) {
   bool real = false;
   ED_TRY(ed_is_real(b->ctx, psi, b->dim, &real));
+  if (real && (op == ED_OP_SISJ || op == ED_OP_SZSZ)) {
+    const int rc = op == ED_OP_SISJ ? expect_sym_r<ED_OP_SISJ>(b, psi, pairs, np, out)
+                                    : expect_sym_r<ED_OP_SZSZ>(b, psi, pairs, np, out);
+    if (rc != ED_ENOMEM && rc != ED_ENOTSUP) return rc;  // else the general kernel below
+  }
   if (real) return expect_g<MEAS_GR, true>(b, op, psi, pairs, np, out);
   return expect_g<MEAS_G, false>(b, op, psi, pairs, np, out);
 }

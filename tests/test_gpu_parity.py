@@ -559,6 +559,37 @@ def test_correlations_vs_oracle(ed, envs):
                 assert abs(got[i, j] - ref) <= 1e-14, (op, i, j, got[i, j], ref)
 
 
+@pytest.mark.parametrize('ltype,N,lx,ly,mag', [(1, 12, 4, 3, 0), (0, 14, 14, 1, 1), (1, 16, 4, 4, 2)])
+def test_correlations_real_state_vs_oracle(ed, envs, ltype, N, lx, ly, mag):
+    """A real state (the solver's eigenvectors are real): S^z S^z and S.S run
+    a kernel of their own (compact real copy of the state, the flipped state's
+    rank from the row's own), SpSm / SmSp the general one.  All four
+    operators, all N^2 pairs, against the oracle at 1e-14; pairs inside the
+    low half of the rank table, inside the high half, and across."""
+    env, b, h, M = make_pair(ed, envs, ltype, N, lx, ly, mag, 1.0, 1.0, 0.5, 0.5)
+    psi = oracle.start_vector(22 + N, b.size).real.copy()
+    psi /= np.linalg.norm(psi)
+    for op, cls in ((0, ed.SzSz), (1, ed.SpSm), (2, ed.SmSp), (3, ed.SiSj)):
+        got = cls(env, b).AllPairs(psi)
+        assert np.abs(got - got.T.conj()).max() == 0.0, op
+        for i in range(N):
+            for j in range(N):
+                ref = M.expect(op, i, j, psi)
+                assert abs(got[i, j] - ref) <= 1e-14, (op, i, j, got[i, j], ref)
+
+
+def test_correlations_nonfinite_state(ed, envs):
+    """A real state with a NaN entry: S.S and S^z S^z fall back to the general
+    kernel (their fixed-point sums need a finite norm) and every pair is NaN,
+    as in FP64."""
+    env, b, h, M = make_pair(ed, envs, 1, 12, 4, 3, 0, 1.0, 1.0, 0.5, 0.5)
+    psi = oracle.start_vector(7, b.size).real.copy()
+    psi[17] = np.nan
+    for cls in (ed.SzSz, ed.SiSj):
+        C = cls(env, b).AllPairs(psi)
+        assert np.isnan(C.real).all(), cls
+
+
 def test_sublattice_magnetisation(ed, envs):
     env, b, h, M = make_pair(ed, envs, 1, 16, 4, 4, 0, 1.0, 1.0, 0.0, 0.0)
     eps, nconv, ev, errs = solve(ed, env, h, 1)
