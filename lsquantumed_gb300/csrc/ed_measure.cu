@@ -148,15 +148,13 @@ static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t
 //    once;
 //  * the flip part (S+_i S-_j + S-_i S+_j) / 2 pairs every antiparallel row
 //    with its partner r' = rank(s ^ m) (an involution), so it equals
-//    sum over the rows with bit i set and bit j clear of psi_r psi_r': one
-//    FP64 FMA per pair and row, half the gathers;
+//    sum over the rows with bit i set and bit j clear of psi_r psi_r': half
+//    the gathers, and only those rows do any FP64 work (below);
 //  * psi is read as 8-byte real parts from a compact copy;
 //  * the row's own rank r = T0[s_lo] + T1[s_hi] gives both halves, so a flip
 //    inside the low bits needs no T1 load and one inside the high bits no T0
 //    lookup;
-//  * a row's gathers are issued together: each is predicated on its own
-//    condition, with no branch between them, and a row that does not
-//    contribute adds zero.
+//  * a lane's gathers are issued together, several in flight.
 struct PairMasks {
   int n;
   uint32_t diag;         // bit g: pair g has i == j
@@ -191,6 +189,16 @@ __device__ __forceinline__ void ed_block_reduce_i64(long long (&v)[NV], long lon
 // partial[(2 g) nblk + blk]: flip sum of pair g (FP64); partial[(2 g + 1)
 // nblk + blk]: its S^z S^z sum in fixed point (int64 bits), times 4 in the
 // units of the final result.
+//
+// A warp takes 32 consecutive rows at a time, one per lane, for the S^z S^z
+// part.  For the flip part, lane l serves pair l / 2: a ballot per pair marks
+// the rows with bit i set and bit j clear, and the pair's two lanes take
+// alternate marked rows (state, psi and rank halves by shuffle).  A row and
+// pair that contribute nothing then costs no FMA and no gather: about a
+// quarter of them contribute, and the FP64 FMAs per warp drop from 16 per
+// row to the largest share of one lane.  Up to FL_U items per lane have their
+// gathers in flight together.
+#define FL_U 4
 template <int OP>
 __global__ void __launch_bounds__(256, 2) k_expect_sym_r(const uint32_t* __restrict__ states,
                                                       const double* __restrict__ pr,
@@ -201,35 +209,41 @@ __global__ void __launch_bounds__(256, 2) k_expect_sym_r(const uint32_t* __restr
   extern __shared__ uint16_t t0s[];
   for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
-  double fl[MEAS_GR];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gl = lane >> 1, par = lane & 1;  // this lane's pair (flip part) and its turn
+  const bool gl_on = OP == ED_OP_SISJ && gl < pm.n && !((pm.diag >> gl) & 1u);
+  const uint32_t my_m = pm.m[gl], my_ml = pm.ml[gl], my_mh = pm.mh[gl];
+  double fl = 0.0;
   long long zz[MEAS_GR];
 #pragma unroll
-  for (int k = 0; k < MEAS_GR; ++k) { fl[k] = 0.0; zz[k] = 0ll; }
+  for (int k = 0; k < MEAS_GR; ++k) zz[k] = 0ll;
   const uint32_t low = (1u << w0) - 1u;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
-    const uint32_t s = states[r];
-    const long long wq = wqv[r];
-    if (OP == ED_OP_SISJ) {
-      const double x = pr[r];
-      const uint32_t r0 = t0s[s & low];        // rank(s) = r0 + T1[s_hi]
-      const uint32_t r1 = (uint32_t)r - r0;  // = T1[s_hi]
-      double q[MEAS_GR];
-#pragma unroll
-      for (int g = 0; g < MEAS_GR; ++g) {
-        q[g] = 0.0;
-        if (g < pm.n && !((pm.diag >> g) & 1u)) {
-          const uint32_t m = pm.m[g];
-          if ((s & m) == pm.bi[g]) {  // bit i set, bit j clear: predicated, no memory request otherwise
-            const uint32_t f = s ^ m;
-            const uint32_t c = (pm.ml[g] ? (uint32_t)t0s[f & low] : r0) + (pm.mh[g] ? __ldg(&t1[f >> w0]) : r1);
-            q[g] = __ldg(&pr[c]);
-          }
-        }
-      }
-#pragma unroll
-      for (int g = 0; g < MEAS_GR; ++g)
-        if (g < pm.n && !((pm.diag >> g) & 1u)) fl[g] = fma(x, q[g], fl[g]);
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t step = nwarps * 32;
+  int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  // the next chunk's row is loaded while this one is worked on
+  uint32_t s_n = 0u;
+  long long wq_n = 0ll;
+  double x_n = 0.0;
+  if (base + lane < dim) {
+    s_n = states[base + lane];
+    wq_n = wqv[base + lane];
+    if (OP == ED_OP_SISJ) x_n = pr[base + lane];
+  }
+  for (; base < dim; base += step) {
+    const int64_t r = base + lane;
+    const bool valid = r < dim;
+    const uint32_t s = s_n;
+    const long long wq = wq_n;
+    const double x = x_n;
+    s_n = 0u;  // rows past the end: weight 0, never marked
+    wq_n = 0ll;
+    x_n = 0.0;
+    if (base + step + lane < dim) {
+      s_n = states[base + step + lane];
+      wq_n = wqv[base + step + lane];
+      if (OP == ED_OP_SISJ) x_n = pr[base + step + lane];
     }
 #pragma unroll
     for (int g = 0; g < MEAS_GR; ++g) {
@@ -242,17 +256,65 @@ __global__ void __launch_bounds__(256, 2) k_expect_sym_r(const uint32_t* __restr
         }
       }
     }
+    if (OP == ED_OP_SISJ) {
+      const uint32_t r0 = valid ? (uint32_t)t0s[s & low] : 0u;  // rank(s) = r0 + T1[s_hi]
+      const uint32_t r1 = (uint32_t)r - r0;                    // = T1[s_hi]
+      uint32_t L = 0u;
+#pragma unroll
+      for (int g = 0; g < MEAS_GR; ++g) {
+        const bool lead = valid && g < pm.n && !((pm.diag >> g) & 1u) && (s & pm.m[g]) == pm.bi[g];
+        const uint32_t bal = __ballot_sync(FULL, lead);
+        L = gl == g ? bal : L;
+      }
+      if (!gl_on) L = 0u;
+      if (par) L &= L - 1u;  // the pair's second lane starts at its second marked row
+      const int mine = (__popc(L) + 1) >> 1;
+      const int T = __reduce_max_sync(FULL, (unsigned)mine);
+      for (int t = 0; t < T; t += FL_U) {
+        int k[FL_U];
+        bool has[FL_U];
+#pragma unroll
+        for (int u = 0; u < FL_U; ++u) {
+          has[u] = L != 0u;
+          k[u] = has[u] ? __ffs(L) - 1 : lane;
+          L &= L - 1u;  // taken
+          L &= L - 1u;  // the other lane's
+        }
+        double xk[FL_U], q[FL_U];
+#pragma unroll
+        for (int u = 0; u < FL_U; ++u) {
+          const uint32_t sk = __shfl_sync(FULL, s, k[u]);
+          const uint32_t r0k = __shfl_sync(FULL, r0, k[u]);
+          const uint32_t r1k = __shfl_sync(FULL, r1, k[u]);
+          xk[u] = __shfl_sync(FULL, x, k[u]);
+          q[u] = 0.0;
+          if (has[u]) {
+            const uint32_t f = sk ^ my_m;
+            const uint32_t c = (my_ml ? (uint32_t)t0s[f & low] : r0k) + (my_mh ? __ldg(&t1[f >> w0]) : r1k);
+            q[u] = __ldg(&pr[c]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < FL_U; ++u)
+          if (has[u]) fl = fma(xk[u], q[u], fl);
+      }
+    }
   }
-  __shared__ double shd[MEAS_GR * 32];
+  __shared__ double shf[8 * 32];
   __shared__ long long shi[MEAS_GR * 32];
-  ed_block_reduce<MEAS_GR>(fl, shd);
   ed_block_reduce_i64<MEAS_GR>(zz, shi);
+  if (OP == ED_OP_SISJ) shf[wid * 32 + lane] = fl;
+  __syncthreads();
+  if (threadIdx.x < MEAS_GR) {
+    const int g = threadIdx.x;
+    double a = 0.0;
+    if (OP == ED_OP_SISJ)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += shf[w * 32 + 2 * g] + shf[w * 32 + 2 * g + 1];
+    partial[(size_t)(2 * g) * nblk + blockIdx.x] = a;
+  }
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < MEAS_GR; ++k) {
-      partial[(size_t)(2 * k) * nblk + blockIdx.x] = fl[k];
-      partial[(size_t)(2 * k + 1) * nblk + blockIdx.x] = __longlong_as_double(zz[k]);
-    }
+    for (int k = 0; k < MEAS_GR; ++k) partial[(size_t)(2 * k + 1) * nblk + blockIdx.x] = __longlong_as_double(zz[k]);
   }
 }
 
