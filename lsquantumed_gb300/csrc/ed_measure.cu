@@ -140,21 +140,27 @@ static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t
 // Real psi and a symmetric operator (S^z_i S^z_j or S_i.S_j): the solver's
 // eigenvectors and the all-pairs measurement.  The general kernel above spends
 // about four FP64 operations per pair and row, and GB300 runs FP64 at a small
-// fraction of its other rates: at N=30 that pass is FP64-bound.  Here
-//  * the S^z S^z part, 0.25 sum_r w_r sigma_i sigma_j with w_r = psi_r^2, is
-//    summed in 64-bit integers: w_r in fixed point once per call (scale
-//    2^(60 - e) with sum_r w_r < 2^e, so no sum can overflow), then one
-//    integer add or subtract per pair and row; each sum is exact and rounded
-//    once;
-//  * the flip part (S+_i S-_j + S-_i S+_j) / 2 pairs every antiparallel row
-//    with its partner r' = rank(s ^ m) (an involution), so it equals
-//    sum over the rows with bit i set and bit j clear of psi_r psi_r': half
-//    the gathers, and only those rows do any FP64 work (below);
-//  * psi is read as 8-byte real parts from a compact copy;
-//  * the row's own rank r = T0[s_lo] + T1[s_hi] gives both halves, so a flip
-//    inside the low bits needs no T1 load and one inside the high bits no T0
-//    lookup;
-//  * a lane's gathers are issued together, several in flight.
+// fraction of its other rates: at N=30 that pass is FP64-bound.  Here two
+// kernels share a pass of up to MEAS_GR pairs:
+//  * k_expect_zz_r, the S^z S^z part 0.25 sum_r w_r sigma_i sigma_j with
+//    w_r = psi_r^2 (FP64, as the general kernel forms it): each w_r becomes a
+//    128-bit integer at the scale 2^(124 - e), sum_r w_r < 2^e, which holds
+//    every w_r above 2^(e - 72) exactly; the sums T = sum_r w_r and, per pair,
+//    A = sum over antiparallel rows of w_r are exact integer sums, and
+//    0.25 (T - 2 A) is rounded once at the end;
+//  * k_expect_flip_r, the flip part (S+_i S-_j + S-_i S+_j) / 2: it pairs
+//    every antiparallel row with its partner r' = rank(s ^ m) (an
+//    involution), so it equals the sum over the rows with bit i set and bit j
+//    clear of psi_r psi_r'.  Lane l of a warp serves pair l / 2: a ballot per
+//    pair marks the contributing rows among the warp's 32, and the pair's two
+//    lanes take alternate marked rows (state, psi and rank halves by
+//    shuffle), four gathers in flight each.  A row and pair that contribute
+//    nothing cost no FMA and no gather;
+//  * psi is read as 8-byte real parts from a compact copy, and the next
+//    chunk's rows are loaded while the current one is worked on;
+//  * the row's own rank r = T0[s_lo] + T1[s_hi] gives both halves of the
+//    flipped state's rank, so a flip inside the low bits needs no T1 load and
+//    one inside the high bits no T0 lookup.
 struct PairMasks {
   int n;
   uint32_t diag;         // bit g: pair g has i == j
@@ -164,198 +170,256 @@ struct PairMasks {
   uint32_t mh[MEAS_GR];  // m >> w0
 };
 
-template <int NV>
-__device__ __forceinline__ void ed_block_reduce_i64(long long (&v)[NV], long long* sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    long long a = v[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-    if (lane == 0) sh[k * 32 + wid] = a;
-  }
-  __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      long long a = lane < nw ? sh[k * 32 + lane] : 0ll;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-      v[k] = a;
-    }
+// 128-bit integer accumulators (two 64-bit words, add with carry)
+__device__ __forceinline__ void ed_add128(unsigned long long& lo, unsigned long long& hi, unsigned long long alo,
+                                          unsigned long long ahi) {
+  asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(alo), "l"(ahi));
+}
+
+// w >= 0 (finite) as the 128-bit integer round(w 2^S); exact when w's last
+// bit is at or above 2^-S.  w < 2^(124 - S) keeps it below 2^124.
+__device__ __forceinline__ void ed_fx128(double w, int S, unsigned long long& lo, unsigned long long& hi) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(w);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = E - 1075 + S;  // w 2^S = mant 2^sh
+  lo = 0ull;
+  hi = 0ull;
+  if (E == 0) return;  // zero or below 2^-1022
+  if (sh >= 64) {
+    hi = mant << (sh - 64);
+  } else if (sh > 0) {
+    lo = mant << sh;
+    hi = mant >> (64 - sh);
+  } else if (sh == 0) {
+    lo = mant;
+  } else if (sh > -54) {
+    lo = (mant + (1ull << (-sh - 1))) >> (-sh);
   }
 }
 
-// partial[(2 g) nblk + blk]: flip sum of pair g (FP64); partial[(2 g + 1)
-// nblk + blk]: its S^z S^z sum in fixed point (int64 bits), times 4 in the
-// units of the final result.
-//
-// A warp takes 32 consecutive rows at a time, one per lane, for the S^z S^z
-// part.  For the flip part, lane l serves pair l / 2: a ballot per pair marks
-// the rows with bit i set and bit j clear, and the pair's two lanes take
-// alternate marked rows (state, psi and rank halves by shuffle).  A row and
-// pair that contribute nothing then costs no FMA and no gather: about a
-// quarter of them contribute, and the FP64 FMAs per warp drop from 16 per
-// row to the largest share of one lane.  Up to FL_U items per lane have their
-// gathers in flight together.
+// partial[(3 g) nblk + blk] and [(3 g + 1) nblk + blk]: lo and hi words of
+// pair g's antiparallel sum A; partial[(3 MEAS_GR) nblk + blk], [(3 MEAS_GR
+// + 1) nblk + blk]: the block's T (int64 bits in the double array).
+__global__ void __launch_bounds__(256, 2) k_expect_zz_r(const uint32_t* __restrict__ states,
+                                                     const double* __restrict__ pr, int64_t dim, int S,
+                                                     const PairMasks pm, double* __restrict__ partial, int nblk) {
+  unsigned long long alo[MEAS_GR], ahi[MEAS_GR];
+#pragma unroll
+  for (int k = 0; k < MEAS_GR; ++k) { alo[k] = 0ull; ahi[k] = 0ull; }
+  unsigned long long tlo = 0ull, thi = 0ull;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t s_n = 0u;
+  double x_n = 0.0;
+  if (r < dim) {
+    s_n = states[r];
+    x_n = pr[r];
+  }
+  for (; r < dim; r += stride) {
+    const uint32_t s = s_n;
+    const double x = x_n;
+    if (r + stride < dim) {  // the next row, loaded while this one is worked on
+      s_n = states[r + stride];
+      x_n = pr[r + stride];
+    }
+    unsigned long long wlo, whi;
+    ed_fx128(x * x, S, wlo, whi);
+    ed_add128(tlo, thi, wlo, whi);
+#pragma unroll
+    for (int g = 0; g < MEAS_GR; ++g) {
+      if (g < pm.n) {
+        const uint32_t m = pm.m[g], bits = s & m;
+        if (bits != 0u && bits != m) ed_add128(alo[g], ahi[g], wlo, whi);  // antiparallel
+      }
+    }
+  }
+  // block sums: warp shuffles with carries, then lane 0 of each warp in
+  // shared memory, summed by thread 0 in a fixed order
+  __shared__ unsigned long long shz[(MEAS_GR + 1) * 2 * 8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k <= MEAS_GR; ++k) {
+    unsigned long long lo = k < MEAS_GR ? alo[k] : tlo, hi = k < MEAS_GR ? ahi[k] : thi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long olo = __shfl_down_sync(0xffffffffu, lo, o), ohi = __shfl_down_sync(0xffffffffu, hi, o);
+      ed_add128(lo, hi, olo, ohi);
+    }
+    if (lane == 0) {
+      shz[(k * 8 + wid) * 2] = lo;
+      shz[(k * 8 + wid) * 2 + 1] = hi;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x <= MEAS_GR) {
+    const int k = threadIdx.x;
+    unsigned long long lo = 0ull, hi = 0ull;
+    for (int w = 0; w < nw; ++w) ed_add128(lo, hi, shz[(k * 8 + w) * 2], shz[(k * 8 + w) * 2 + 1]);
+    partial[(size_t)(3 * k) * nblk + blockIdx.x] = __longlong_as_double((long long)lo);
+    partial[(size_t)(3 * k + 1) * nblk + blockIdx.x] = __longlong_as_double((long long)hi);
+  }
+}
+
+// partial[(3 g + 2) nblk + blk]: flip sum of pair g (FP64).
 #define FL_U 4
-template <int OP>
-__global__ void __launch_bounds__(256, 2) k_expect_sym_r(const uint32_t* __restrict__ states,
-                                                      const double* __restrict__ pr,
-                                                      const long long* __restrict__ wqv, int64_t dim,
-                                                      const uint16_t* __restrict__ t0,
-                                                      const uint32_t* __restrict__ t1, int w0, const PairMasks pm,
-                                                      double* __restrict__ partial, int nblk) {
+__global__ void __launch_bounds__(256, 3) k_expect_flip_r(const uint32_t* __restrict__ states,
+                                                       const double* __restrict__ pr, int64_t dim,
+                                                       const uint16_t* __restrict__ t0,
+                                                       const uint32_t* __restrict__ t1, int w0, const PairMasks pm,
+                                                       double* __restrict__ partial, int nblk) {
   extern __shared__ uint16_t t0s[];
   for (int i = threadIdx.x; i < (1 << w0); i += blockDim.x) t0s[i] = t0[i];
   __syncthreads();
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gl = lane >> 1, par = lane & 1;  // this lane's pair (flip part) and its turn
-  const bool gl_on = OP == ED_OP_SISJ && gl < pm.n && !((pm.diag >> gl) & 1u);
+  const int gl = lane >> 1, par = lane & 1;  // this lane's pair and its turn
+  const bool gl_on = gl < pm.n && !((pm.diag >> gl) & 1u);
   const uint32_t my_m = pm.m[gl], my_ml = pm.ml[gl], my_mh = pm.mh[gl];
   double fl = 0.0;
-  long long zz[MEAS_GR];
-#pragma unroll
-  for (int k = 0; k < MEAS_GR; ++k) zz[k] = 0ll;
   const uint32_t low = (1u << w0) - 1u;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t step = nwarps * 32;
+  const int64_t step = (((int64_t)gridDim.x * blockDim.x) >> 5) * 32;
   int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
-  // the next chunk's row is loaded while this one is worked on
   uint32_t s_n = 0u;
-  long long wq_n = 0ll;
   double x_n = 0.0;
   if (base + lane < dim) {
     s_n = states[base + lane];
-    wq_n = wqv[base + lane];
-    if (OP == ED_OP_SISJ) x_n = pr[base + lane];
+    x_n = pr[base + lane];
   }
   for (; base < dim; base += step) {
     const int64_t r = base + lane;
     const bool valid = r < dim;
     const uint32_t s = s_n;
-    const long long wq = wq_n;
     const double x = x_n;
-    s_n = 0u;  // rows past the end: weight 0, never marked
-    wq_n = 0ll;
+    s_n = 0u;  // rows past the end: never marked
     x_n = 0.0;
     if (base + step + lane < dim) {
       s_n = states[base + step + lane];
-      wq_n = wqv[base + step + lane];
-      if (OP == ED_OP_SISJ) x_n = pr[base + step + lane];
+      x_n = pr[base + step + lane];
     }
+    const uint32_t r0 = valid ? (uint32_t)t0s[s & low] : 0u;  // rank(s) = r0 + T1[s_hi]
+    const uint32_t r1 = (uint32_t)r - r0;                    // = T1[s_hi]
+    uint32_t L = 0u;
 #pragma unroll
     for (int g = 0; g < MEAS_GR; ++g) {
-      if (g < pm.n) {
-        if ((pm.diag >> g) & 1u) {
-          zz[g] += OP == ED_OP_SISJ ? 3 * wq : wq;  // S_i.S_i = 3/4, S^z_i S^z_i = 1/4
-        } else {
-          const uint32_t m = pm.m[g], bits = s & m;
-          zz[g] += (bits != 0u && bits != m) ? -wq : wq;  // antiparallel: -1/4
-        }
-      }
+      const bool lead = valid && g < pm.n && !((pm.diag >> g) & 1u) && (s & pm.m[g]) == pm.bi[g];
+      const uint32_t bal = __ballot_sync(FULL, lead);
+      L = gl == g ? bal : L;
     }
-    if (OP == ED_OP_SISJ) {
-      const uint32_t r0 = valid ? (uint32_t)t0s[s & low] : 0u;  // rank(s) = r0 + T1[s_hi]
-      const uint32_t r1 = (uint32_t)r - r0;                    // = T1[s_hi]
-      uint32_t L = 0u;
+    if (!gl_on) L = 0u;
+    if (par) L &= L - 1u;  // the pair's second lane starts at its second marked row
+    const int mine = (__popc(L) + 1) >> 1;
+    const int T = __reduce_max_sync(FULL, (unsigned)mine);
+    for (int t = 0; t < T; t += FL_U) {
+      int k[FL_U];
+      bool has[FL_U];
 #pragma unroll
-      for (int g = 0; g < MEAS_GR; ++g) {
-        const bool lead = valid && g < pm.n && !((pm.diag >> g) & 1u) && (s & pm.m[g]) == pm.bi[g];
-        const uint32_t bal = __ballot_sync(FULL, lead);
-        L = gl == g ? bal : L;
+      for (int u = 0; u < FL_U; ++u) {
+        has[u] = L != 0u;
+        k[u] = has[u] ? __ffs(L) - 1 : lane;
+        L &= L - 1u;  // taken
+        L &= L - 1u;  // the other lane's
       }
-      if (!gl_on) L = 0u;
-      if (par) L &= L - 1u;  // the pair's second lane starts at its second marked row
-      const int mine = (__popc(L) + 1) >> 1;
-      const int T = __reduce_max_sync(FULL, (unsigned)mine);
-      for (int t = 0; t < T; t += FL_U) {
-        int k[FL_U];
-        bool has[FL_U];
+      double xk[FL_U], q[FL_U];
 #pragma unroll
-        for (int u = 0; u < FL_U; ++u) {
-          has[u] = L != 0u;
-          k[u] = has[u] ? __ffs(L) - 1 : lane;
-          L &= L - 1u;  // taken
-          L &= L - 1u;  // the other lane's
+      for (int u = 0; u < FL_U; ++u) {
+        const uint32_t sk = __shfl_sync(FULL, s, k[u]);
+        const uint32_t r0k = __shfl_sync(FULL, r0, k[u]);
+        const uint32_t r1k = __shfl_sync(FULL, r1, k[u]);
+        xk[u] = __shfl_sync(FULL, x, k[u]);
+        q[u] = 0.0;
+        if (has[u]) {
+          const uint32_t f = sk ^ my_m;
+          const uint32_t c = (my_ml ? (uint32_t)t0s[f & low] : r0k) + (my_mh ? __ldg(&t1[f >> w0]) : r1k);
+          q[u] = __ldg(&pr[c]);
         }
-        double xk[FL_U], q[FL_U];
-#pragma unroll
-        for (int u = 0; u < FL_U; ++u) {
-          const uint32_t sk = __shfl_sync(FULL, s, k[u]);
-          const uint32_t r0k = __shfl_sync(FULL, r0, k[u]);
-          const uint32_t r1k = __shfl_sync(FULL, r1, k[u]);
-          xk[u] = __shfl_sync(FULL, x, k[u]);
-          q[u] = 0.0;
-          if (has[u]) {
-            const uint32_t f = sk ^ my_m;
-            const uint32_t c = (my_ml ? (uint32_t)t0s[f & low] : r0k) + (my_mh ? __ldg(&t1[f >> w0]) : r1k);
-            q[u] = __ldg(&pr[c]);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < FL_U; ++u)
-          if (has[u]) fl = fma(xk[u], q[u], fl);
       }
+#pragma unroll
+      for (int u = 0; u < FL_U; ++u)
+        if (has[u]) fl = fma(xk[u], q[u], fl);
     }
   }
   __shared__ double shf[8 * 32];
-  __shared__ long long shi[MEAS_GR * 32];
-  ed_block_reduce_i64<MEAS_GR>(zz, shi);
-  if (OP == ED_OP_SISJ) shf[wid * 32 + lane] = fl;
+  shf[wid * 32 + lane] = fl;
   __syncthreads();
   if (threadIdx.x < MEAS_GR) {
     const int g = threadIdx.x;
     double a = 0.0;
-    if (OP == ED_OP_SISJ)
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += shf[w * 32 + 2 * g] + shf[w * 32 + 2 * g + 1];
-    partial[(size_t)(2 * g) * nblk + blockIdx.x] = a;
-  }
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < MEAS_GR; ++k) partial[(size_t)(2 * k + 1) * nblk + blockIdx.x] = __longlong_as_double(zz[k]);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += shf[w * 32 + 2 * g] + shf[w * 32 + 2 * g + 1];
+    partial[(size_t)(3 * g + 2) * nblk + blockIdx.x] = a;
   }
 }
 
-// out[g] = 0.25 zz_g / wscale + flip_g, the block partials summed in a fixed
-// order (the integer sums exactly).  One block per pair.
-__global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk, int n, double wscale,
-                                    double* __restrict__ out) {
+// Signed 128-bit (lo, hi) to the nearest double, approximately: |error| below
+// 2^-52 of the value.
+__device__ __forceinline__ double ed_i128_to_double(unsigned long long lo, unsigned long long hi) {
+  const bool neg = (long long)hi < 0;
+  if (neg) {  // magnitude
+    lo = ~lo;
+    hi = ~hi;
+    ed_add128(lo, hi, 1ull, 0ull);
+  }
+  const double d = fma((double)hi, 0x1p64, (double)lo);
+  return neg ? -d : d;
+}
+
+// out[g]: 0.25 (T - 2 A_g) 2^-S, plus (S.S) the flip sum, or for i == j
+// another 0.5 T 2^-S; block partials summed in a fixed order (the integer
+// ones exactly).  One block per pair.
+__global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk, const PairMasks pm, int sisj,
+                                    double inv_scale, double* __restrict__ out) {
   const int g = blockIdx.x;
-  if (g >= n) return;
+  if (g >= pm.n) return;
   __shared__ double shd[256];
-  __shared__ long long shi[256];
+  __shared__ unsigned long long sh[4][256];
   double a = 0.0;
-  long long z = 0ll;
+  unsigned long long alo = 0ull, ahi = 0ull, tlo = 0ull, thi = 0ull;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-    a += partial[(size_t)(2 * g) * nblk + b];
-    z += __double_as_longlong(partial[(size_t)(2 * g + 1) * nblk + b]);
+    if (sisj) a += partial[(size_t)(3 * g + 2) * nblk + b];
+    ed_add128(alo, ahi, (unsigned long long)__double_as_longlong(partial[(size_t)(3 * g) * nblk + b]),
+              (unsigned long long)__double_as_longlong(partial[(size_t)(3 * g + 1) * nblk + b]));
+    ed_add128(tlo, thi, (unsigned long long)__double_as_longlong(partial[(size_t)(3 * MEAS_GR) * nblk + b]),
+              (unsigned long long)__double_as_longlong(partial[(size_t)(3 * MEAS_GR + 1) * nblk + b]));
   }
   shd[threadIdx.x] = a;
-  shi[threadIdx.x] = z;
+  sh[0][threadIdx.x] = alo;
+  sh[1][threadIdx.x] = ahi;
+  sh[2][threadIdx.x] = tlo;
+  sh[3][threadIdx.x] = thi;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      shd[threadIdx.x] += shd[threadIdx.x + s];
-      shi[threadIdx.x] += shi[threadIdx.x + s];
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      shd[threadIdx.x] += shd[threadIdx.x + st];
+      unsigned long long l0 = sh[0][threadIdx.x], h0 = sh[1][threadIdx.x];
+      ed_add128(l0, h0, sh[0][threadIdx.x + st], sh[1][threadIdx.x + st]);
+      sh[0][threadIdx.x] = l0;
+      sh[1][threadIdx.x] = h0;
+      unsigned long long l1 = sh[2][threadIdx.x], h1 = sh[3][threadIdx.x];
+      ed_add128(l1, h1, sh[2][threadIdx.x + st], sh[3][threadIdx.x + st]);
+      sh[2][threadIdx.x] = l1;
+      sh[3][threadIdx.x] = h1;
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[g] = 0.25 * ((double)shi[0] / wscale) + shd[0];
+  if (threadIdx.x == 0) {
+    // Z = T - 2 A (|Z| <= T < 2^124)
+    unsigned long long zlo = sh[2][0], zhi = sh[3][0];
+    unsigned long long nlo = ~sh[0][0], nhi = ~sh[1][0];
+    ed_add128(nlo, nhi, 1ull, 0ull);  // -A
+    ed_add128(zlo, zhi, nlo, nhi);
+    ed_add128(zlo, zhi, nlo, nhi);
+    double v = 0.25 * (ed_i128_to_double(zlo, zhi) * inv_scale);
+    if (sisj) {
+      if ((pm.diag >> g) & 1u) v += 0.5 * (ed_i128_to_double(sh[2][0], sh[3][0]) * inv_scale);  // (S+S- + S-S+) / 2
+      else v += shd[0];
+    }
+    out[g] = v;
+  }
 }
 
 __global__ void k_real_parts(const double2* __restrict__ src, double* __restrict__ dst, int64_t n) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) dst[r] = src[r].x;
-}
-
-// w_r = psi_r^2 in fixed point, once per call (the passes then run no FP64
-// operation per row for it)
-__global__ void k_weights_fx(const double* __restrict__ pr, long long* __restrict__ wq, int64_t n, double wscale) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
-    wq[r] = __double2ll_rn(pr[r] * pr[r] * wscale);
 }
 
 // ED_ENOMEM (nothing launched) when the compact copy does not fit, ED_ENOTSUP
@@ -366,38 +430,32 @@ static int expect_sym_r(const ed_basis* b, const double2* psi, const int32_t* pa
   const int64_t dim = b->dim;
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 4));
   const size_t smem = sizeof(uint16_t) * ((size_t)1 << b->lin_w0);
-  // the real parts and their squares in fixed point, side by side
   double* pr = nullptr;
-  if (cudaMalloc(&pr, 2 * sizeof(double) * (size_t)dim) != cudaSuccess) {
+  if (cudaMalloc(&pr, sizeof(double) * (size_t)dim) != cudaSuccess) {
     cudaGetLastError();  // clear the allocation failure
     return ED_ENOMEM;
   }
-  long long* wqv = (long long*)(pr + dim);
-  const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 8));
   int rc = ED_OK;
   {
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((dim + 255) / 256, (int64_t)ctx->num_sms * 8));
     k_real_parts<<<gs, 256, 0, ctx->stream>>>(psi, pr, dim);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) rc = ed_cuda_fail(le, "k_real_parts launch", __FILE__, __LINE__);
     else ctx->kernels++;
   }
-  // sum_r psi_r^2 = W < 2^e: every fixed-point w_r is below 2^60 and every
-  // integer sum (at most 3 sum_r w_r) below 2^62 (the rounding of W moves it
-  // by far less than the two spare bits)
+  // sum_r psi_r^2 = W < 2^e: every w_r and every integer sum stays below
+  // 2^124 at the scale 2^(124 - e) (the rounding of W moves it by far less
+  // than the spare bits)
   double W = 0.0;
   if (rc == ED_OK) rc = ed_multidot_r(ctx, nullptr, 0, pr, dim, nullptr, 0.0, nullptr, 0.0, nullptr, &W);
   if (rc == ED_OK && !std::isfinite(W)) rc = ED_ENOTSUP;
   int e = 0;
   if (rc == ED_OK && W > 0.0) std::frexp(W, &e);
-  const double wscale = std::ldexp(1.0, 60 - e);
-  if (rc == ED_OK) {
-    k_weights_fx<<<gs, 256, 0, ctx->stream>>>(pr, wqv, dim, wscale);
-    const cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) rc = ed_cuda_fail(le, "k_weights_fx launch", __FILE__, __LINE__);
-    else ctx->kernels++;
-  }
-  if (rc == ED_OK) rc = ed_ensure_reduce(ctx, (size_t)2 * MEAS_GR * nblk + MEAS_GR + 8);
-  double* out_dev = ctx->d_red + (size_t)2 * MEAS_GR * nblk;
+  const int S = 124 - e;
+  const double inv_scale = std::ldexp(1.0, -S);
+  const size_t items = (size_t)3 * (MEAS_GR + 1);
+  if (rc == ED_OK) rc = ed_ensure_reduce(ctx, items * nblk + MEAS_GR + 8);
+  double* out_dev = ctx->d_red + items * nblk;
   const uint32_t low = (1u << b->lin_w0) - 1u;
   for (int64_t p0 = 0; p0 < np && rc == ED_OK; p0 += MEAS_GR) {
     PairMasks pm;
@@ -412,12 +470,20 @@ static int expect_sym_r(const ed_basis* b, const double2* psi, const int32_t* pa
       pm.ml[g] = m & low;
       pm.mh[g] = m >> b->lin_w0;
     }
-    k_expect_sym_r<OP><<<nblk, 256, smem, ctx->stream>>>(b->d_states, pr, wqv, dim, b->d_lin_t0, b->d_lin_t1,
-                                                          b->lin_w0, pm, ctx->d_red, nblk);
+    k_expect_zz_r<<<nblk, 256, 0, ctx->stream>>>(b->d_states, pr, dim, S, pm, ctx->d_red, nblk);
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) {
       ctx->kernels++;
-      k_expect_sym_finish<<<pm.n, 256, 0, ctx->stream>>>(ctx->d_red, nblk, pm.n, wscale, out_dev);
+      if (OP == ED_OP_SISJ) {
+        k_expect_flip_r<<<nblk, 256, smem, ctx->stream>>>(b->d_states, pr, dim, b->d_lin_t0, b->d_lin_t1,
+                                                          b->lin_w0, pm, ctx->d_red, nblk);
+        le = cudaGetLastError();
+        if (le == cudaSuccess) ctx->kernels++;
+      }
+    }
+    if (le == cudaSuccess) {
+      k_expect_sym_finish<<<pm.n, 256, 0, ctx->stream>>>(ctx->d_red, nblk, pm, OP == ED_OP_SISJ ? 1 : 0, inv_scale,
+                                                         out_dev);
       le = cudaGetLastError();
     }
     if (le == cudaSuccess) {

@@ -578,6 +578,24 @@ def test_correlations_real_state_vs_oracle(ed, envs, ltype, N, lx, ly, mag):
                 assert abs(got[i, j] - ref) <= 1e-14, (op, i, j, got[i, j], ref)
 
 
+def test_correlations_wide_range_state(ed, envs):
+    """One large amplitude and 12,869 of size 0.8 2^-30 (random signs): the
+    S^z S^z sums of the real-state kernel are exact integer sums of psi_r^2 at
+    a scale fixed by their total, so the tiny weights must not be rounded
+    away (at 2^-59 resolution each would lose about 2^-60, 1e-14 in all).
+    Against the oracle at 1e-15."""
+    env, b, h, M = make_pair(ed, envs, 1, 16, 4, 4, 0, 1.0, 1.0, 0.5, 0.5)
+    rng = np.random.default_rng(11)
+    psi = np.where(rng.random(b.size) < 0.5, -1.0, 1.0) * (0.8 * 2.0 ** -30)
+    psi[0] = 1.0
+    for op, cls in ((0, ed.SzSz), (3, ed.SiSj)):
+        got = cls(env, b).AllPairs(psi)
+        for i in range(16):
+            for j in range(16):
+                ref = M.expect(op, i, j, psi)
+                assert abs(got[i, j] - ref) <= 1e-15, (op, i, j, got[i, j], ref)
+
+
 def test_correlations_nonfinite_state(ed, envs):
     """A real state with a NaN entry: S.S and S^z S^z fall back to the general
     kernel (their fixed-point sums need a finite norm) and every pair is NaN,
