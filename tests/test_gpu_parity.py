@@ -596,6 +596,31 @@ def test_correlations_wide_range_state(ed, envs):
                 assert abs(got[i, j] - ref) <= 1e-15, (op, i, j, got[i, j], ref)
 
 
+@pytest.mark.parametrize('N,lx,ly,mag,wide', [(12, 4, 3, 0, False), (16, 4, 4, 1, True)])
+def test_szsz_real_state_bit_exact_vs_model(ed, envs, N, lx, ly, mag, wide):
+    """The S^z S^z sums of a real state (exact 128-bit integer sums of the
+    FP64 weights psi_r^2, rounded once) bit for bit against the host
+    restatement tests/zz_model.py, for every pair."""
+    import zz_model
+    env = envs(N)
+    b = ed.Basis(env, mag)
+    states = zz_model.basis_states(N, N // 2 + mag)
+    assert len(states) == b.size
+    rng = np.random.default_rng(N + mag)
+    psi = rng.standard_normal(b.size)
+    if wide:
+        psi *= np.exp2(-rng.integers(0, 40, b.size))
+        psi[0] = 1.2
+    else:
+        psi *= np.sqrt(1.5) / np.linalg.norm(psi)  # sum of weights away from a power of two
+    got = ed.SzSz(env, b).AllPairs(psi).real
+    pairs = [(i, j) for i in range(N) for j in range(i, N)]
+    want = zz_model.szsz(states, psi, pairs)
+    for (i, j), w in zip(pairs, want):
+        assert got[i, j].view(np.uint64) == np.float64(w).view(np.uint64), (i, j, got[i, j], w)
+        assert got[j, i] == got[i, j]
+
+
 def test_correlations_nonfinite_state(ed, envs):
     """A real state with a NaN entry: S.S and S^z S^z fall back to the general
     kernel (their fixed-point sums need a finite norm) and every pair is NaN,
