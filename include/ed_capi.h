@@ -332,11 +332,11 @@ int ed_batch_set_restart_arithmetic(ed_batch* bt, int mode);
  *      (src/spinOperators/correlation.cpp:38-299) --------------------------- */
 /* out[p] = ExpectVal(op, i_p, j_p, psi) for npairs pairs, 16 per pass over
  * the basis (PETSc VecDot convention: sum_s psi_s * conj((O psi)_s)).  For a
- * real psi (every imaginary part zero, as the solver's eigenvectors) and
- * op = ED_OP_SZSZ or ED_OP_SISJ, the S^z S^z part is an exact integer sum of
- * the FP64 weights psi_s^2 rounded once, and the call holds a temporary copy
- * of the real parts (8 * dim bytes) on the device; without room for it, or
- * for a non-finite psi, the general FP64 kernel runs instead. */
+ * real psi (every imaginary part zero, as the solver's eigenvectors), the
+ * S^z S^z part and the one-site sums are exact integer sums of the FP64
+ * weights psi_s^2 rounded once, and the call holds a temporary copy of the
+ * real parts (8 * dim bytes) on the device; without room for it, or for a
+ * non-finite psi, the general FP64 kernel runs instead. */
 int ed_expect_pairs(const ed_basis* b, int op, const ed_cplx* psi_dev, const int32_t* pairs_host,
                     int64_t npairs, ed_cplx* out_host);
 /* All N*N <S_i.S_j> (op = ED_OP_SISJ) into out_host[i*N + j]. */

@@ -137,8 +137,9 @@ static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t
   return ED_OK;
 }
 
-// Real psi and a symmetric operator (S^z_i S^z_j or S_i.S_j): the solver's
-// eigenvectors and the all-pairs measurement.  The general kernel above spends
+// Real psi (the solver's eigenvectors) and any of the four operators; the
+// all-pairs measurement.  For a real psi, <S+_i S-_j> = <S-_i S+_j> = F_ij,
+// the flip sum below, for i != j.  The general kernel above spends
 // about four FP64 operations per pair and row, and GB300 runs FP64 at a small
 // fraction of its other rates: at N=30 that pass is FP64-bound.  Here two
 // kernels share a pass of up to MEAS_GR pairs:
@@ -146,8 +147,9 @@ static int expect_g(const ed_basis* b, int op, const double2* psi, const int32_t
 //    w_r = psi_r^2 (FP64, as the general kernel forms it): each w_r becomes a
 //    128-bit integer at the scale 2^(124 - e), sum_r w_r < 2^e, which holds
 //    every w_r above 2^(e - 72) exactly; the sums T = sum_r w_r and, per pair,
-//    A = sum over antiparallel rows of w_r are exact integer sums, and
-//    0.25 (T - 2 A) is rounded once at the end;
+//    A = sum over antiparallel rows of w_r (for i == j: over the rows with
+//    spin i up, for S+S- and S-S+) are exact integer sums, and 0.25 (T - 2 A)
+//    is rounded once at the end;
 //  * k_expect_flip_r, the flip part (S+_i S-_j + S-_i S+_j) / 2: it pairs
 //    every antiparallel row with its partner r' = rank(s ^ m) (an
 //    involution), so it equals the sum over the rows with bit i set and bit j
@@ -199,7 +201,8 @@ __device__ __forceinline__ void ed_fx128(double w, int S, unsigned long long& lo
 }
 
 // partial[(3 g) nblk + blk] and [(3 g + 1) nblk + blk]: lo and hi words of
-// pair g's antiparallel sum A; partial[(3 MEAS_GR) nblk + blk], [(3 MEAS_GR
+// pair g's sum A over its antiparallel rows (i != j) or over the rows with
+// spin i up (i == j); partial[(3 MEAS_GR) nblk + blk], [(3 MEAS_GR
 // + 1) nblk + blk]: the block's T (int64 bits in the double array).
 __global__ void __launch_bounds__(256, 2) k_expect_zz_r(const uint32_t* __restrict__ states,
                                                      const double* __restrict__ pr, int64_t dim, int S,
@@ -230,7 +233,9 @@ __global__ void __launch_bounds__(256, 2) k_expect_zz_r(const uint32_t* __restri
     for (int g = 0; g < MEAS_GR; ++g) {
       if (g < pm.n) {
         const uint32_t m = pm.m[g], bits = s & m;
-        if (bits != 0u && bits != m) ed_add128(alo[g], ahi[g], wlo, whi);  // antiparallel
+        // i != j: antiparallel rows; i == j: rows with the spin up
+        const bool hit = ((pm.diag >> g) & 1u) ? bits != 0u : (bits != 0u && bits != m);
+        if (hit) ed_add128(alo[g], ahi[g], wlo, whi);
       }
     }
   }
@@ -363,11 +368,15 @@ __device__ __forceinline__ double ed_i128_to_double(unsigned long long lo, unsig
   return neg ? -d : d;
 }
 
-// out[g]: 0.25 (T - 2 A_g) 2^-S, plus (S.S) the flip sum, or for i == j
-// another 0.5 T 2^-S; block partials summed in a fixed order (the integer
-// ones exactly).  One block per pair.
-__global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk, const PairMasks pm, int sisj,
+// out[g] from the block partials, summed in a fixed order (the integer ones
+// exactly), F the flip sum, all integer sums times 2^-S:
+//   S^z S^z: 0.25 (T - 2 A) (i != j), 0.25 T (i == j);
+//   S.S:     0.25 (T - 2 A) + F (i != j), 0.75 T (i == j);
+//   S+S-:    F (i != j), A (i == j: n_i);  S-S+: F (i != j), T - A (1 - n_i).
+// One block per pair.
+__global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk, const PairMasks pm, int op,
                                     double inv_scale, double* __restrict__ out) {
+  const bool flips = op != ED_OP_SZSZ;
   const int g = blockIdx.x;
   if (g >= pm.n) return;
   __shared__ double shd[256];
@@ -375,7 +384,7 @@ __global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk
   double a = 0.0;
   unsigned long long alo = 0ull, ahi = 0ull, tlo = 0ull, thi = 0ull;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-    if (sisj) a += partial[(size_t)(3 * g + 2) * nblk + b];
+    if (flips) a += partial[(size_t)(3 * g + 2) * nblk + b];
     ed_add128(alo, ahi, (unsigned long long)__double_as_longlong(partial[(size_t)(3 * g) * nblk + b]),
               (unsigned long long)__double_as_longlong(partial[(size_t)(3 * g + 1) * nblk + b]));
     ed_add128(tlo, thi, (unsigned long long)__double_as_longlong(partial[(size_t)(3 * MEAS_GR) * nblk + b]),
@@ -402,16 +411,30 @@ __global__ void k_expect_sym_finish(const double* __restrict__ partial, int nblk
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    // Z = T - 2 A (|Z| <= T < 2^124)
-    unsigned long long zlo = sh[2][0], zhi = sh[3][0];
-    unsigned long long nlo = ~sh[0][0], nhi = ~sh[1][0];
+    const bool diag = (pm.diag >> g) & 1u;
+    const unsigned long long Alo = sh[0][0], Ahi = sh[1][0], Tlo = sh[2][0], Thi = sh[3][0];
+    unsigned long long nlo = ~Alo, nhi = ~Ahi;
     ed_add128(nlo, nhi, 1ull, 0ull);  // -A
-    ed_add128(zlo, zhi, nlo, nhi);
-    ed_add128(zlo, zhi, nlo, nhi);
-    double v = 0.25 * (ed_i128_to_double(zlo, zhi) * inv_scale);
-    if (sisj) {
-      if ((pm.diag >> g) & 1u) v += 0.5 * (ed_i128_to_double(sh[2][0], sh[3][0]) * inv_scale);  // (S+S- + S-S+) / 2
-      else v += shd[0];
+    double v;
+    if (op == ED_OP_SZSZ || op == ED_OP_SISJ) {
+      unsigned long long zlo = Tlo, zhi = Thi;  // Z = T - 2 A, |Z| <= T < 2^124 (A = 0 counts for i == j)
+      if (!diag) {
+        ed_add128(zlo, zhi, nlo, nhi);
+        ed_add128(zlo, zhi, nlo, nhi);
+      }
+      v = 0.25 * (ed_i128_to_double(zlo, zhi) * inv_scale);
+      if (op == ED_OP_SISJ) {
+        if (diag) v += 0.5 * (ed_i128_to_double(Tlo, Thi) * inv_scale);  // (S+S- + S-S+) / 2
+        else v += shd[0];
+      }
+    } else if (!diag) {
+      v = shd[0];
+    } else if (op == ED_OP_SPSM) {
+      v = ed_i128_to_double(Alo, Ahi) * inv_scale;
+    } else {
+      unsigned long long dlo = Tlo, dhi = Thi;
+      ed_add128(dlo, dhi, nlo, nhi);  // T - A
+      v = ed_i128_to_double(dlo, dhi) * inv_scale;
     }
     out[g] = v;
   }
@@ -474,7 +497,7 @@ static int expect_sym_r(const ed_basis* b, const double2* psi, const int32_t* pa
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) {
       ctx->kernels++;
-      if (OP == ED_OP_SISJ) {
+      if (OP != ED_OP_SZSZ) {
         k_expect_flip_r<<<nblk, 256, smem, ctx->stream>>>(b->d_states, pr, dim, b->d_lin_t0, b->d_lin_t1,
                                                           b->lin_w0, pm, ctx->d_red, nblk);
         le = cudaGetLastError();
@@ -482,8 +505,7 @@ static int expect_sym_r(const ed_basis* b, const double2* psi, const int32_t* pa
       }
     }
     if (le == cudaSuccess) {
-      k_expect_sym_finish<<<pm.n, 256, 0, ctx->stream>>>(ctx->d_red, nblk, pm, OP == ED_OP_SISJ ? 1 : 0, inv_scale,
-                                                         out_dev);
+      k_expect_sym_finish<<<pm.n, 256, 0, ctx->stream>>>(ctx->d_red, nblk, pm, OP, inv_scale, out_dev);
       le = cudaGetLastError();
     }
     if (le == cudaSuccess) {
@@ -509,9 +531,15 @@ int ed_launch_expect_pairs(const ed_basis* b, int op, const double2* psi, const 
                            double2* out) {
   bool real = false;
   ED_TRY(ed_is_real(b->ctx, psi, b->dim, &real));
-  if (real && (op == ED_OP_SISJ || op == ED_OP_SZSZ)) {
-    const int rc = op == ED_OP_SISJ ? expect_sym_r<ED_OP_SISJ>(b, psi, pairs, np, out)
-                                    : expect_sym_r<ED_OP_SZSZ>(b, psi, pairs, np, out);
+  if (real) {
+    int rc = ED_ENOTSUP;
+    switch (op) {
+      case ED_OP_SZSZ: rc = expect_sym_r<ED_OP_SZSZ>(b, psi, pairs, np, out); break;
+      case ED_OP_SPSM: rc = expect_sym_r<ED_OP_SPSM>(b, psi, pairs, np, out); break;
+      case ED_OP_SMSP: rc = expect_sym_r<ED_OP_SMSP>(b, psi, pairs, np, out); break;
+      case ED_OP_SISJ: rc = expect_sym_r<ED_OP_SISJ>(b, psi, pairs, np, out); break;
+      default: break;
+    }
     if (rc != ED_ENOMEM && rc != ED_ENOTSUP) return rc;  // else the general kernel below
   }
   if (real) return expect_g<MEAS_GR, true>(b, op, psi, pairs, np, out);
