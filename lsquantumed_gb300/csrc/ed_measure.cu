@@ -24,7 +24,9 @@ struct PairGroup {
 // Groups of up to G pairs per pass over the basis.  Ranks of flipped states
 // come from the basis's two-table rank (T0 in shared memory, T1 through the
 // read-only cache).  REAL: psi has zero imaginary parts (then every result is
-// real and only real parts are accumulated; G = 16 pairs share one pass).
+// real and only real parts are accumulated; G = 16 pairs share one pass); a
+// real psi normally takes k_expect_zz_r / k_expect_flip_r below, and this
+// form only when their compact copy does not fit or psi is not finite.
 template <int G, bool REAL>
 __global__ void __launch_bounds__(256) k_expect(const uint32_t* __restrict__ states, const double2* __restrict__ psi,
                                                 int64_t dim, const uint16_t* __restrict__ t0,
